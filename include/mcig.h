@@ -1,0 +1,165 @@
+/*
+ * mcig.h -- C ABI of the GB300-native Monte Carlo integrator (libmcigpu.so).
+ *
+ * The entry points mirror the reference's integrator facade mci::MCI
+ * (include/mci/MCIntegrator.hpp:93-225 of DCM-UPB/MCIntegratorPlusPlus): one
+ * opaque handle stands for an MCI object, except that it holds `nchains`
+ * independent Markov chains that run on the GPU, one chain per thread.  With
+ * nchains == 1 and MCIG_PREC_FP64 the arithmetic is the reference's.  With
+ * several chains, integrate() combines the per-chain averages and errors the
+ * way MPIMCI::integrate combines ranks (src/MPIMCI.cpp:85-92): mean of the
+ * averages, sqrt(sum of squared errors)/nchains.
+ *
+ * Conventions
+ *  - Every call returns an mcig_status; mcig_last_error() gives the message
+ *    of the last failure in the calling thread.  Where the reference throws
+ *    std::invalid_argument / std::domain_error / std::runtime_error, the
+ *    matching MCIG_ERR_* code is returned and nothing is changed.
+ *  - Host pointers only.  Arrays of per-chain vectors are [nchains][ndim]
+ *    row-major (one reference walker per row).
+ *  - All device work of a handle runs on one CUDA stream (mcig_get_stream);
+ *    calls return after that work has finished.
+ *  - User sampling functions and observables are device functors chosen by
+ *    kind code + parameter vector (include/mcig_types.h).
+ */
+#ifndef MCIG_H
+#define MCIG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "mcig_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mcig_mci mcig_mci;
+
+/* last error message of the calling thread ("" if none) */
+const char *mcig_last_error(void);
+/* library version string */
+const char *mcig_version(void);
+
+/* MCI::MCI(int ndim) (MCIntegrator.cpp:624-649): unbound domain, uniform all-move
+ * with step 0.05, target acceptance 0.5, NfindMRT2Iterations -50,
+ * NdecorrelationSteps -10000, every chain at x = 0.  `device` is the CUDA
+ * ordinal; `precision` an mcig_precision. */
+int mcig_create(int ndim, int64_t nchains, int device, int precision, mcig_mci **out);
+int mcig_destroy(mcig_mci *h);
+int mcig_get_ndim(const mcig_mci *h, int *ndim);
+int64_t mcig_get_nchains(const mcig_mci *h);
+int mcig_set_precision(mcig_mci *h, int precision);
+/* stream the handle's work is queued on (cudaStream_t as void*) */
+void *mcig_get_stream(const mcig_mci *h);
+
+/* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
+ * from counter (step, c).  */
+int mcig_set_seed(mcig_mci *h, uint64_t seed);
+
+/* MCI::setX (:594-604): x is [nchains][ndim], or [ndim] broadcast when n == 1 */
+int mcig_set_x(mcig_mci *h, const double *x, int64_t n);
+int mcig_get_x(mcig_mci *h, double *x /* [nchains][ndim] */);
+/* MCI::centerX (MCIntegrator.hpp:105): domain centre (0 in the unbound domain) */
+int mcig_center_x(mcig_mci *h);
+
+/* MCI::setMRT2Step (:557-579) for every chain; getMRT2Step (:581-585) of chain 0
+ * (0 for a non-existing index, as the reference) */
+int mcig_set_mrt2step(mcig_mci *h, double step);
+int mcig_set_mrt2step_i(mcig_mci *h, int i, double step);
+int mcig_get_mrt2step(const mcig_mci *h, int64_t chain, int i, double *step);
+int mcig_get_nstepsizes(const mcig_mci *h, int *n);
+/* per-chain step sizes, [nchains][nstepsizes] */
+int mcig_get_mrt2steps(const mcig_mci *h, double *steps);
+
+/* MCI::setTargetAcceptanceRate / setNfindMRT2Iterations / setNdecorrelationSteps
+ * (MCIntegrator.hpp:113-123): N < 0 automatic with at most |N|, 0 off, N > 0 fixed */
+int mcig_set_target_acceptance_rate(mcig_mci *h, double rate);
+int mcig_set_nfind_mrt2_iterations(mcig_mci *h, int n);
+int mcig_set_ndecorrelation_steps(mcig_mci *h, int64_t n);
+
+/* MCI::setTrialMove(SRRDType, veclen, ntypes, typeEnds) (MCIntegrator.cpp:431-446)
+ * and setTrialMove(MoveType) (:423-429).  movetype MCIG_MOVE_ALL ignores
+ * veclen; MCIG_MOVE_VEC uses veclen >= 1; MCIG_MOVE_MULTISTEP installs the
+ * default MultiStepMove(ndim) (MultiStepMove.hpp:49-52).  Only the uniform and
+ * Gaussian distributions run on the device (MCIG_ERR_UNSUPPORTED otherwise). */
+int mcig_set_trial_move(mcig_mci *h, int movetype, int srrd, int veclen, int ntypes, const int *typeEnds);
+/* MultiStepMove(ndim, nsteps) with sub-move SRRDVecMove(ndim/veclen, veclen, step)
+ * (MultiStepMove.hpp:40-52, src/MultiStepMove.cpp:6-75) */
+int mcig_set_multistep_move(mcig_mci *h, int nsteps, int sub_srrd, int sub_veclen, double sub_step);
+/* MultiStepMove::addSamplingFunction (src/MultiStepMove.cpp:61-67) */
+int mcig_multistep_add_pdf(mcig_mci *h, int kind, const double *params, int nparams);
+
+/* MCI::addSamplingFunction / popSamplingFunction / clearSamplingFunctions (MCIntegrator.hpp:181-184) */
+int mcig_add_sampling_function(mcig_mci *h, int kind, const double *params, int nparams);
+int mcig_pop_sampling_function(mcig_mci *h);
+int mcig_clear_sampling_functions(mcig_mci *h);
+int mcig_get_npdf(const mcig_mci *h, int *n);
+
+/* MCI::addObservable(obs, blocksize, nskip, flag_equil, EstimatorType) (MCIntegrator.cpp:451-465);
+ * blocksize 0 -> SimpleAccumulator, 1 -> FullAccumulator, >1 -> BlockAccumulator
+ * (Factories.hpp:24-38).  mcig_add_observable_default applies the defaults of
+ * addObservable(obs, blocksize, nskip) (MCIntegrator.hpp:161-164). */
+int mcig_add_observable(mcig_mci *h, int kind, const double *params, int nparams, int blocksize, int nskip,
+                        int flag_equil, int estimator);
+int mcig_add_observable_default(mcig_mci *h, int kind, const double *params, int nparams, int blocksize, int nskip);
+int mcig_pop_observable(mcig_mci *h);
+int mcig_clear_observables(mcig_mci *h);
+int mcig_get_nobs(const mcig_mci *h, int *n);
+int mcig_get_nobsdim(const mcig_mci *h, int *n);
+/* FullAccumulator samples stored as float (32) or double (64, default) */
+int mcig_set_full_storage(mcig_mci *h, int bits);
+
+/* MCI::setIRange (:398-408): orthorhombic periodic box; resetDomain (:390-396) */
+int mcig_set_irange(mcig_mci *h, const double *lbounds, const double *ubounds);
+int mcig_reset_domain(mcig_mci *h);
+
+/* MCI::integrate (MCIntegrator.cpp:43-82).  average/error have getNObsDim()
+ * entries (combined over chains).  chain_avg / chain_err, if not NULL, receive
+ * [nchains][nobsdim] per-chain results. */
+int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double *error, int do_find_mrt2step,
+                   int do_decorrelation);
+int mcig_get_chain_results(const mcig_mci *h, double *chain_avg, double *chain_err);
+/* MCI::getAcceptanceRate (:587-592) of the last sampling run, over all chains */
+int mcig_get_acceptance_rate(const mcig_mci *h, double *rate);
+/* per-chain accepted / rejected counts of the last sampling run */
+int mcig_get_counts(const mcig_mci *h, int64_t *acc, int64_t *rej);
+
+/* Accumulator data of observable o after the last integrate, in the
+ * reference's per-chain layout [nchains][nstore][nobs] (AccumulatorInterface::getData,
+ * AccumulatorInterface.hpp:81).  n receives the element count when data is NULL. */
+int mcig_get_obs_data(const mcig_mci *h, int o, double *data, int64_t *n);
+
+/* Replay mode (tests): consume recorded distribution outputs instead of
+ * Philox draws.  tape is [nchains][stride] in the order the reference draws
+ * them; lens the per-chain lengths.  Requires MCIG_PREC_FP64.  NULL switches
+ * back to Philox. */
+int mcig_set_replay(mcig_mci *h, const double *tape, int64_t stride, const int64_t *lens);
+/* record the accept/reject decision of every main-sampling step into a
+ * [nsteps][nchains] byte array readable with mcig_get_accept_bits */
+int mcig_set_record_accepts(mcig_mci *h, int on);
+int mcig_get_accept_bits(const mcig_mci *h, uint8_t *bits, int64_t *nsteps);
+
+/* Estimators on host arrays x[n][ndim] computed on the device
+ * (src/Estimators.cpp:36-293, src/MJBlocker.cpp:19-154).  `estimator` is an
+ * mcig_estimator.  MCIG_PREC_FP64 arithmetic, reference operation order. */
+int mcig_estimate(int device, int estimator, int64_t n, int ndim, const double *x, double *average, double *error);
+
+/* Accumulator of one observable driven by a recorded walk (test/ut1 pattern):
+ * xs[nsteps][ndim] walker positions after each step, accepted[nsteps] flags.
+ * data receives nstore*nobs values (AccumulatorInterface.cpp:31-122). */
+int mcig_accumulate_walk(int device, int obs_kind, const double *params, int nparams, int ndim, int blocksize,
+                         int nskip, int64_t nsteps, const double *xs, const uint8_t *accepted, double *data,
+                         int64_t *ndata);
+
+/* Device-side timing of the last integrate (milliseconds per phase:
+ * calibration, burn-in, sampling, estimation) and the number of kernels it launched. */
+int mcig_get_last_timings(const mcig_mci *h, double *ms4, int64_t *nlaunches);
+
+/* Philox4x32-10 block (for known-answer tests of the device generator) */
+int mcig_philox_block(int device, const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,5 @@
+"""GB300-native Monte Carlo integrator: the hot path of MCIntegrator++'s
+MCI::integrate (Metropolis sampling, accumulators, estimators) as sm_103a CUDA
+kernels behind the C ABI of include/mcig.h (libmcigpu.so)."""
+from .mci import *  # noqa: F401,F403
+from .mci import MCI, estimate, accumulate_walk, philox_block  # noqa: F401

@@ -1,0 +1,78 @@
+"""Build libmcigpu.so (the C ABI of include/mcig.h) for sm_103a with nvcc.
+
+Translation units are compiled in parallel into mcintegratorplusplus_gb300/_build/ and linked
+into mcintegratorplusplus_gb300/_build/libmcigpu.so (CUDA runtime linked statically).  Units
+holding reference-order double arithmetic are compiled with -fmad=false.
+
+    python -m mcintegratorplusplus_gb300.build [--force]
+"""
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libmcigpu.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# unit -> extra flags
+UNITS = {
+    "mcig_capi": ["-fmad=false"],
+    "sample_generic_f64": ["-fmad=false"],
+    "sample_generic_f32": [],
+    "sample_fast_f32": [],
+    "mcig_noalloc": ["-fmad=false"],
+}
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return "nvcc"
+
+
+def _deps():
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    files += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
+    return max(os.path.getmtime(f) for f in files)
+
+
+def _compile(unit, flags, verbose):
+    src = os.path.join(CSRC, unit + ".cu")
+    obj = os.path.join(BUILD, unit + ".o")
+    cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + flags + \
+        ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    with open(os.path.join(BUILD, unit + ".log"), "w") as f:
+        f.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s" % (unit, r.stderr[-4000:]))
+    if verbose:
+        print("compiled", unit)
+    return obj
+
+
+def build(force=False, verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > _deps():
+        return LIB
+    units = {u: f for u, f in UNITS.items() if os.path.exists(os.path.join(CSRC, u + ".cu"))}
+    with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), units.items()))
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = [_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + r.stderr[-4000:])
+    os.replace(tmp, LIB)
+    if verbose:
+        print("linked", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)

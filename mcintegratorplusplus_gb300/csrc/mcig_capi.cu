@@ -1,0 +1,1284 @@
+// mcig_capi.cu -- the C ABI of include/mcig.h: host orchestration of MCI::integrate
+// (reference src/MCIntegrator.cpp:43-82) over the device kernels.
+//
+// Compiled with -fmad=false: the estimator kernels in this unit follow the
+// reference's double operation order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mcig.h"
+#include "mcig_common.cuh"
+#include "mcig_estimators.cuh"
+#include "mcig_launchers.h"
+
+// ------------------------------------------------------------------------
+// errors
+// ------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int set_err(int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) { return set_err(MCIG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); } \
+    } while (0)
+
+extern "C" const char *mcig_last_error(void) { return g_err.c_str(); }
+extern "C" const char *mcig_version(void) { return "mcig 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------------------
+// device buffer helper
+// ------------------------------------------------------------------------
+template <class T> struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        if (count <= n && p) { return MCIG_OK; }
+        release();
+        if (count == 0) { return MCIG_OK; }
+        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        if (e != cudaSuccess) { p = nullptr; n = 0; return set_err(MCIG_ERR_CUDA, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e)); }
+        n = count;
+        return MCIG_OK;
+    }
+    void release()
+    {
+        if (p) { cudaFree(p); }
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct PdfDef {
+    int kind;
+    std::vector<double> params;
+};
+
+struct ObsDef {
+    int kind;
+    std::vector<double> params;
+    int nv, blocksize, nskip, flag_equil, estimator, acc;
+};
+
+struct mcig_mci {
+    int ndim;
+    int64_t nchains;
+    int device;
+    int prec;
+    cudaStream_t stream = nullptr;
+    uint64_t seed = 0;
+    // trial move
+    int movetype = MCIG_MOVE_ALL, srrd = MCIG_SRRD_UNIFORM, veclen = 0, ntypes = 1;
+    int typeEnds[MCIG_MAXTYPES] = {0, 0, 0, 0};
+    int ms_nsteps = 0, ms_srrd = 0, ms_veclen = 1;
+    std::vector<PdfDef> ms_pdfs, pdfs;
+    std::vector<ObsDef> obs;
+    int periodic = 0;
+    std::vector<double> lb, ub;
+    double target = 0.5;
+    int nfind = -50;
+    int64_t ndecorr = -10000;
+    int full32 = 0;
+    // device chain state
+    DBuf<double> x, step;
+    DBuf<uint64_t> ctr;
+    DBuf<int64_t> tpos, nacc, nrej, tape_len;
+    DBuf<int> status;
+    DBuf<double> params, lbub, stepmax;
+    DBuf<float> fblob;
+    DBuf<double> tape;
+    int64_t tape_stride = 0;
+    bool replay = false;
+    // observable data of the last integrate
+    std::vector<DBuf<char>> obsdata;
+    std::vector<int64_t> obs_nstore;
+    DBuf<double> est_avg, est_err, scratch;
+    DBuf<uint8_t> active;
+    // results
+    std::vector<double> chain_avg, chain_err;
+    std::vector<int64_t> h_nacc, h_nrej;
+    bool record = false;
+    DBuf<uint8_t> bits;
+    int64_t bits_steps = 0;
+    double ms[4] = {0, 0, 0, 0};
+    int64_t launches = 0;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+static int nobsdim(const mcig_mci *h)
+{
+    int n = 0;
+    for (auto &o : h->obs) { n += o.nv; }
+    return n;
+}
+
+static int maxd_bucket(int ndim)
+{
+    const int b[] = {4, 8, 16, 32, 64};
+    for (int v : b) {
+        if (ndim <= v) { return v; }
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------------
+// validation of functor parameters (mirrors the oracle's pdf_init / obs_init)
+// ------------------------------------------------------------------------
+static int check_pdf(int ndim, int kind, const double *params, int np)
+{
+    switch (kind) {
+    case MCIG_PDF_GAUSS_SUM:
+    case MCIG_PDF_GAUSS:
+    case MCIG_PDF_EXP: return MCIG_OK;
+    case MCIG_PDF_GAUSS_PREC:
+        if (np != ndim * ndim) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "GAUSS_PREC needs ndim*ndim params"); }
+        return MCIG_OK;
+    case MCIG_PDF_GAUSS_BLOCK:
+        if (np != 3) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "GAUSS_BLOCK needs [b0,b1,w]"); }
+        if ((int)params[0] < 0 || (int)params[1] > ndim || (int)params[0] >= (int)params[1] || !(params[2] > 0.)) {
+            return set_err(MCIG_ERR_INVALID_ARGUMENT, "GAUSS_BLOCK bad block");
+        }
+        return MCIG_OK;
+    case MCIG_PDF_GAUSS_MIX: {
+        if (np < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "GAUSS_MIX needs params"); }
+        const int nc = (int)params[0];
+        if (nc < 1 || nc > 16 || np != 1 + nc + 2 * nc * ndim) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "GAUSS_MIX bad param count (1..16 components)"); }
+        return MCIG_OK;
+    }
+    default: return set_err(MCIG_ERR_INVALID_ARGUMENT, "unknown sampling function kind %d", kind);
+    }
+}
+
+static int obs_nvals(int ndim, int kind, const double *params, int np, int *nv)
+{
+    switch (kind) {
+    case MCIG_OBS_X2SUM:
+    case MCIG_OBS_X2MEAN:
+    case MCIG_OBS_POLYNOM:
+    case MCIG_OBS_GAUSSX2: *nv = 1; return MCIG_OK;
+    case MCIG_OBS_CONST:
+        if (np < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "CONST needs its value"); }
+        *nv = 1;
+        return MCIG_OK;
+    case MCIG_OBS_XND:
+    case MCIG_OBS_X2: *nv = ndim; return MCIG_OK;
+    case MCIG_OBS_X2BLOCK: {
+        if (np < 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "X2BLOCK needs [nb, b0..b_nb]"); }
+        const int nb = (int)params[0];
+        if (nb < 1 || np != nb + 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "X2BLOCK bad param count"); }
+        for (int k = 0; k < nb; ++k) {
+            if ((int)params[1 + k] < 0 || (int)params[2 + k] > ndim || (int)params[1 + k] > (int)params[2 + k]) {
+                return set_err(MCIG_ERR_INVALID_ARGUMENT, "X2BLOCK bad bounds");
+            }
+        }
+        *nv = nb;
+        return MCIG_OK;
+    }
+    default: return set_err(MCIG_ERR_INVALID_ARGUMENT, "unknown observable kind %d", kind);
+    }
+}
+
+// ------------------------------------------------------------------------
+// creation / state
+// ------------------------------------------------------------------------
+static int upload_state_defaults(mcig_mci *h)
+{
+    const size_t nc = (size_t)h->nchains;
+    int rc;
+    if ((rc = h->x.alloc(nc * h->ndim)) || (rc = h->step.alloc(nc * MCIG_MAXTYPES)) || (rc = h->ctr.alloc(nc)) ||
+        (rc = h->tpos.alloc(nc)) || (rc = h->nacc.alloc(nc)) || (rc = h->nrej.alloc(nc)) || (rc = h->status.alloc(1))) {
+        return rc;
+    }
+    CK(cudaMemsetAsync(h->x.p, 0, nc * h->ndim * sizeof(double), h->stream));
+    CK(cudaMemsetAsync(h->ctr.p, 0, nc * sizeof(uint64_t), h->stream));
+    CK(cudaMemsetAsync(h->tpos.p, 0, nc * sizeof(int64_t), h->stream));
+    CK(cudaMemsetAsync(h->nacc.p, 0, nc * sizeof(int64_t), h->stream));
+    CK(cudaMemsetAsync(h->nrej.p, 0, nc * sizeof(int64_t), h->stream));
+    return MCIG_OK;
+}
+
+static int fill_steps(mcig_mci *h, double v)
+{
+    std::vector<double> s((size_t)h->nchains * MCIG_MAXTYPES, v);
+    CK(cudaMemcpyAsync(h->step.p, s.data(), s.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MCIG_OK;
+}
+
+extern "C" int mcig_create(int ndim, int64_t nchains, int device, int precision, mcig_mci **out)
+{
+    if (!out) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "out is NULL"); }
+    *out = nullptr;
+    if (ndim < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[ProtoFunctionInterface] Number of dimensions must be at least 1."); }
+    if (maxd_bucket(ndim) == 0) { return set_err(MCIG_ERR_UNSUPPORTED, "ndim %d exceeds the device maximum of 64", ndim); }
+    if (nchains < 1 || nchains > (int64_t)1 << 30) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "nchains must be in [1, 2^30]"); }
+    if (precision < MCIG_PREC_FP64 || precision > MCIG_PREC_FP32_ACC64) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "bad precision"); }
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "device %d not present (%d devices)", device, ndev); }
+    CK(cudaSetDevice(device));
+    mcig_mci *h = new mcig_mci();
+    h->ndim = ndim;
+    h->nchains = nchains;
+    h->device = device;
+    h->prec = precision;
+    h->typeEnds[0] = ndim;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return set_err(MCIG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    for (auto &ev : h->ev) { cudaEventCreate(&ev); }
+    int rc = upload_state_defaults(h);
+    if (!rc) { rc = fill_steps(h, 0.05); } // DEFAULT_MRT2STEP (Factories.hpp:145)
+    if (rc) {
+        mcig_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_destroy(mcig_mci *h)
+{
+    if (!h) { return MCIG_OK; }
+    cudaSetDevice(h->device);
+    if (h->stream) { cudaStreamSynchronize(h->stream); }
+    h->x.release(); h->step.release(); h->ctr.release(); h->tpos.release(); h->nacc.release(); h->nrej.release();
+    h->tape_len.release(); h->status.release(); h->params.release(); h->lbub.release(); h->stepmax.release();
+    h->fblob.release(); h->tape.release(); h->est_avg.release(); h->est_err.release(); h->scratch.release();
+    h->active.release(); h->bits.release();
+    for (auto &b : h->obsdata) { b.release(); }
+    for (auto &ev : h->ev) { if (ev) { cudaEventDestroy(ev); } }
+    if (h->stream) { cudaStreamDestroy(h->stream); }
+    delete h;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_ndim(const mcig_mci *h, int *ndim) { *ndim = h->ndim; return MCIG_OK; }
+extern "C" int64_t mcig_get_nchains(const mcig_mci *h) { return h->nchains; }
+extern "C" void *mcig_get_stream(const mcig_mci *h) { return (void *)h->stream; }
+
+extern "C" int mcig_set_precision(mcig_mci *h, int precision)
+{
+    if (precision < MCIG_PREC_FP64 || precision > MCIG_PREC_FP32_ACC64) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "bad precision"); }
+    if (h->replay && precision != MCIG_PREC_FP64) { return set_err(MCIG_ERR_UNSUPPORTED, "replay needs MCIG_PREC_FP64"); }
+    h->prec = precision;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_seed(mcig_mci *h, uint64_t seed)
+{
+    h->seed = seed;
+    cudaSetDevice(h->device);
+    CK(cudaMemsetAsync(h->ctr.p, 0, (size_t)h->nchains * sizeof(uint64_t), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MCIG_OK;
+}
+
+static void apply_domain_host(const mcig_mci *h, double *x)
+{
+    if (!h->periodic) { return; }
+    for (int i = 0; i < h->ndim; ++i) {
+        while (x[i] < h->lb[i]) { x[i] += h->ub[i] - h->lb[i]; }
+        while (x[i] > h->ub[i]) { x[i] -= h->ub[i] - h->lb[i]; }
+    }
+}
+
+extern "C" int mcig_set_x(mcig_mci *h, const double *x, int64_t n)
+{
+    if (!x) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "x is NULL"); }
+    if (n != 1 && n != h->nchains) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "set_x: n must be 1 or nchains"); }
+    cudaSetDevice(h->device);
+    const size_t nc = (size_t)h->nchains;
+    std::vector<double> t(nc * h->ndim);
+    std::vector<double> v(h->ndim);
+    for (size_t c = 0; c < nc; ++c) {
+        const double *src = x + (n == 1 ? 0 : c * h->ndim);
+        std::copy(src, src + h->ndim, v.begin());
+        apply_domain_host(h, v.data()); // MCI::setX applies the domain (MCIntegrator.cpp:594-604)
+        for (int i = 0; i < h->ndim; ++i) { t[(size_t)i * nc + c] = v[i]; }
+    }
+    CK(cudaMemcpyAsync(h->x.p, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_x(mcig_mci *h, double *x)
+{
+    cudaSetDevice(h->device);
+    const size_t nc = (size_t)h->nchains;
+    std::vector<double> t(nc * h->ndim);
+    CK(cudaMemcpyAsync(t.data(), h->x.p, t.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t c = 0; c < nc; ++c) {
+        for (int i = 0; i < h->ndim; ++i) { x[c * h->ndim + i] = t[(size_t)i * nc + c]; }
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_center_x(mcig_mci *h)
+{
+    std::vector<double> v(h->ndim, 0.);
+    if (h->periodic) { // DomainInterface::getCenter (DomainInterface.hpp:36-40)
+        for (int i = 0; i < h->ndim; ++i) { v[i] = h->lb[i] + 0.5 * (h->ub[i] - h->lb[i]); }
+    }
+    return mcig_set_x(h, v.data(), 1);
+}
+
+static int nstepsizes(const mcig_mci *h) { return h->ntypes; }
+
+extern "C" int mcig_set_mrt2step(mcig_mci *h, double v)
+{
+    cudaSetDevice(h->device);
+    return fill_steps(h, v);
+}
+
+extern "C" int mcig_set_mrt2step_i(mcig_mci *h, int i, double v)
+{
+    if (i < 0 || i >= nstepsizes(h)) {
+        std::printf("[MCI::setMRT2Step] Warning: Tried to set non-existing MRT2step index.\n");
+        return MCIG_OK;
+    }
+    cudaSetDevice(h->device);
+    std::vector<double> s((size_t)h->nchains, v);
+    CK(cudaMemcpyAsync(h->step.p + (size_t)i * h->nchains, s.data(), s.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_nstepsizes(const mcig_mci *h, int *n) { *n = nstepsizes(h); return MCIG_OK; }
+
+extern "C" int mcig_get_mrt2step(const mcig_mci *h, int64_t chain, int i, double *v)
+{
+    if (chain < 0 || chain >= h->nchains) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "chain out of range"); }
+    if (i < 0 || i >= nstepsizes(h)) { *v = 0.; return MCIG_OK; }
+    cudaSetDevice(h->device);
+    CK(cudaMemcpyAsync(v, h->step.p + (size_t)i * h->nchains + chain, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_mrt2steps(const mcig_mci *h, double *steps)
+{
+    cudaSetDevice(h->device);
+    const size_t nc = (size_t)h->nchains;
+    const int ns = nstepsizes(h);
+    std::vector<double> t(nc * ns);
+    CK(cudaMemcpyAsync(t.data(), h->step.p, t.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t c = 0; c < nc; ++c) {
+        for (int i = 0; i < ns; ++i) { steps[c * ns + i] = t[(size_t)i * nc + c]; }
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_target_acceptance_rate(mcig_mci *h, double r) { h->target = r; return MCIG_OK; }
+extern "C" int mcig_set_nfind_mrt2_iterations(mcig_mci *h, int n) { h->nfind = n; return MCIG_OK; }
+extern "C" int mcig_set_ndecorrelation_steps(mcig_mci *h, int64_t n) { h->ndecorr = n; return MCIG_OK; }
+
+extern "C" int mcig_set_multistep_move(mcig_mci *h, int nsteps, int sub_srrd, int sub_veclen, double sub_step)
+{
+    if (sub_srrd != MCIG_SRRD_UNIFORM && sub_srrd != MCIG_SRRD_GAUSSIAN) {
+        return set_err(MCIG_ERR_UNSUPPORTED, "only uniform and Gaussian sub-moves run on the device");
+    }
+    if (sub_veclen < 1 || h->ndim % sub_veclen != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[MCI::setTrialMove] MCI's number of walkers must be a multiple of passed veclen."); }
+    if (nsteps < 0 || nsteps > 65534) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "multi-step move: nsteps must be in [0, 65534]"); }
+    h->movetype = MCIG_MOVE_MULTISTEP;
+    h->ms_nsteps = nsteps;
+    h->ms_srrd = sub_srrd;
+    h->ms_veclen = sub_veclen;
+    h->ms_pdfs.clear();
+    h->ntypes = 1;
+    h->typeEnds[0] = h->ndim;
+    cudaSetDevice(h->device);
+    return fill_steps(h, sub_step);
+}
+
+extern "C" int mcig_set_trial_move(mcig_mci *h, int movetype, int srrd, int veclen, int ntypes, const int *typeEnds)
+{
+    if (movetype == MCIG_MOVE_MULTISTEP) { return mcig_set_multistep_move(h, h->ndim, MCIG_SRRD_UNIFORM, 1, 0.05); }
+    if (movetype != MCIG_MOVE_ALL && movetype != MCIG_MOVE_VEC) { return set_err(MCIG_ERR_DOMAIN, "[createMoveDefault] Unhandled MoveType enumerator."); }
+    if (srrd < MCIG_SRRD_UNIFORM || srrd > MCIG_SRRD_FISHER) { return set_err(MCIG_ERR_DOMAIN, "[createSRRDAllMove] Unhandled SRRDType enumerator."); }
+    if (srrd != MCIG_SRRD_UNIFORM && srrd != MCIG_SRRD_GAUSSIAN) {
+        return set_err(MCIG_ERR_UNSUPPORTED, "only the uniform and Gaussian distributions run on the device");
+    }
+    if (ntypes < 1) { ntypes = 1; }
+    if (ntypes > MCIG_MAXTYPES) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d step-size types on the device", MCIG_MAXTYPES); }
+    const int vl = (movetype == MCIG_MOVE_VEC) ? std::max(1, veclen) : 0;
+    if (vl > 0 && h->ndim % vl != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[MCI::setTrialMove] MCI's number of walkers must be a multiple of passed veclen."); }
+    if (ntypes > 1 && !typeEnds) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[TypedMoveInterface] When ntypes>1, passed typeEnds must not be null."); }
+    if (ntypes > 1 && vl > 0) {
+        for (int i = 0; i < ntypes; ++i) {
+            if (typeEnds[i] % vl != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[SRRDVecMove] All type end indices must be multiples of vector length."); }
+        }
+    }
+    h->movetype = (vl > 0) ? MCIG_MOVE_VEC : MCIG_MOVE_ALL;
+    h->srrd = srrd;
+    h->veclen = vl;
+    h->ntypes = ntypes;
+    for (int i = 0; i < MCIG_MAXTYPES; ++i) { h->typeEnds[i] = (ntypes > 1 && i < ntypes) ? typeEnds[i] : h->ndim; }
+    cudaSetDevice(h->device);
+    return fill_steps(h, 0.05);
+}
+
+extern "C" int mcig_multistep_add_pdf(mcig_mci *h, int kind, const double *params, int nparams)
+{
+    if (h->movetype != MCIG_MOVE_MULTISTEP) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "no multi-step move is set"); }
+    if ((int)h->ms_pdfs.size() >= MCIG_MAXPDF) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d sub-sampling functions", MCIG_MAXPDF); }
+    int rc = check_pdf(h->ndim, kind, params, nparams);
+    if (rc) { return rc; }
+    h->ms_pdfs.push_back(PdfDef{kind, std::vector<double>(params, params + std::max(nparams, 0))});
+    return MCIG_OK;
+}
+
+extern "C" int mcig_add_sampling_function(mcig_mci *h, int kind, const double *params, int nparams)
+{
+    if ((int)h->pdfs.size() >= MCIG_MAXPDF) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d sampling functions", MCIG_MAXPDF); }
+    int rc = check_pdf(h->ndim, kind, params, nparams);
+    if (rc) { return rc; }
+    h->pdfs.push_back(PdfDef{kind, std::vector<double>(params, params + std::max(nparams, 0))});
+    return MCIG_OK;
+}
+
+extern "C" int mcig_pop_sampling_function(mcig_mci *h)
+{
+    if (!h->pdfs.empty()) { h->pdfs.pop_back(); }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_clear_sampling_functions(mcig_mci *h)
+{
+    h->pdfs.clear();
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_npdf(const mcig_mci *h, int *n) { *n = (int)h->pdfs.size(); return MCIG_OK; }
+
+extern "C" int mcig_add_observable(mcig_mci *h, int kind, const double *params, int nparams, int blocksize, int nskip,
+                                   int flag_equil, int estimator)
+{
+    if ((int)h->obs.size() >= MCIG_MAXOBS) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d observables", MCIG_MAXOBS); }
+    blocksize = std::max(0, blocksize);
+    nskip = std::max(1, nskip);
+    if (flag_equil && estimator == MCIG_EST_NOOP) {
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "[MCI::addObservable] Requested automatic observable equilibration requires estimator with error calculation.");
+    }
+    if (estimator < MCIG_EST_NOOP || estimator > MCIG_EST_MJBLOCKER) { return set_err(MCIG_ERR_DOMAIN, "[createEstimator] Unhandled estimator enumerator."); }
+    int nv = 0;
+    int rc = obs_nvals(h->ndim, kind, params, nparams, &nv);
+    if (rc) { return rc; }
+    int maxnv = 2 * maxd_bucket(h->ndim) + 8;
+    if (nobsdim(h) + nv > maxnv) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d observable values for ndim %d", maxnv, h->ndim); }
+    ObsDef o;
+    o.kind = kind;
+    o.params.assign(params, params + std::max(nparams, 0));
+    o.nv = nv;
+    o.blocksize = blocksize;
+    o.nskip = nskip;
+    o.flag_equil = flag_equil ? 1 : 0;
+    o.estimator = estimator;
+    o.acc = (blocksize == 0) ? MCIG_ACC_SIMPLE : (blocksize == 1 ? MCIG_ACC_FULL : MCIG_ACC_BLOCK);
+    h->obs.push_back(o);
+    return MCIG_OK;
+}
+
+extern "C" int mcig_add_observable_default(mcig_mci *h, int kind, const double *params, int nparams, int blocksize, int nskip)
+{
+    // addObservable(obs, blocksize, nskip) -> flag_equil = blocksize > 0,
+    // flag_correlated = blocksize == 1, selectEstimatorType (Factories.hpp:56-66)
+    const int bs = std::max(0, blocksize);
+    const int est = (bs == 1) ? MCIG_EST_CORRELATED : (bs > 0 ? MCIG_EST_UNCORRELATED : MCIG_EST_NOOP);
+    return mcig_add_observable(h, kind, params, nparams, blocksize, nskip, bs > 0, est);
+}
+
+extern "C" int mcig_pop_observable(mcig_mci *h)
+{
+    if (!h->obs.empty()) { h->obs.pop_back(); }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_clear_observables(mcig_mci *h)
+{
+    h->obs.clear();
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_nobs(const mcig_mci *h, int *n) { *n = (int)h->obs.size(); return MCIG_OK; }
+extern "C" int mcig_get_nobsdim(const mcig_mci *h, int *n) { *n = nobsdim(h); return MCIG_OK; }
+
+extern "C" int mcig_set_full_storage(mcig_mci *h, int bits)
+{
+    if (bits != 32 && bits != 64) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "full storage must be 32 or 64 bits"); }
+    h->full32 = (bits == 32);
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_irange(mcig_mci *h, const double *lb, const double *ub)
+{
+    for (int i = 0; i < h->ndim; ++i) {
+        if (!(ub[i] > lb[i])) {
+            return set_err(MCIG_ERR_INVALID_ARGUMENT, "[OrthoPeriodicDomain::checkBounds] All upper bounds must be truly greater than their corresponding lower bounds.");
+        }
+    }
+    h->lb.assign(lb, lb + h->ndim);
+    h->ub.assign(ub, ub + h->ndim);
+    h->periodic = 1;
+    // MCI::setIRange applies the new domain to the walkers (MCIntegrator.cpp:398-408)
+    std::vector<double> x((size_t)h->nchains * h->ndim);
+    int rc = mcig_get_x(h, x.data());
+    if (rc) { return rc; }
+    return mcig_set_x(h, x.data(), h->nchains);
+}
+
+extern "C" int mcig_reset_domain(mcig_mci *h)
+{
+    h->periodic = 0;
+    h->lb.clear();
+    h->ub.clear();
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_replay(mcig_mci *h, const double *tape, int64_t stride, const int64_t *lens)
+{
+    cudaSetDevice(h->device);
+    if (!tape) {
+        h->replay = false;
+        return MCIG_OK;
+    }
+    if (h->prec != MCIG_PREC_FP64) { return set_err(MCIG_ERR_UNSUPPORTED, "replay needs MCIG_PREC_FP64"); }
+    if (stride < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "tape stride must be >= 1"); }
+    const size_t nc = (size_t)h->nchains;
+    int rc;
+    if ((rc = h->tape.alloc(nc * stride)) || (rc = h->tape_len.alloc(nc))) { return rc; }
+    for (size_t c = 0; c < nc; ++c) {
+        if (lens[c] < 0 || lens[c] > stride) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "tape length out of range"); }
+    }
+    CK(cudaMemcpyAsync(h->tape.p, tape, nc * stride * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->tape_len.p, lens, nc * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->tpos.p, 0, nc * sizeof(int64_t), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->tape_stride = stride;
+    h->replay = true;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_record_accepts(mcig_mci *h, int on)
+{
+    h->record = on != 0;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_accept_bits(const mcig_mci *h, uint8_t *bits, int64_t *nsteps)
+{
+    *nsteps = h->bits_steps;
+    if (bits && h->bits_steps > 0) {
+        cudaSetDevice(h->device);
+        CK(cudaMemcpyAsync(bits, h->bits.p, (size_t)h->bits_steps * h->nchains, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    return MCIG_OK;
+}
+
+// ------------------------------------------------------------------------
+// parameter upload
+// ------------------------------------------------------------------------
+// upper Cholesky factor U (P = U^T U) of a symmetric positive definite matrix
+static bool cholesky_upper(int n, const double *P, std::vector<double> &U)
+{
+    std::vector<double> L((size_t)n * n, 0.);
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j <= i; ++j) {
+            double s = P[i * n + j];
+            for (int k = 0; k < j; ++k) { s -= L[i * n + k] * L[j * n + k]; }
+            if (i == j) {
+                if (!(s > 0.)) { return false; }
+                L[i * n + i] = std::sqrt(s);
+            } else {
+                L[i * n + j] = s / L[j * n + j];
+            }
+        }
+    }
+    U.assign((size_t)n * n, 0.);
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) { U[i * n + j] = L[j * n + i]; }
+    }
+    return true;
+}
+
+static int build_pdf_desc(mcig_mci *h, const PdfDef &d, std::vector<double> &P, std::vector<float> &F, PdfDesc &out)
+{
+    const int nd = h->ndim;
+    memset(&out, 0, sizeof(out));
+    out.kind = d.kind;
+    out.poff = (int)P.size();
+    out.np = (int)d.params.size();
+    P.insert(P.end(), d.params.begin(), d.params.end());
+    if (d.kind == MCIG_PDF_GAUSS_BLOCK) {
+        out.b0 = (int)d.params[0];
+        out.b1 = (int)d.params[1];
+        out.c = 0.5 / (d.params[2] * d.params[2]);
+    }
+    if (d.kind == MCIG_PDF_GAUSS_MIX) { // per-component log normalisation appended after the parameters
+        const int nc = (int)d.params[0];
+        const double *w = d.params.data() + 1, *s = d.params.data() + 1 + nc + nc * nd;
+        for (int c = 0; c < nc; ++c) {
+            double l = std::log(w[c]) - 0.5 * nd * std::log(2.0 * M_PI);
+            for (int i = 0; i < nd; ++i) { l -= std::log(s[c * nd + i]); }
+            P.push_back(l);
+        }
+        out.foff = (int)F.size();
+        F.push_back((float)nc);
+        const double *m = d.params.data() + 1 + nc;
+        for (int c = 0; c < nc; ++c) {
+            F.push_back((float)P[P.size() - nc + c]);
+            for (int i = 0; i < nd; ++i) { F.push_back((float)m[c * nd + i]); }
+            for (int i = 0; i < nd; ++i) { F.push_back((float)(1.0 / s[c * nd + i])); }
+        }
+    }
+    if (d.kind == MCIG_PDF_GAUSS_PREC) {
+        std::vector<double> U;
+        if (!cholesky_upper(nd, d.params.data(), U)) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "GAUSS_PREC matrix is not positive definite"); }
+        out.foff = (int)F.size();
+        for (double v : U) { F.push_back((float)v); }
+    }
+    return MCIG_OK;
+}
+
+static int fill_common(mcig_mci *h, KParams &kp)
+{
+    memset(&kp, 0, sizeof(kp));
+    kp.ndim = h->ndim;
+    kp.nchains = (int)h->nchains;
+    kp.srrd = h->srrd;
+    kp.veclen = h->veclen;
+    kp.ntypes = h->ntypes;
+    for (int i = 0; i < MCIG_MAXTYPES; ++i) { kp.typeEnds[i] = h->typeEnds[i]; }
+    kp.ms_nsteps = h->ms_nsteps;
+    kp.ms_srrd = h->ms_srrd;
+    kp.ms_veclen = h->ms_veclen;
+    std::vector<double> P;
+    std::vector<float> F;
+    int rc;
+    kp.npdf = (int)h->pdfs.size();
+    for (int k = 0; k < kp.npdf; ++k) {
+        if ((rc = build_pdf_desc(h, h->pdfs[k], P, F, kp.pdf[k]))) { return rc; }
+    }
+    kp.ms_npdf = (int)h->ms_pdfs.size();
+    for (int k = 0; k < kp.ms_npdf; ++k) {
+        if ((rc = build_pdf_desc(h, h->ms_pdfs[k], P, F, kp.ms_pdf[k]))) { return rc; }
+    }
+    kp.nobs = (int)h->obs.size();
+    int voff = 0;
+    for (int o = 0; o < kp.nobs; ++o) {
+        const ObsDef &d = h->obs[o];
+        ObsDesc &od = kp.obs[o];
+        od.kind = d.kind;
+        od.nv = d.nv;
+        od.poff = (int)P.size();
+        if (d.kind == MCIG_OBS_GAUSSX2) {
+            P.push_back(1. / std::sqrt(M_PI * M_PI * M_PI) / 3.); // GaussXSquared::_normf (TestMCIFunctions.hpp:285)
+        } else {
+            P.insert(P.end(), d.params.begin(), d.params.end());
+        }
+        od.np = (int)d.params.size();
+        od.acc = d.acc;
+        od.nskip = d.nskip;
+        od.bs = d.blocksize;
+        od.voff = voff;
+        od.full32 = h->full32;
+        voff += d.nv;
+    }
+    kp.nobsdim = voff;
+    if (P.empty()) { P.push_back(0.); }
+    if ((rc = h->params.alloc(P.size()))) { return rc; }
+    CK(cudaMemcpyAsync(h->params.p, P.data(), P.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    kp.params = h->params.p;
+    if (!F.empty()) {
+        if ((rc = h->fblob.alloc(F.size()))) { return rc; }
+        CK(cudaMemcpyAsync(h->fblob.p, F.data(), F.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+        kp.fblob = h->fblob.p;
+        kp.fblob_len = (int)F.size();
+    }
+    kp.periodic = h->periodic;
+    if (h->periodic) {
+        std::vector<double> v(3 * (size_t)h->ndim);
+        for (int i = 0; i < h->ndim; ++i) {
+            v[i] = h->lb[i];
+            v[h->ndim + i] = h->ub[i];
+            v[2 * h->ndim + i] = 0.5 * (h->ub[i] - h->lb[i]);
+        }
+        if ((rc = h->lbub.alloc(v.size()))) { return rc; }
+        CK(cudaMemcpyAsync(h->lbub.p, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        kp.lb = h->lbub.p;
+        kp.ub = h->lbub.p + h->ndim;
+        kp.step_max_i = h->lbub.p + 2 * h->ndim;
+    }
+    // UnboundDomain::getSizes = 2*FLT_MAX, so the clamp is at FLT_MAX (UnboundDomain.hpp:34)
+    kp.step_max = 0.5 * (2. * (double)3.4028234663852886e+38);
+    kp.x = h->x.p;
+    kp.step = h->step.p;
+    kp.ctr = h->ctr.p;
+    kp.tpos = h->tpos.p;
+    kp.nacc = h->nacc.p;
+    kp.nrej = h->nrej.p;
+    kp.key0 = (uint32_t)h->seed;
+    kp.key1 = (uint32_t)(h->seed >> 32);
+    if (h->replay) {
+        kp.tape = h->tape.p;
+        kp.tape_stride = h->tape_stride;
+        kp.tape_len = h->tape_len.p;
+    }
+    kp.nfind = h->nfind;
+    kp.target = h->target;
+    kp.status = h->status.p;
+    return MCIG_OK;
+}
+
+static int launch(mcig_mci *h, const KParams &kp)
+{
+    mcig_launch_fn fn = mcig_generic_launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX);
+    if (!fn) { return set_err(MCIG_ERR_UNSUPPORTED, "no kernel for this configuration"); }
+    const int block = 128;
+    const int grid = (int)((h->nchains + block - 1) / block);
+    fn(kp, h->movetype, grid, block, (size_t)kp.fblob_len * sizeof(float), h->stream);
+    ++h->launches;
+    CK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+static int check_status(mcig_mci *h)
+{
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (st & 1) { return set_err(MCIG_ERR_RUNTIME, "replay tape exhausted"); }
+    return MCIG_OK;
+}
+
+// ------------------------------------------------------------------------
+// estimators
+// ------------------------------------------------------------------------
+static int run_estimator(mcig_mci *h, int est, const void *data, int is_float, int64_t n, int nv, int nchains,
+                         double *d_avg, double *d_err, int ldo, int off, DBuf<double> &scratch, cudaStream_t st,
+                         int64_t *launches)
+{
+    EstArgs a;
+    a.data = data;
+    a.is_float = is_float;
+    a.n = n;
+    a.nv = nv;
+    a.nchains = nchains;
+    a.avg = d_avg;
+    a.err = d_err;
+    a.ldo = ldo;
+    a.off = off;
+    a.scratch = nullptr;
+    a.one_d = (nv == 1);
+    const int64_t S = (int64_t)nv * nchains;
+    const int block = 128;
+    const int grid = (int)((S + block - 1) / block);
+    if (est == MCIG_EST_CORRELATED) { est = (n > 0 && (n & (n - 1)) == 0) ? MCIG_EST_MJBLOCKER : MCIG_EST_FCBLOCKER; }
+    switch (est) {
+    case MCIG_EST_NOOP: est_noop_kernel<<<grid, block, 0, st>>>(a); break;
+    case MCIG_EST_UNCORRELATED:
+        if (n < 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[UncorrelatedEstimator] n must be larger than 1"); }
+        est_uncorr_kernel<<<grid, block, 0, st>>>(a);
+        break;
+    case MCIG_EST_FCBLOCKER:
+        if (n < 50) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "FCBlockerEstimator: n must be >= 50"); }
+        est_fc_kernel<<<grid, block, 0, st>>>(a);
+        break;
+    case MCIG_EST_MJBLOCKER: {
+        if (n <= 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[MJBlocker] ndata must be a natural number."); }
+        if ((n & (n - 1)) != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[MJBlocker] ndata must be a power of two."); }
+        int rc = scratch.alloc((size_t)n * S);
+        if (rc) { return rc; }
+        a.scratch = scratch.p;
+        est_mj_kernel<<<grid, block, 0, st>>>(a);
+        break;
+    }
+    default: return set_err(MCIG_ERR_DOMAIN, "[createEstimator] Unhandled estimator enumerator.");
+    }
+    if (launches) { ++*launches; }
+    CK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+extern "C" int mcig_estimate(int device, int estimator, int64_t n, int ndim, const double *x, double *average, double *error)
+{
+    if (!x || !average || !error || ndim < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "bad arguments"); }
+    if (n < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "n must be >= 1"); }
+    CK(cudaSetDevice(device));
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    DBuf<double> d_x, d_out, scratch;
+    int rc = d_x.alloc((size_t)n * ndim);
+    if (!rc) { rc = d_out.alloc(2 * (size_t)ndim); }
+    if (!rc) {
+        // [n][ndim] with one chain is exactly the [n][nv][nchains] layout
+        cudaMemcpyAsync(d_x.p, x, (size_t)n * ndim * sizeof(double), cudaMemcpyHostToDevice, st);
+        rc = run_estimator(nullptr, estimator, d_x.p, 0, n, ndim, 1, d_out.p, d_out.p + ndim, ndim, 0, scratch, st, nullptr);
+    }
+    if (!rc) {
+        cudaMemcpyAsync(average, d_out.p, ndim * sizeof(double), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(error, d_out.p + ndim, ndim * sizeof(double), cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { rc = set_err(MCIG_ERR_CUDA, "estimate: %s", cudaGetErrorString(e)); }
+    }
+    d_x.release();
+    d_out.release();
+    scratch.release();
+    cudaStreamDestroy(st);
+    return rc;
+}
+
+// ------------------------------------------------------------------------
+// accumulators on a recorded walk
+// ------------------------------------------------------------------------
+__global__ void walk_accumulate_kernel(int kind, const double *params, int ndim, int nv, int acc, int bs, int nskip,
+                                       int64_t nsteps, const double *xs, const uint8_t *accepted, double *data)
+{
+    // AccumulatorInterface::accumulate with _processFull / _processOld (AccumulatorInterface.cpp:31-114)
+    // for one walk; a single thread walks the steps in order.
+    if (blockIdx.x != 0 || threadIdx.x != 0) { return; }
+    double vals[136];
+    for (int j = 0; j < nv; ++j) { vals[j] = 0.; }
+    int nchanged = ndim, skipidx = nskip - 1, bidx = 0;
+    int64_t storeidx = 0;
+    for (int64_t i = 0; i < nsteps; ++i) {
+        const double *x = xs + i * ndim;
+        bool store = false;
+        if (accepted[i] || nchanged > 0) {
+            nchanged = ndim;
+            if (++skipidx == nskip) {
+                skipidx = 0;
+                // observableFunction of the kind, reference operation order
+                switch (kind) {
+                case MCIG_OBS_X2SUM: { double s = 0.; for (int k = 0; k < ndim; ++k) { s = s + x[k] * x[k]; } vals[0] = s; break; }
+                case MCIG_OBS_XND: for (int k = 0; k < ndim; ++k) { vals[k] = x[k]; } break;
+                case MCIG_OBS_X2: for (int k = 0; k < ndim; ++k) { vals[k] = x[k] * x[k]; } break;
+                case MCIG_OBS_X2MEAN: { double s = x[0] * x[0]; for (int k = 1; k < ndim; ++k) { s = s + x[k] * x[k]; } vals[0] = s / ndim; break; }
+                case MCIG_OBS_CONST: vals[0] = params[0]; break;
+                case MCIG_OBS_POLYNOM: { double s = 0.; for (int k = 0; k < ndim; ++k) { s = s + x[k]; } vals[0] = s; break; }
+                default: break;
+                }
+                nchanged = 0;
+                store = true;
+            }
+        } else if (++skipidx == nskip) {
+            skipidx = 0;
+            store = true;
+        }
+        if (store) {
+            if (acc == MCIG_ACC_FULL) {
+                for (int j = 0; j < nv; ++j) { data[storeidx + j] = vals[j]; }
+                storeidx += nv;
+            } else if (acc == MCIG_ACC_SIMPLE) {
+                for (int j = 0; j < nv; ++j) { data[j] = data[j] + vals[j]; }
+            } else {
+                for (int j = 0; j < nv; ++j) { data[storeidx + j] = data[storeidx + j] + vals[j]; }
+                if (++bidx == bs) { bidx = 0; storeidx += nv; }
+            }
+        }
+    }
+    const int64_t naccu = 1 + (nsteps - 1) / nskip;
+    if (acc == MCIG_ACC_SIMPLE) {
+        const double normf = 1. / (double)naccu;
+        for (int j = 0; j < nv; ++j) { data[j] = data[j] * normf; }
+    } else if (acc == MCIG_ACC_BLOCK) {
+        const double normf = 1. / bs;
+        for (int64_t i = 0; i < (naccu / bs) * nv; ++i) { data[i] = data[i] * normf; }
+    }
+}
+
+extern "C" int mcig_accumulate_walk(int device, int obs_kind, const double *params, int nparams, int ndim, int blocksize,
+                                    int nskip, int64_t nsteps, const double *xs, const uint8_t *accepted, double *data,
+                                    int64_t *ndata)
+{
+    if (ndim < 1 || ndim > 64 || !xs || !accepted || !ndata) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "bad arguments"); }
+    int nv = 0;
+    int rc = obs_nvals(ndim, obs_kind, params, nparams, &nv);
+    if (rc) { return rc; }
+    if (obs_kind == MCIG_OBS_X2BLOCK || obs_kind == MCIG_OBS_GAUSSX2) { return set_err(MCIG_ERR_UNSUPPORTED, "observable kind not supported on a walk"); }
+    blocksize = std::max(0, blocksize);
+    nskip = std::max(1, nskip);
+    if (nsteps < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[AccumulatorInterface::allocate] Provided number of MC steps was < 1 ."); }
+    const int acc = (blocksize == 0) ? MCIG_ACC_SIMPLE : (blocksize == 1 ? MCIG_ACC_FULL : MCIG_ACC_BLOCK);
+    const int64_t naccu = 1 + (nsteps - 1) / nskip;
+    int64_t nstore = 1;
+    if (acc == MCIG_ACC_FULL) { nstore = naccu; }
+    if (acc == MCIG_ACC_BLOCK) {
+        if (naccu < blocksize) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[BlockAccumulator::allocate] Requested number of accumulations is smaller than the requested block size."); }
+        if (naccu % blocksize != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[BlockAccumulator::allocate] Requested number of accumulations is not a multiple of the requested block size."); }
+        nstore = naccu / blocksize;
+    }
+    *ndata = nstore * nv;
+    if (!data) { return MCIG_OK; }
+    CK(cudaSetDevice(device));
+    DBuf<double> d_xs, d_p, d_data;
+    DBuf<uint8_t> d_acc;
+    if ((rc = d_xs.alloc((size_t)nsteps * ndim)) || (rc = d_p.alloc(std::max(1, nparams))) ||
+        (rc = d_data.alloc((size_t)nstore * nv)) || (rc = d_acc.alloc((size_t)nsteps))) {
+        return rc;
+    }
+    CK(cudaMemcpy(d_xs.p, xs, (size_t)nsteps * ndim * sizeof(double), cudaMemcpyHostToDevice));
+    if (nparams > 0) { CK(cudaMemcpy(d_p.p, params, nparams * sizeof(double), cudaMemcpyHostToDevice)); }
+    CK(cudaMemcpy(d_acc.p, accepted, (size_t)nsteps, cudaMemcpyHostToDevice));
+    CK(cudaMemset(d_data.p, 0, (size_t)nstore * nv * sizeof(double)));
+    walk_accumulate_kernel<<<1, 32>>>(obs_kind, d_p.p, ndim, nv, acc, blocksize, nskip, nsteps, d_xs.p, d_acc.p, d_data.p);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(data, d_data.p, (size_t)nstore * nv * sizeof(double), cudaMemcpyDeviceToHost));
+    d_xs.release(); d_p.release(); d_data.release(); d_acc.release();
+    return MCIG_OK;
+}
+
+// ------------------------------------------------------------------------
+// integrate
+// ------------------------------------------------------------------------
+static int64_t min_stat(int ndim)
+{
+    const double d = std::sqrt(40000. * ndim);
+    return (int64_t)(d > 100. ? d : 100.); // MIN_STAT / MIN_NMC (MCIntegrator.cpp:107, :193)
+}
+
+static int alloc_obs_data(mcig_mci *h, const std::vector<ObsDef> &obs, int64_t nmc, std::vector<DBuf<char>> &bufs,
+                          std::vector<int64_t> &nstore, int full32)
+{
+    bufs.resize(obs.size());
+    nstore.assign(obs.size(), 0);
+    for (size_t o = 0; o < obs.size(); ++o) {
+        const ObsDef &d = obs[o];
+        const int64_t naccu = 1 + (nmc - 1) / d.nskip;
+        int64_t ns = 1;
+        size_t elem = sizeof(double);
+        if (d.acc == MCIG_ACC_FULL) {
+            ns = naccu;
+            if (full32) { elem = sizeof(float); }
+        } else if (d.acc == MCIG_ACC_BLOCK) {
+            ns = naccu / d.blocksize;
+        }
+        nstore[o] = ns;
+        int rc = bufs[o].alloc((size_t)ns * d.nv * h->nchains * elem);
+        if (rc) { return rc; }
+    }
+    return MCIG_OK;
+}
+
+static int validate_accumulators(const mcig_mci *h, int64_t nmc)
+{
+    for (auto &d : h->obs) { // BlockAccumulator::_allocate (BlockAccumulator.cpp:6-17)
+        if (d.acc != MCIG_ACC_BLOCK) { continue; }
+        const int64_t naccu = 1 + (nmc - 1) / d.nskip;
+        if (naccu < d.blocksize) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[BlockAccumulator::allocate] Requested number of accumulations is smaller than the requested block size."); }
+        if (naccu % d.blocksize != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[BlockAccumulator::allocate] Requested number of accumulations is not a multiple of the requested block size."); }
+    }
+    for (auto &d : h->obs) {
+        const int64_t ns = d.acc == MCIG_ACC_FULL ? 1 + (nmc - 1) / d.nskip : (d.acc == MCIG_ACC_BLOCK ? (1 + (nmc - 1) / d.nskip) / d.blocksize : 1);
+        int e = d.estimator;
+        if (e == MCIG_EST_CORRELATED) { e = (ns > 0 && (ns & (ns - 1)) == 0) ? MCIG_EST_MJBLOCKER : MCIG_EST_FCBLOCKER; }
+        if (e == MCIG_EST_UNCORRELATED && ns < 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[UncorrelatedEstimator] n must be larger than 1"); }
+        if (e == MCIG_EST_FCBLOCKER && ns < 50) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "FCBlockerEstimator: n must be >= 50"); }
+        if (e == MCIG_EST_MJBLOCKER && (ns & (ns - 1)) != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[MJBlocker] ndata must be a power of two."); }
+    }
+    return MCIG_OK;
+}
+
+// estimators of all observables -> per-chain avg/err (host vectors [nchains][nod])
+static int estimate_all(mcig_mci *h, const std::vector<ObsDef> &obs, const std::vector<DBuf<char>> &bufs,
+                        const std::vector<int64_t> &nstore, int full32, std::vector<double> &cavg, std::vector<double> &cerr)
+{
+    int nod = 0;
+    for (auto &o : obs) { nod += o.nv; }
+    const size_t nc = (size_t)h->nchains;
+    int rc;
+    if ((rc = h->est_avg.alloc(nc * std::max(nod, 1))) || (rc = h->est_err.alloc(nc * std::max(nod, 1)))) { return rc; }
+    int off = 0;
+    for (size_t o = 0; o < obs.size(); ++o) {
+        const int is_float = (obs[o].acc == MCIG_ACC_FULL && full32) ? 1 : 0;
+        rc = run_estimator(h, obs[o].estimator, bufs[o].p, is_float, nstore[o], obs[o].nv, (int)nc, h->est_avg.p,
+                           h->est_err.p, nod, off, h->scratch, h->stream, &h->launches);
+        if (rc) { return rc; }
+        off += obs[o].nv;
+    }
+    cavg.resize(nc * nod);
+    cerr.resize(nc * nod);
+    if (nod > 0) {
+        CK(cudaMemcpyAsync(cavg.data(), h->est_avg.p, nc * nod * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(cerr.data(), h->est_err.p, nc * nod * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return MCIG_OK;
+}
+
+// MCI::initialDecorrelation automatic mode (MCIntegrator.cpp:171-243), chain by chain:
+// a chain leaves the loop when its consecutive estimates agree within 2 sigma.
+static int auto_decorrelation(mcig_mci *h, KParams kp)
+{
+    std::vector<ObsDef> eq;
+    for (auto &o : h->obs) {
+        if (o.flag_equil) {
+            ObsDef e = o;
+            e.blocksize = 1;
+            e.nskip = 1;
+            e.acc = MCIG_ACC_FULL;
+            e.estimator = MCIG_EST_CORRELATED;
+            eq.push_back(e);
+        }
+    }
+    const int64_t MIN_NMC = min_stat(h->ndim);
+    const size_t nc = (size_t)h->nchains;
+    std::vector<DBuf<char>> bufs;
+    std::vector<int64_t> nstore;
+    int rc = alloc_obs_data(h, eq, MIN_NMC, bufs, nstore, 0);
+    if (rc) { return rc; }
+    if ((rc = h->active.alloc(nc))) { return rc; }
+    std::vector<uint8_t> act(nc, 1);
+    CK(cudaMemcpyAsync(h->active.p, act.data(), nc, cudaMemcpyHostToDevice, h->stream));
+    const KParams orig = kp;
+    kp.mode = KMODE_SAMPLE;
+    kp.nsteps = MIN_NMC;
+    kp.active = h->active.p;
+    kp.nobs = (int)eq.size();
+    int voff = 0;
+    for (int k = 0, o = 0; k < (int)h->obs.size(); ++k) {
+        if (!h->obs[k].flag_equil) { continue; }
+        ObsDesc od = orig.obs[k]; // kind and parameters of the observable, Full accumulator
+        od.acc = MCIG_ACC_FULL;
+        od.nskip = 1;
+        od.bs = 1;
+        od.voff = voff;
+        od.data = bufs[o].p;
+        od.nstore = nstore[o];
+        od.full32 = 0;
+        kp.obs[o] = od;
+        voff += eq[o].nv;
+        ++o;
+    }
+    kp.nobsdim = voff;
+    std::vector<double> oa, oe, na, ne;
+    if ((rc = launch(h, kp))) { return rc; }
+    if ((rc = estimate_all(h, eq, bufs, nstore, 0, oa, oe))) { return rc; }
+    const int nod = voff;
+    int64_t count = 0;
+    while (true) {
+        if ((rc = launch(h, kp))) { return rc; }
+        count += MIN_NMC;
+        if (count >= std::llabs(h->ndecorr)) { break; } // the reference warns here (:219-222)
+        if ((rc = estimate_all(h, eq, bufs, nstore, 0, na, ne))) { return rc; }
+        bool any = false;
+        for (size_t c = 0; c < nc; ++c) {
+            if (!act[c]) { continue; }
+            bool loop = false;
+            for (int i = 0; i < nod; ++i) {
+                const size_t k = c * nod + i;
+                if (std::fabs(oa[k] - na[k]) > 2 * std::sqrt(oe[k] * oe[k] + ne[k] * ne[k])) { loop = true; break; }
+            }
+            for (int i = 0; i < nod; ++i) {
+                oa[c * nod + i] = na[c * nod + i];
+                oe[c * nod + i] = ne[c * nod + i];
+            }
+            act[c] = loop ? 1 : 0;
+            any = any || loop;
+        }
+        if (!any) { break; }
+        CK(cudaMemcpyAsync(h->active.p, act.data(), nc, cudaMemcpyHostToDevice, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    for (auto &b : bufs) { b.release(); }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double *error, int do_find, int do_decorr)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    if (h->pdfs.empty() && !h->periodic) {
+        return set_err(MCIG_ERR_DOMAIN, "[MCI::integrate] Integrating over an infinite domain requires a sampling function.");
+    }
+    if (h->replay && h->prec != MCIG_PREC_FP64) { return set_err(MCIG_ERR_UNSUPPORTED, "replay needs MCIG_PREC_FP64"); }
+    int rc;
+    if (nmc > 0 && (rc = validate_accumulators(h, nmc))) { return rc; }
+    if (nmc > 0 && (!average || !error) && nobsdim(h) > 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "average/error are NULL"); }
+    CK(cudaSetDevice(h->device));
+    h->launches = 0;
+    for (double &m : h->ms) { m = 0.; }
+    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
+    KParams kp;
+    if ((rc = fill_common(h, kp))) { return rc; }
+    CK(cudaEventRecord(h->ev[0], h->stream));
+    // phase 1: MCI::findMRT2Step (only with a pdf; every move here has step sizes)
+    if (!h->pdfs.empty() && do_find && h->nfind != 0) {
+        KParams c = kp;
+        c.mode = KMODE_CALIB;
+        c.nsteps = min_stat(h->ndim);
+        if ((rc = launch(h, c))) { return rc; }
+    }
+    CK(cudaEventRecord(h->ev[1], h->stream));
+    // phase 2: MCI::initialDecorrelation
+    if (!h->pdfs.empty() && do_decorr) {
+        if (h->ndecorr > 0) {
+            KParams d = kp;
+            d.mode = KMODE_STEPS;
+            d.nsteps = h->ndecorr;
+            if ((rc = launch(h, d))) { return rc; }
+        } else if (h->ndecorr < 0) {
+            if ((rc = auto_decorrelation(h, kp))) { return rc; }
+        }
+    }
+    CK(cudaEventRecord(h->ev[2], h->stream));
+    if (nmc > 0) {
+        if ((rc = alloc_obs_data(h, h->obs, nmc, h->obsdata, h->obs_nstore, h->full32))) { return rc; }
+        KParams s = kp;
+        s.mode = KMODE_SAMPLE;
+        s.nsteps = nmc;
+        for (size_t o = 0; o < h->obs.size(); ++o) {
+            s.obs[o].data = h->obsdata[o].p;
+            s.obs[o].nstore = h->obs_nstore[o];
+        }
+        if (h->record) {
+            if ((rc = h->bits.alloc((size_t)nmc * h->nchains))) { return rc; }
+            s.bits = h->bits.p;
+            h->bits_steps = nmc;
+        }
+        if ((rc = launch(h, s))) { return rc; }
+    }
+    CK(cudaEventRecord(h->ev[3], h->stream));
+    if (nmc > 0) {
+        if ((rc = estimate_all(h, h->obs, h->obsdata, h->obs_nstore, h->full32, h->chain_avg, h->chain_err))) { return rc; }
+    }
+    CK(cudaEventRecord(h->ev[4], h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if ((rc = check_status(h))) { return rc; }
+    for (int k = 0; k < 4; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev[k], h->ev[k + 1]);
+        h->ms[k] = ms;
+    }
+    const size_t nc = (size_t)h->nchains;
+    h->h_nacc.resize(nc);
+    h->h_nrej.resize(nc);
+    CK(cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (nmc > 0) {
+        const int nod = nobsdim(h);
+        // MPIMCI::integrate reduction (src/MPIMCI.cpp:85-92), chains in order
+        for (int i = 0; i < nod; ++i) {
+            double sa = 0., se = 0.;
+            for (size_t c = 0; c < nc; ++c) {
+                sa += h->chain_avg[c * nod + i];
+                se += h->chain_err[c * nod + i] * h->chain_err[c * nod + i];
+            }
+            average[i] = sa / (double)nc;
+            error[i] = std::sqrt(se) / (double)nc;
+        }
+        if (h->pdfs.empty()) { // volume scaling (MCIntegrator.cpp:70-77)
+            double vol = 1.;
+            for (int i = 0; i < h->ndim; ++i) { vol *= (h->ub[i] - h->lb[i]); }
+            for (int i = 0; i < nod; ++i) {
+                average[i] *= vol;
+                error[i] *= vol;
+            }
+            for (size_t k = 0; k < h->chain_avg.size(); ++k) {
+                h->chain_avg[k] *= vol;
+                h->chain_err[k] *= vol;
+            }
+        }
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_chain_results(const mcig_mci *h, double *chain_avg, double *chain_err)
+{
+    if (chain_avg) { std::copy(h->chain_avg.begin(), h->chain_avg.end(), chain_avg); }
+    if (chain_err) { std::copy(h->chain_err.begin(), h->chain_err.end(), chain_err); }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_acceptance_rate(const mcig_mci *h, double *rate)
+{
+    int64_t a = 0, r = 0;
+    for (size_t c = 0; c < h->h_nacc.size(); ++c) {
+        a += h->h_nacc[c];
+        r += h->h_nrej[c];
+    }
+    *rate = (a > 0) ? (double)a / ((double)a + (double)r) : 0.;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_counts(const mcig_mci *h, int64_t *acc, int64_t *rej)
+{
+    std::copy(h->h_nacc.begin(), h->h_nacc.end(), acc);
+    std::copy(h->h_nrej.begin(), h->h_nrej.end(), rej);
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_obs_data(const mcig_mci *h, int o, double *data, int64_t *n)
+{
+    if (o < 0 || o >= (int)h->obsdata.size() || o >= (int)h->obs.size()) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "no data for observable %d", o); }
+    const ObsDef &d = h->obs[o];
+    const int64_t ns = h->obs_nstore[o];
+    const size_t nc = (size_t)h->nchains;
+    *n = ns * d.nv * (int64_t)nc;
+    if (!data) { return MCIG_OK; }
+    cudaSetDevice(h->device);
+    const bool f32 = (d.acc == MCIG_ACC_FULL && h->full32);
+    const size_t cnt = (size_t)ns * d.nv * nc;
+    std::vector<double> t(cnt);
+    if (f32) {
+        std::vector<float> tf(cnt);
+        CK(cudaMemcpy(tf.data(), h->obsdata[o].p, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < cnt; ++i) { t[i] = tf[i]; }
+    } else {
+        CK(cudaMemcpy(t.data(), h->obsdata[o].p, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    for (size_t c = 0; c < nc; ++c) {
+        for (int64_t i = 0; i < ns; ++i) {
+            for (int j = 0; j < d.nv; ++j) { data[(c * ns + i) * d.nv + j] = t[((size_t)i * d.nv + j) * nc + c]; }
+        }
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_last_timings(const mcig_mci *h, double *ms4, int64_t *nlaunches)
+{
+    for (int k = 0; k < 4; ++k) { ms4[k] = h->ms[k]; }
+    if (nlaunches) { *nlaunches = h->launches; }
+    return MCIG_OK;
+}
+
+__global__ void philox_block_kernel(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t *out)
+{
+    const P4 q = philox4x32_10(c0, c1, c2, c3, k0, k1);
+    out[0] = q.a; out[1] = q.b; out[2] = q.c; out[3] = q.d;
+}
+
+extern "C" int mcig_philox_block(int device, const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    CK(cudaSetDevice(device));
+    DBuf<uint32_t> d;
+    int rc = d.alloc(4);
+    if (rc) { return rc; }
+    philox_block_kernel<<<1, 1>>>(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1], d.p);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(out, d.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    d.release();
+    return MCIG_OK;
+}

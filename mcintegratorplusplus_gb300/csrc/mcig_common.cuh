@@ -1,0 +1,209 @@
+// mcig_common.cuh -- parameter block, Philox generator and draw helpers shared by the
+// sampling kernels (mcig_generic.cuh, mcig_fast.cuh); one chain per thread.
+//
+// A launch runs `nsteps` steps of MCI::sample (reference src/MCIntegrator.cpp:273-321)
+// for every chain: trial move (SRRDAllMove.hpp:67-80, SRRDVecMove.hpp:75-96,
+// src/MultiStepMove.cpp:6-47), domain (OrthoPeriodicDomain.cpp:38-61), product of
+// sampling-function acceptances (SamplingFunctionContainer.cpp:41-48), the
+// Metropolis test (MCIntegrator.cpp:343) and the accumulators
+// (AccumulatorInterface.cpp:31-114, Simple/Block/FullAccumulator.cpp), or the
+// step-size calibration loop of MCI::findMRT2Step (MCIntegrator.cpp:87-168).
+//
+// Memory layout (chain-minor so that a warp's accesses are coalesced):
+//   x[ndim][nchains], step[ntypes][nchains], Full data [nstore][nobs][nchains],
+//   Block data [nblocks][nobs][nchains], Simple data [nobs][nchains].
+//
+// Random numbers: Philox4x32-10 keyed by the seed; the block for draw group
+// (substep, tag, b) of step t of chain c has counter (t lo, t hi, c,
+// substep<<16 | tag<<12 | b), so every draw is addressable and a chain's stream
+// does not depend on the launch configuration.  Replay mode reads the
+// reference's recorded distribution outputs ("tape") in its draw order.
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+#include "../../include/mcig_types.h"
+
+#define MCIG_MAXPDF 4
+#define MCIG_MAXOBS 8
+#define MCIG_MAXTYPES 4
+#define MCIG_PERIODIC_MAXWRAP 64
+#define MCIG_MAXDIM 64
+
+enum { RNG_PHILOX = 0, RNG_TAPE = 1 };
+enum { KMODE_STEPS = 0, KMODE_SAMPLE = 1, KMODE_CALIB = 2 };
+
+struct PdfDesc {
+    int kind;
+    int poff;     // offset of the parameters in KParams::params (double) / the float blob
+    int np;
+    int b0, b1;   // GAUSS_BLOCK bounds
+    double c;     // GAUSS_BLOCK: 1/(2 w^2)
+    int foff;     // float path: offset of this pdf's data in the shared-memory blob
+};
+
+struct ObsDesc {
+    int kind;
+    int nv;       // number of values
+    int poff, np; // parameters (double) in KParams::params
+    int acc;      // mcig_accumulator
+    int nskip;
+    int bs;       // block size (Block)
+    int voff;     // offset of this observable's values in the accumulator arrays
+    void *data;   // device data (see layout above)
+    int64_t nstore;
+    int full32;   // Full data stored as float
+};
+
+struct KParams {
+    int ndim;
+    int nchains;
+    int64_t nsteps;     // steps of this launch (KMODE_STEPS / KMODE_SAMPLE), MIN_STAT (KMODE_CALIB)
+    int mode;
+    // trial move
+    int srrd, veclen, ntypes;
+    int typeEnds[MCIG_MAXTYPES];
+    int ms_nsteps, ms_srrd, ms_veclen, ms_npdf;
+    PdfDesc ms_pdf[MCIG_MAXPDF];
+    // sampling functions
+    int npdf;
+    PdfDesc pdf[MCIG_MAXPDF];
+    const double *params;   // all pdf / observable parameters (double)
+    const float *fblob;     // float path: pdf data copied into shared memory
+    int fblob_len;          // floats
+    // observables
+    int nobs;
+    int nobsdim;
+    ObsDesc obs[MCIG_MAXOBS];
+    // domain
+    int periodic;
+    const double *lb, *ub;
+    // chain state
+    double *x;
+    double *step;
+    uint64_t *ctr;          // Philox step counter per chain
+    int64_t *tpos;          // tape cursor per chain
+    int64_t *nacc, *nrej;   // counts of this launch (KMODE_CALIB: of the last iteration)
+    uint8_t *bits;          // optional [nsteps][nchains] accept record
+    const uint8_t *active;  // optional: chains with active[c] == 0 skip this launch
+    // random numbers
+    uint32_t key0, key1;
+    const double *tape;
+    int64_t tape_stride;
+    const int64_t *tape_len;
+    // calibration (MCI::findMRT2Step)
+    int nfind;
+    double target;
+    double step_max;        // 0.5 * domain size (same for every index in the unbound domain)
+    const double *step_max_i; // periodic: 0.5*(ub-lb) per index
+    // error reporting
+    int *status;
+};
+
+// ------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
+// ------------------------------------------------------------------------
+struct P4 { uint32_t a, b, c, d; };
+
+__device__ __forceinline__ P4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                            uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c0;
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0;
+        const uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return P4{c0, c1, c2, c3};
+}
+
+// Counter layout of one draw block: (step lo, step hi, chain, sub), with
+// sub = (substep << 16) | (tag << 12) | block.  substep is 0 for the outer
+// move and 1 + s for sub-step s of a MultiStepMove.
+enum { TAG_MOVE = 0, TAG_ACCEPT = 1, TAG_INDEX = 2 };
+
+struct PhiloxCtx {
+    uint32_t k0, k1, s0, s1, chain;
+    __device__ __forceinline__ P4 block(uint32_t substep, uint32_t tag, uint32_t b) const
+    {
+        return philox4x32_10(s0, s1, chain, (substep << 16) | (tag << 12) | b, k0, k1);
+    }
+};
+
+__device__ __forceinline__ float u01_f(uint32_t w) { return (float)(w >> 8) * 5.9604644775390625e-08f; }           // [0,1)
+__device__ __forceinline__ float u01_open0_f(uint32_t w) { return (float)((w >> 8) + 1u) * 5.9604644775390625e-08f; } // (0,1]
+__device__ __forceinline__ double u01_d(uint32_t hi, uint32_t lo)
+{
+    return (double)(((uint64_t)hi << 21) | (uint64_t)(lo >> 11)) * 1.1102230246251565e-16; // [0,1), 53 bits
+}
+
+// two standard normals from two uniforms (Box-Muller)
+__device__ __forceinline__ void box_muller_f(uint32_t w0, uint32_t w1, float &z0, float &z1)
+{
+    const float u = u01_open0_f(w0);
+    const float r = sqrtf(-2.0f * 0.69314718f * __log2f(u));
+    float s, c;
+    __sincosf(6.28318530717958648f * (u01_f(w1) - 0.5f), &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+
+__device__ __forceinline__ void box_muller_d(P4 q, double &z0, double &z1)
+{
+    const double u = 1.0 - u01_d(q.a, q.b); // (0,1]
+    const double r = sqrt(-2.0 * log(u));
+    double s, c;
+    sincospi(2.0 * u01_d(q.c, q.d), &s, &c);
+    z0 = r * c;
+    z1 = r * s;
+}
+
+// Move draws for coordinates [b*CPB, b*CPB+CPB) from one Philox block.
+// float: 4 coordinates per block (4 uniforms or 2 Box-Muller pairs).
+// double: 2 coordinates per block (2 uniforms of 53 bits or 1 pair).
+template <class R> struct Cpb { static constexpr int v = 4; };
+template <> struct Cpb<double> { static constexpr int v = 2; };
+
+template <class R>
+__device__ __forceinline__ void move_draws(P4 q, int gaussian, R *d /* Cpb<R>::v */);
+
+template <>
+__device__ __forceinline__ void move_draws<float>(P4 q, int gaussian, float *d)
+{
+    if (gaussian) {
+        box_muller_f(q.a, q.b, d[0], d[1]);
+        box_muller_f(q.c, q.d, d[2], d[3]);
+    } else {
+        d[0] = u01_f(q.a) * 2.0f - 1.0f;
+        d[1] = u01_f(q.b) * 2.0f - 1.0f;
+        d[2] = u01_f(q.c) * 2.0f - 1.0f;
+        d[3] = u01_f(q.d) * 2.0f - 1.0f;
+    }
+}
+
+template <>
+__device__ __forceinline__ void move_draws<double>(P4 q, int gaussian, double *d)
+{
+    if (gaussian) {
+        box_muller_d(q, d[0], d[1]);
+    } else {
+        d[0] = u01_d(q.a, q.b) * 2.0 - 1.0;
+        d[1] = u01_d(q.c, q.d) * 2.0 - 1.0;
+    }
+}
+
+template <class R>
+__device__ __forceinline__ R accept_draw(P4 q);
+template <>
+__device__ __forceinline__ float accept_draw<float>(P4 q) { return u01_f(q.a); }
+template <>
+__device__ __forceinline__ double accept_draw<double>(P4 q) { return u01_d(q.a, q.b); }
+

@@ -1,0 +1,642 @@
+// mcig_generic.cuh -- the general sampling kernel: every move, sampling function,
+// observable, accumulator and domain of the device path, with runtime loops over
+// the coordinates (walker arrays in thread-local memory, ndim <= MCIG_MAXDIM).
+//
+//   R = double: the reference's arithmetic and operation order.  The
+//     translation unit is compiled with -fmad=false, so no product is fused
+//     into an add (the reference is built for baseline x86-64, without FMA).
+//     With RNG_TAPE the kernel consumes the reference's recorded draws and
+//     reproduces its accept/reject sequence bit for bit.
+//   R = float: float walker, log-space Metropolis test; sums of the
+//     accumulators in float with Kahan compensation (KAHAN) or in double.
+//
+// The register-resident kernel for the common float configurations is in
+// mcig_fast.cuh; this one serves everything else.
+#pragma once
+
+#include "mcig_common.cuh"
+
+template <class R>
+__device__ __forceinline__ R step_of_rt(const KParams &p, const R *st, int i)
+{
+    int t = 0;
+    while (t + 1 < p.ntypes && i >= p.typeEnds[t]) { ++t; }
+    return st[t];
+}
+
+template <class R>
+__device__ __forceinline__ void periodic_wrap(R &v, double lb, double ub)
+{
+    // OrthoPeriodicDomain::applyDomain (OrthoPeriodicDomain.cpp:38-61).  The
+    // loops are bounded; a coordinate still outside after that is clamped.
+    const R L = (R)(ub - lb);
+    int n = 0;
+    while (v < (R)lb && n < MCIG_PERIODIC_MAXWRAP) { v += L; ++n; }
+    while (v > (R)ub && n < MCIG_PERIODIC_MAXWRAP) { v -= L; ++n; }
+    if (n >= MCIG_PERIODIC_MAXWRAP) { v = v < (R)lb ? (R)lb : (v > (R)ub ? (R)ub : v); }
+}
+
+// ------------------------------------------------------------------------
+// sampling functions, double (test/common/TestMCIFunctions.hpp arithmetic;
+// the same formulas as the oracle's pdf_* functions)
+// ------------------------------------------------------------------------
+__device__ __forceinline__ double proto_i_d(int kind, double v) { return kind == MCIG_PDF_GAUSS ? v * v : fabs(v); }
+
+// the single proto value of the scalar-proto kinds (GAUSS_SUM, GAUSS_PREC, GAUSS_BLOCK, GAUSS_MIX)
+static __device__ double pdf_proto_scalar_d(const KParams &p, const PdfDesc &d, const double *x)
+{
+    const int nd = p.ndim;
+    switch (d.kind) {
+    case MCIG_PDF_GAUSS_SUM: { // ThreeDimGaussianPDF::protoFunction (:134-137), any ndim
+        double s = x[0] * x[0];
+        for (int i = 1; i < nd; ++i) { s = s + x[i] * x[i]; }
+        return s;
+    }
+    case MCIG_PDF_GAUSS_PREC: {
+        const double *P = p.params + d.poff;
+        double q = 0.;
+        for (int i = 0; i < nd; ++i) {
+            double t = 0.;
+            for (int j = 0; j < nd; ++j) { t = t + P[i * nd + j] * x[j]; }
+            q = q + x[i] * t;
+        }
+        return 0.5 * q;
+    }
+    case MCIG_PDF_GAUSS_BLOCK: {
+        double s = 0.;
+        for (int i = d.b0; i < d.b1; ++i) { s = s + x[i] * x[i]; }
+        return s * d.c;
+    }
+    case MCIG_PDF_GAUSS_MIX: {
+        const double *pp = p.params + d.poff;
+        const int nc = (int)pp[0];
+        const double *m = pp + 1 + nc, *sg = pp + 1 + nc + nc * nd, *lc = pp + 1 + nc + 2 * nc * nd;
+        double e[16];
+        double mx = -INFINITY;
+        for (int c = 0; c < nc; ++c) {
+            double a = lc[c];
+            for (int i = 0; i < nd; ++i) {
+                const double z = (x[i] - m[c * nd + i]) / sg[c * nd + i];
+                a += -0.5 * (z * z);
+            }
+            e[c] = a;
+            mx = a > mx ? a : mx;
+        }
+        double sum = 0.;
+        for (int c = 0; c < nc; ++c) { sum += exp(e[c] - mx); }
+        return -(mx + log(sum));
+    }
+    default: return 0.;
+    }
+}
+
+// SamplingFunctionInterface::computeAcceptance (SamplingFunctionInterface.hpp:49-57).
+// xo: accepted position, xn: proposal, partial: nchanged < ndim with the changed
+// indices [lo, hi), po: cached scalar proto of xo, pn: scalar proto of xn (out).
+static __device__ double pdf_accept_d(const KParams &p, const PdfDesc &d, const double *xo, const double *xn, bool partial,
+                               int lo, int hi, double po, double &pn)
+{
+    const int nd = p.ndim;
+    if (d.kind == MCIG_PDF_GAUSS || d.kind == MCIG_PDF_EXP) {
+        if (partial) { // Gauss::updatedAcceptance (:181-189), ExpNDPDF::updatedAcceptance (:246-255)
+            double e = 0.;
+            for (int i = lo; i < hi; ++i) { e = e + (proto_i_d(d.kind, xn[i]) - proto_i_d(d.kind, xo[i])); }
+            return exp(-e);
+        }
+        double e = 0.; // Gauss::acceptanceFunction (:174-179)
+        for (int i = 0; i < nd; ++i) { e = e + proto_i_d(d.kind, xo[i]); }
+        double f = 0.;
+        for (int i = 0; i < nd; ++i) { f = f + proto_i_d(d.kind, xn[i]); }
+        e = e - f;
+        return exp(e);
+    }
+    pn = pdf_proto_scalar_d(p, d, xn);
+    return exp(-pn + po); // ThreeDimGaussianPDF::acceptanceFunction (:144-147)
+}
+
+// samplingFunction at the stored protos of x (SamplingFunctionContainer::getOldSamplingFunction)
+static __device__ double pdf_value_d(const KParams &p, const PdfDesc &d, const double *x, double po)
+{
+    if (d.kind == MCIG_PDF_GAUSS || d.kind == MCIG_PDF_EXP) {
+        double s = 0.;
+        for (int i = 0; i < p.ndim; ++i) { s = s + proto_i_d(d.kind, x[i]); }
+        return exp(-s);
+    }
+    return exp(-po);
+}
+
+// ------------------------------------------------------------------------
+// sampling functions, float (log density; parameter blob in shared memory)
+//   GAUSS_PREC : U[ndim][ndim], upper Cholesky factor of P (x^T P x = |U x|^2)
+//   GAUSS_MIX  : nc, then per component: log-normalisation, m[nd], 1/s[nd]
+// ------------------------------------------------------------------------
+static __device__ float pdf_logp_f(const KParams &p, const PdfDesc &d, const float *x, const float *blob)
+{
+    const int nd = p.ndim;
+    switch (d.kind) {
+    case MCIG_PDF_GAUSS_SUM:
+    case MCIG_PDF_GAUSS: {
+        float s = 0.f;
+        for (int i = 0; i < nd; ++i) { s = fmaf(x[i], x[i], s); }
+        return -s;
+    }
+    case MCIG_PDF_EXP: {
+        float s = 0.f;
+        for (int i = 0; i < nd; ++i) { s += fabsf(x[i]); }
+        return -s;
+    }
+    case MCIG_PDF_GAUSS_PREC: {
+        const float *U = blob + d.foff;
+        float q = 0.f;
+        for (int i = 0; i < nd; ++i) {
+            float t = 0.f;
+            for (int j = i; j < nd; ++j) { t = fmaf(U[i * nd + j], x[j], t); }
+            q = fmaf(t, t, q);
+        }
+        return -0.5f * q;
+    }
+    case MCIG_PDF_GAUSS_BLOCK: {
+        float s = 0.f;
+        for (int i = d.b0; i < d.b1; ++i) { s = fmaf(x[i], x[i], s); }
+        return -(float)d.c * s;
+    }
+    case MCIG_PDF_GAUSS_MIX: {
+        const float *b = blob + d.foff;
+        const int nc = (int)b[0];
+        const int stride = 1 + 2 * nd;
+        float e[16];
+        float mx = -INFINITY;
+        for (int c = 0; c < nc; ++c) {
+            const float *cb = b + 1 + c * stride;
+            float a = 0.f;
+            for (int i = 0; i < nd; ++i) {
+                const float z = (x[i] - cb[1 + i]) * cb[1 + nd + i];
+                a = fmaf(z, z, a);
+            }
+            a = fmaf(-0.5f, a, cb[0]);
+            e[c] = a;
+            mx = fmaxf(mx, a);
+        }
+        float sum = 0.f;
+        for (int c = 0; c < nc; ++c) { sum += __expf(e[c] - mx); }
+        return mx + __logf(sum);
+    }
+    default: return 0.f;
+    }
+}
+
+// ------------------------------------------------------------------------
+// observables (observableFunction of the test classes; oracle obs_eval)
+// ------------------------------------------------------------------------
+template <class R>
+__device__ void obs_eval(const KParams &p, const ObsDesc &o, const R *x, R *out)
+{
+    const int nd = p.ndim;
+    switch (o.kind) {
+    case MCIG_OBS_X2SUM: { // X2Sum (:424-430)
+        R s = (R)0;
+        for (int i = 0; i < nd; ++i) { s = s + x[i] * x[i]; }
+        out[0] = s;
+        break;
+    }
+    case MCIG_OBS_XND: // XND (:344-347)
+        for (int i = 0; i < nd; ++i) { out[i] = x[i]; }
+        break;
+    case MCIG_OBS_X2: // X2 (:445-450)
+        for (int i = 0; i < nd; ++i) { out[i] = x[i] * x[i]; }
+        break;
+    case MCIG_OBS_X2MEAN: { // XSquared (:269-272)
+        R s = x[0] * x[0];
+        for (int i = 1; i < nd; ++i) { s = s + x[i] * x[i]; }
+        out[0] = s / (R)nd;
+        break;
+    }
+    case MCIG_OBS_CONST: out[0] = (R)p.params[o.poff]; break; // Constval (:385-388)
+    case MCIG_OBS_POLYNOM: { // Polynom (:403-409)
+        R s = (R)0;
+        for (int i = 0; i < nd; ++i) { s = s + x[i]; }
+        out[0] = s;
+        break;
+    }
+    case MCIG_OBS_X2BLOCK: {
+        const double *pp = p.params + o.poff;
+        const int nb = (int)pp[0];
+        for (int k = 0; k < nb; ++k) {
+            R s = (R)0;
+            for (int i = (int)pp[1 + k]; i < (int)pp[2 + k]; ++i) { s = s + x[i] * x[i]; }
+            out[k] = s;
+        }
+        break;
+    }
+    case MCIG_OBS_GAUSSX2: { // GaussXSquared (:287-293); normf computed on the host
+        R r2 = x[0] * x[0];
+        for (int i = 1; i < nd; ++i) { r2 = r2 + x[i] * x[i]; }
+        out[0] = exp(-r2) * r2 * (R)p.params[o.poff];
+        break;
+    }
+    default: break;
+    }
+}
+
+// ------------------------------------------------------------------------
+// accumulator sums
+// ------------------------------------------------------------------------
+template <bool KAHAN> struct AccSlot;
+template <> struct AccSlot<false> {
+    double s;
+    __device__ __forceinline__ void zero() { s = 0.; }
+    __device__ __forceinline__ void add(double v) { s = s + v; }
+    __device__ __forceinline__ double get() const { return s; }
+};
+template <> struct AccSlot<true> {
+    float s, c;
+    __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
+    __device__ __forceinline__ void add(float v)
+    { // Kahan compensated summation
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
+// ------------------------------------------------------------------------
+// the sampler
+// ------------------------------------------------------------------------
+template <class R, int RNG, bool KAHAN>
+struct GenericSampler {
+    static constexpr bool EXACT = std::is_same<R, double>::value;
+    static constexpr int NV = 2 * MCIG_MAXDIM + 8;
+    using AccV = typename std::conditional<KAHAN, float, double>::type;
+
+    const KParams &p;
+    const int c;
+    const float *blob;
+    R x[MCIG_MAXDIM];
+    R xn[MCIG_MAXDIM];
+    R w[MCIG_MAXDIM];
+    R st[MCIG_MAXTYPES];
+    R lp[MCIG_MAXPDF]; // double: scalar proto per pdf at x; float: log density per pdf at x
+    PhiloxCtx ph;
+    uint64_t ctr;
+    int64_t tpos, tlen;
+    const double *tape;
+    int tape_err;
+
+    __device__ GenericSampler(const KParams &pp, int cc, const float *bl) : p(pp), c(cc), blob(bl), tape_err(0)
+    {
+        for (int i = 0; i < p.ndim; ++i) { x[i] = (R)p.x[(size_t)i * p.nchains + c]; }
+        for (int t = 0; t < p.ntypes; ++t) { st[t] = (R)p.step[(size_t)t * p.nchains + c]; }
+        ctr = 0;
+        tpos = 0;
+        tlen = 0;
+        tape = nullptr;
+        if constexpr (RNG == RNG_PHILOX) {
+            ctr = p.ctr[c];
+            ph.k0 = p.key0;
+            ph.k1 = p.key1;
+            ph.chain = (uint32_t)c;
+        } else {
+            tpos = p.tpos[c];
+            tlen = p.tape_len[c];
+            tape = p.tape + (size_t)c * p.tape_stride;
+        }
+    }
+
+    __device__ __forceinline__ double tape_next()
+    {
+        if (tpos < tlen) { return tape[tpos++]; }
+        tape_err = 1;
+        return 0.5;
+    }
+
+    __device__ __forceinline__ void begin_step()
+    {
+        if constexpr (RNG == RNG_PHILOX) {
+            ph.s0 = (uint32_t)ctr;
+            ph.s1 = (uint32_t)(ctr >> 32);
+        }
+    }
+    __device__ __forceinline__ void end_step()
+    {
+        if constexpr (RNG == RNG_PHILOX) { ++ctr; }
+    }
+
+    __device__ __forceinline__ R pdf_state(const PdfDesc &d, const R *pos)
+    {
+        if constexpr (EXACT) { return pdf_proto_scalar_d(p, d, pos); }
+        else { return pdf_logp_f(p, d, pos, blob); }
+    }
+
+    // ProtoFunctionInterface::initializeProtoValues (ProtoFunctionInterface.cpp:40-44)
+    __device__ void init_protos()
+    {
+        for (int k = 0; k < p.npdf; ++k) { lp[k] = pdf_state(p.pdf[k], x); }
+    }
+
+    // draw j of the move group (substep, TAG_MOVE): coordinate-indexed for Philox
+    __device__ __forceinline__ void move_group(int substep, int srrd, int b, R *d)
+    {
+        move_draws<R>(ph.block(substep, TAG_MOVE, b), srrd == MCIG_SRRD_GAUSSIAN, d);
+    }
+
+    // SRRDAllMove::trialMove (SRRDAllMove.hpp:67-80): xn = x + step(type(i)) * d_i
+    __device__ void all_move(int srrd)
+    {
+        constexpr int CPB = Cpb<R>::v;
+        R d[CPB];
+        for (int i = 0; i < p.ndim; ++i) {
+            R v;
+            if constexpr (RNG == RNG_TAPE) { v = (R)tape_next(); }
+            else {
+                if (i % CPB == 0) { move_group(0, srrd, i / CPB, d); }
+                v = d[i % CPB];
+            }
+            xn[i] = x[i];
+            xn[i] = xn[i] + step_of_rt<R>(p, st, i) * v;
+        }
+    }
+
+    // SRRDVecMove::trialMove (SRRDVecMove.hpp:75-96) from pos into xn; returns the first index
+    __device__ int vec_move(const R *pos, int substep, int srrd, int veclen)
+    {
+        const int nvecs = p.ndim / veclen;
+        int vidx;
+        if constexpr (RNG == RNG_TAPE) {
+            vidx = (int)tape_next();
+            vidx = vidx < 0 ? 0 : (vidx >= nvecs ? nvecs - 1 : vidx);
+        } else {
+            // multiply-shift index; bias below nvecs / 2^32
+            vidx = (int)__umulhi(ph.block(substep, TAG_INDEX, 0).a, (uint32_t)nvecs);
+        }
+        const int lo = vidx * veclen;
+        const R s = step_of_rt<R>(p, st, lo);
+        for (int i = 0; i < p.ndim; ++i) { xn[i] = pos[i]; }
+        constexpr int CPB = Cpb<R>::v;
+        R d[CPB];
+        for (int i = lo; i < lo + veclen; ++i) {
+            R v;
+            if constexpr (RNG == RNG_TAPE) { v = (R)tape_next(); }
+            else {
+                if (i == lo || i % CPB == 0) { move_group(substep, srrd, i / CPB, d); }
+                v = d[i % CPB];
+            }
+            xn[i] = xn[i] + s * v;
+        }
+        return lo;
+    }
+
+    __device__ __forceinline__ R accept_u(int substep)
+    {
+        if constexpr (RNG == RNG_TAPE) { return (R)tape_next(); }
+        else { return accept_draw<R>(ph.block(substep, TAG_ACCEPT, 0)); }
+    }
+
+    // MultiStepMove::trialMove (src/MultiStepMove.cpp:6-47): nested chain on the
+    // sub-pdfs; returns oldPDF/newPDF (double) or its log (float); xn = end point.
+    __device__ R multistep()
+    {
+        for (int i = 0; i < p.ndim; ++i) { w[i] = x[i]; }
+        R sp[MCIG_MAXPDF];
+        for (int k = 0; k < p.ms_npdf; ++k) { sp[k] = pdf_state(p.ms_pdf[k], w); }
+        R oldv;
+        if constexpr (EXACT) {
+            oldv = 1.;
+            for (int k = 0; k < p.ms_npdf; ++k) { oldv *= pdf_value_d(p, p.ms_pdf[k], w, sp[k]); }
+        } else {
+            oldv = 0.f;
+            for (int k = 0; k < p.ms_npdf; ++k) { oldv += sp[k]; }
+        }
+        for (int s = 0; s < p.ms_nsteps; ++s) {
+            const int lo = vec_move(w, 1 + s, p.ms_srrd, p.ms_veclen);
+            const int hi = lo + p.ms_veclen;
+            R spn[MCIG_MAXPDF];
+            bool acc;
+            if constexpr (EXACT) {
+                double a = 1.;
+                const bool partial = p.ms_veclen < p.ndim;
+                for (int k = 0; k < p.ms_npdf; ++k) {
+                    double pn = 0.;
+                    a *= pdf_accept_d(p, p.ms_pdf[k], w, xn, partial, lo, hi, sp[k], pn);
+                    spn[k] = pn;
+                }
+                acc = (accept_u(1 + s) <= a * 1.);
+            } else {
+                float dl = 0.f;
+                for (int k = 0; k < p.ms_npdf; ++k) {
+                    spn[k] = pdf_logp_f(p, p.ms_pdf[k], xn, blob);
+                    dl += spn[k] - sp[k];
+                }
+                acc = (__log2f(accept_u(1 + s)) <= dl * 1.44269504f);
+            }
+            if (acc) {
+                for (int i = lo; i < hi; ++i) { w[i] = xn[i]; }
+                for (int k = 0; k < p.ms_npdf; ++k) { sp[k] = spn[k]; }
+            }
+        }
+        for (int i = 0; i < p.ndim; ++i) { xn[i] = w[i]; }
+        if constexpr (EXACT) {
+            double newv = 1.;
+            for (int k = 0; k < p.ms_npdf; ++k) { newv *= pdf_value_d(p, p.ms_pdf[k], w, sp[k]); }
+            return oldv / newv;
+        } else {
+            float newv = 0.f;
+            for (int k = 0; k < p.ms_npdf; ++k) { newv += sp[k]; }
+            return oldv - newv;
+        }
+    }
+
+    // MCI::doStepMRT2 (MCIntegrator.cpp:326-360)
+    __device__ bool step_mrt2(int movetype)
+    {
+        begin_step();
+        R moveAcc = EXACT ? (R)1 : (R)0;
+        bool partial = false;
+        int lo = 0, hi = p.ndim;
+        if (movetype == MCIG_MOVE_ALL) {
+            all_move(p.srrd);
+        } else if (movetype == MCIG_MOVE_VEC) {
+            lo = vec_move(x, 0, p.srrd, p.veclen);
+            hi = lo + p.veclen;
+            partial = p.veclen < p.ndim;
+        } else {
+            moveAcc = multistep();
+        }
+        if (p.periodic) {
+            for (int i = lo; i < hi; ++i) { periodic_wrap(xn[i], p.lb[i], p.ub[i]); }
+        }
+        R lpn[MCIG_MAXPDF];
+        bool acc;
+        if constexpr (EXACT) {
+            double a = 1.;
+            for (int k = 0; k < p.npdf; ++k) {
+                double pn = lp[k];
+                a *= pdf_accept_d(p, p.pdf[k], x, xn, partial, lo, hi, lp[k], pn);
+                lpn[k] = pn;
+            }
+            acc = (accept_u(0) <= a * moveAcc);
+        } else {
+            float dl = moveAcc;
+            for (int k = 0; k < p.npdf; ++k) {
+                lpn[k] = pdf_logp_f(p, p.pdf[k], xn, blob);
+                dl += lpn[k] - lp[k];
+            }
+            acc = (__log2f(accept_u(0)) <= dl * 1.44269504f);
+        }
+        if (acc) {
+            for (int i = lo; i < hi; ++i) { x[i] = xn[i]; }
+            for (int k = 0; k < p.npdf; ++k) { lp[k] = lpn[k]; }
+        }
+        end_step();
+        return acc;
+    }
+
+    // MCI::doStepRandom (MCIntegrator.cpp:362-376) in the periodic box
+    __device__ bool step_random()
+    {
+        begin_step();
+        constexpr int CPB = Cpb<R>::v;
+        R d[CPB];
+        for (int i = 0; i < p.ndim; ++i) {
+            R u;
+            if constexpr (RNG == RNG_TAPE) { u = (R)tape_next(); }
+            else {
+                if (i % CPB == 0) { move_group(0, MCIG_SRRD_UNIFORM, i / CPB, d); }
+                u = (d[i % CPB] + (R)1) * (R)0.5;
+            }
+            xn[i] = u;
+        }
+        for (int i = 0; i < p.ndim; ++i) { x[i] = (R)p.lb[i] + xn[i] * (R)(p.ub[i] - p.lb[i]); }
+        end_step();
+        return true;
+    }
+
+    __device__ __forceinline__ bool step(int movetype) { return p.npdf > 0 ? step_mrt2(movetype) : step_random(); }
+
+    __device__ void store_state()
+    {
+        for (int i = 0; i < p.ndim; ++i) { p.x[(size_t)i * p.nchains + c] = (double)x[i]; }
+        for (int t = 0; t < p.ntypes; ++t) { p.step[(size_t)t * p.nchains + c] = (double)st[t]; }
+        if constexpr (RNG == RNG_PHILOX) { p.ctr[c] = ctr; }
+        else { p.tpos[c] = tpos; }
+        if (tape_err) { atomicOr(p.status, 1); }
+    }
+
+    // MCI::sample(npoints) (MCIntegrator.cpp:273-288)
+    __device__ void run_steps(int movetype, int64_t n)
+    {
+        init_protos();
+        int64_t na = 0;
+        for (int64_t r = 0; r < n; ++r) { na += step(movetype) ? 1 : 0; }
+        p.nacc[c] = na;
+        p.nrej[c] = n - na;
+    }
+
+    // MCI::sample(npoints, container, flagMC) (MCIntegrator.cpp:290-321) with the
+    // accumulators: observable o is evaluated at the walker position after steps
+    // r = 0, nskip, 2 nskip, ... (AccumulatorInterface.cpp:21-29, :99-114).  The
+    // reference reuses the last values on rejected steps; a pure function of the
+    // unchanged position gives the same values, so they are recomputed.
+    __device__ void run_sample(int movetype, int64_t n)
+    {
+        init_protos();
+        AccSlot<KAHAN> sums[NV];
+        R vals[NV];
+        for (int j = 0; j < p.nobsdim; ++j) { sums[j].zero(); }
+        int64_t na = 0;
+        for (int64_t r = 0; r < n; ++r) {
+            const bool a = step(movetype);
+            na += a ? 1 : 0;
+            if (p.bits) { p.bits[(size_t)r * p.nchains + c] = a ? 1 : 0; }
+            for (int o = 0; o < p.nobs; ++o) {
+                const ObsDesc &od = p.obs[o];
+                if (r % od.nskip != 0) { continue; }
+                const int64_t k = r / od.nskip; // accumulation index
+                obs_eval<R>(p, od, x, vals);
+                if (od.acc == MCIG_ACC_FULL) { // FullAccumulator::_accumulate (FullAccumulator.cpp:14-18)
+                    if (od.full32) {
+                        float *dst = (float *)od.data + (size_t)k * od.nv * p.nchains + c;
+                        for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (float)vals[j]; }
+                    } else {
+                        double *dst = (double *)od.data + (size_t)k * od.nv * p.nchains + c;
+                        for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (double)vals[j]; }
+                    }
+                } else {
+                    for (int j = 0; j < od.nv; ++j) { sums[od.voff + j].add((AccV)vals[j]); }
+                    if (od.acc == MCIG_ACC_BLOCK && (k + 1) % od.bs == 0) {
+                        // block sum times 1./blocksize (BlockAccumulator.cpp:20-41)
+                        const double normf = 1. / od.bs;
+                        double *dst = (double *)od.data + (size_t)(k / od.bs) * od.nv * p.nchains + c;
+                        for (int j = 0; j < od.nv; ++j) {
+                            dst[(size_t)j * p.nchains] = sums[od.voff + j].get() * normf;
+                            sums[od.voff + j].zero();
+                        }
+                    }
+                }
+            }
+        }
+        for (int o = 0; o < p.nobs; ++o) { // SimpleAccumulator::_finalize (SimpleAccumulator.cpp:22-29)
+            const ObsDesc &od = p.obs[o];
+            if (od.acc != MCIG_ACC_SIMPLE) { continue; }
+            const double normf = 1. / (double)(1 + (n - 1) / od.nskip);
+            double *dst = (double *)od.data + c;
+            for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = sums[od.voff + j].get() * normf; }
+        }
+        p.nacc[c] = na;
+        p.nrej[c] = n - na;
+    }
+
+    // MCI::findMRT2Step (MCIntegrator.cpp:87-168) for this chain alone
+    __device__ void run_calibration(int movetype)
+    {
+        const int64_t MIN_STAT = p.nsteps;
+        const int MIN_CONS = 5;
+        const double TOLERANCE = 0.05;
+        const double SMALLEST = 1.1754943508222875e-38; // numeric_limits<float>::min()
+        int cons = 0, counter = 0;
+        int64_t na = 0;
+        while ((p.nfind < 0 && cons < MIN_CONS) || counter < p.nfind) {
+            init_protos();
+            na = 0;
+            for (int64_t r = 0; r < MIN_STAT; ++r) { na += step(movetype) ? 1 : 0; }
+            const double rate = (na > 0) ? (double)na / ((double)na + (double)(MIN_STAT - na)) : 0.;
+            if (fabs(rate - p.target) < TOLERANCE) { ++cons; } else { cons = 0; }
+            double f = rate / p.target;
+            f = (f > 0.5) ? f : 0.5;
+            f = (f < 2.) ? f : 2.;
+            double sd[MCIG_MAXTYPES];
+            for (int t = 0; t < p.ntypes; ++t) { sd[t] = (double)st[t] * f; } // scaleStepSizes
+            for (int i = 0; i < p.ndim; ++i) {
+                int t = 0;
+                while (t + 1 < p.ntypes && i >= p.typeEnds[t]) { ++t; }
+                const double lim = p.step_max_i ? p.step_max_i[i] : p.step_max;
+                if (sd[t] > lim) { sd[t] = lim; }
+            }
+            for (int t = 0; t < p.ntypes; ++t) {
+                if (sd[t] < SMALLEST) { sd[t] = SMALLEST; }
+                st[t] = (R)sd[t];
+            }
+            ++counter;
+            if (p.nfind < 0 && counter >= abs(p.nfind)) { break; }
+        }
+        p.nacc[c] = na;
+        p.nrej[c] = (counter > 0) ? MIN_STAT - na : 0;
+    }
+};
+
+template <class R, int RNG, bool KAHAN>
+__global__ void __launch_bounds__(128) mcig_generic_kernel(const KParams p, int movetype)
+{
+    extern __shared__ float smem_blob[];
+    for (int i = threadIdx.x; i < p.fblob_len; i += blockDim.x) { smem_blob[i] = p.fblob[i]; }
+    __syncthreads();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.nchains) { return; }
+    if (p.active && !p.active[c]) { return; }
+    GenericSampler<R, RNG, KAHAN> s(p, c, smem_blob);
+    if (p.mode == KMODE_CALIB) { s.run_calibration(movetype); }
+    else if (p.mode == KMODE_SAMPLE) { s.run_sample(movetype, p.nsteps); }
+    else { s.run_steps(movetype, p.nsteps); }
+    s.store_state();
+}

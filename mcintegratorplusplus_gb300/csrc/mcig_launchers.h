@@ -1,0 +1,10 @@
+// mcig_launchers.h -- launch entry points of the sampling kernels, one per
+// translation unit (sample_generic_f64.cu, sample_generic_f32.cu, sample_fast_f32.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "mcig_common.cuh"
+
+typedef void (*mcig_launch_fn)(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st);
+
+// general kernel: precision MCIG_PREC_*, rng RNG_PHILOX / RNG_TAPE (tape: FP64 only)
+mcig_launch_fn mcig_generic_launcher(int precision, int rng);

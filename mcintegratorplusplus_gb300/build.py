@@ -22,6 +22,7 @@ UNITS = {
     "mcig_capi": ["-fmad=false"],
     "sample_generic_f64": ["-fmad=false"],
     "sample_generic_f32": [],
+    "sample_generic_f32d": [],
     "sample_fast_f32": [],
     "mcig_noalloc": ["-fmad=false"],
 }
@@ -41,14 +42,26 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
+# flag sets tried in order when nvcc crashes (a compiler segmentation fault on
+# one host is retried with a lower ptxas optimisation level)
+FALLBACKS = [[], ["-Xptxas", "-O2"], ["-Xptxas", "-O1"]]
+
+
 def _compile(unit, flags, verbose):
     src = os.path.join(CSRC, unit + ".cu")
     obj = os.path.join(BUILD, unit + ".o")
-    cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + flags + \
-        ["-c", src, "-o", obj]
-    r = subprocess.run(cmd, capture_output=True, text=True)
+    log = []
+    for extra in FALLBACKS:
+        cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + \
+            flags + extra + ["-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        log.append(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode == 0:
+            break
+        if verbose:
+            print("nvcc failed for %s with %s (rc %d): %s" % (unit, extra, r.returncode, r.stderr[-300:]))
     with open(os.path.join(BUILD, unit + ".log"), "w") as f:
-        f.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        f.write("\n".join(log))
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s" % (unit, r.stderr[-4000:]))
     if verbose:

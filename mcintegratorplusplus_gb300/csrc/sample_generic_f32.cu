@@ -1,17 +1,18 @@
-// General sampling kernel, float arithmetic with log-space acceptance, Philox draws;
-// accumulator sums in float with Kahan compensation or in double.
+// General sampling kernel, float arithmetic with log-space acceptance, Philox
+// draws; accumulator sums in float with Kahan compensation.
 #include "mcig_generic.cuh"
 #include "mcig_launchers.h"
 
-template <class R, int RNG, bool KAHAN>
-static void launch_generic(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st)
+static void launch_f32_kahan(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st)
 {
-    auto k = mcig_generic_kernel<R, RNG, KAHAN>;
+    auto k = mcig_generic_kernel<float, RNG_PHILOX, true>;
     if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
     k<<<grid, block, smem, st>>>(p, movetype);
 }
 
+mcig_launch_fn mcig_generic_launcher_f32_acc64();
+
 mcig_launch_fn mcig_generic_launcher_f32(int precision)
 {
-    return precision == MCIG_PREC_FP32 ? launch_generic<float, RNG_PHILOX, true> : launch_generic<float, RNG_PHILOX, false>;
+    return precision == MCIG_PREC_FP32 ? launch_f32_kahan : mcig_generic_launcher_f32_acc64();
 }

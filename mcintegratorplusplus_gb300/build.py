@@ -42,16 +42,17 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
-# flag sets tried in order when nvcc crashes (a compiler segmentation fault on
-# one host is retried with a lower ptxas optimisation level)
-FALLBACKS = [[], ["-Xptxas", "-O2"], ["-Xptxas", "-O1"]]
+# flag sets tried in order when nvcc crashes.  nvcc has been seen to segfault
+# intermittently on the aarch64 host when several units compile at once; a
+# failed unit is retried alone, first with the same flags.
+FALLBACKS = [[], [], ["-Xptxas", "-O2"], [], ["-Xptxas", "-O1"]]
 
 
-def _compile(unit, flags, verbose):
+def _compile(unit, flags, verbose, attempts):
     src = os.path.join(CSRC, unit + ".cu")
     obj = os.path.join(BUILD, unit + ".o")
     log = []
-    for extra in FALLBACKS:
+    for extra in attempts:
         cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + \
             flags + extra + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -74,8 +75,17 @@ def build(force=False, verbose=False):
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > _deps():
         return LIB
     units = {u: f for u, f in UNITS.items() if os.path.exists(os.path.join(CSRC, u + ".cu"))}
+    def first_try(kv):
+        try:
+            return _compile(kv[0], kv[1], verbose, FALLBACKS[:1])
+        except RuntimeError:
+            return None
+
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), units.items()))
+        objs = list(ex.map(first_try, units.items()))
+    for i, (u, f) in enumerate(units.items()):  # retries one at a time
+        if objs[i] is None:
+            objs[i] = _compile(u, f, verbose, FALLBACKS[1:])
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = [_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)

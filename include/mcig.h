@@ -53,6 +53,11 @@ int mcig_set_precision(mcig_mci *h, int precision);
 /* stream the handle's work is queued on (cudaStream_t as void*) */
 void *mcig_get_stream(const mcig_mci *h);
 
+/* Kernel choice: 0 automatic (register-resident float kernel where it applies,
+ * else the general kernel), 1 general kernel, 2 register-resident kernel
+ * (MCIG_ERR_UNSUPPORTED at integrate when the configuration needs the general one). */
+int mcig_set_kernel(mcig_mci *h, int policy);
+
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
  * from counter (step, c).  */
 int mcig_set_seed(mcig_mci *h, uint64_t seed);

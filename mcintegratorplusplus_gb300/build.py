@@ -23,7 +23,8 @@ UNITS = {
     "sample_generic_f64": ["-fmad=false"],
     "sample_generic_f32": [],
     "sample_generic_f32d": [],
-    "sample_fast_f32": [],
+    "sample_fast_all": [],
+    "sample_fast_vec": [],
     "mcig_noalloc": ["-fmad=false"],
 }
 
@@ -55,7 +56,9 @@ def _compile(unit, flags, verbose, attempts):
     for extra in attempts:
         cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + \
             flags + extra + ["-c", src, "-o", obj]
-        r = subprocess.run(cmd, capture_output=True, text=True)
+        tmp = os.path.join(BUILD, "tmp_" + unit)  # private temporary directory per unit
+        os.makedirs(tmp, exist_ok=True)
+        r = subprocess.run(cmd, capture_output=True, text=True, env=dict(os.environ, TMPDIR=tmp))
         log.append(" ".join(cmd) + "\n" + r.stdout + r.stderr)
         if r.returncode == 0:
             break

@@ -97,6 +97,7 @@ struct mcig_mci {
     int nfind = -50;
     int64_t ndecorr = -10000;
     int full32 = 0;
+    int kernel_policy = 0; // 0 auto, 1 general kernel, 2 register-resident kernel
     // device chain state
     DBuf<double> x, step;
     DBuf<uint64_t> ctr;
@@ -627,7 +628,9 @@ static bool cholesky_upper(int n, const double *P, std::vector<double> &U)
 static int build_pdf_desc(mcig_mci *h, const PdfDef &d, std::vector<double> &P, std::vector<float> &F, PdfDesc &out)
 {
     const int nd = h->ndim;
+    const int fs = maxd_bucket(nd); // float blob stride, zero-padded beyond ndim
     memset(&out, 0, sizeof(out));
+    out.fstride = fs;
     out.kind = d.kind;
     out.poff = (int)P.size();
     out.np = (int)d.params.size();
@@ -650,15 +653,17 @@ static int build_pdf_desc(mcig_mci *h, const PdfDef &d, std::vector<double> &P, 
         const double *m = d.params.data() + 1 + nc;
         for (int c = 0; c < nc; ++c) {
             F.push_back((float)P[P.size() - nc + c]);
-            for (int i = 0; i < nd; ++i) { F.push_back((float)m[c * nd + i]); }
-            for (int i = 0; i < nd; ++i) { F.push_back((float)(1.0 / s[c * nd + i])); }
+            for (int i = 0; i < fs; ++i) { F.push_back(i < nd ? (float)m[c * nd + i] : 0.f); }
+            for (int i = 0; i < fs; ++i) { F.push_back(i < nd ? (float)(1.0 / s[c * nd + i]) : 0.f); }
         }
     }
     if (d.kind == MCIG_PDF_GAUSS_PREC) {
         std::vector<double> U;
         if (!cholesky_upper(nd, d.params.data(), U)) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "GAUSS_PREC matrix is not positive definite"); }
         out.foff = (int)F.size();
-        for (double v : U) { F.push_back((float)v); }
+        for (int i = 0; i < fs; ++i) {
+            for (int j = 0; j < fs; ++j) { F.push_back((i < nd && j < nd) ? (float)U[i * nd + j] : 0.f); }
+        }
     }
     return MCIG_OK;
 }
@@ -753,15 +758,43 @@ static int fill_common(mcig_mci *h, KParams &kp)
     return MCIG_OK;
 }
 
+// the register-resident float kernel serves all/vec moves up to 32 dimensions
+// with a sampling function and observables it evaluates without exp()
+static bool fast_eligible(const mcig_mci *h)
+{
+    if (h->prec == MCIG_PREC_FP64 || h->replay || h->ndim > 32 || h->pdfs.empty()) { return false; }
+    if (h->movetype != MCIG_MOVE_ALL && h->movetype != MCIG_MOVE_VEC) { return false; }
+    for (auto &o : h->obs) {
+        if (o.kind == MCIG_OBS_GAUSSX2) { return false; }
+    }
+    return true;
+}
+
 static int launch(mcig_mci *h, const KParams &kp)
 {
-    mcig_launch_fn fn = mcig_generic_launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX);
-    if (!fn) { return set_err(MCIG_ERR_UNSUPPORTED, "no kernel for this configuration"); }
     const int block = 128;
     const int grid = (int)((h->nchains + block - 1) / block);
-    fn(kp, h->movetype, grid, block, (size_t)kp.fblob_len * sizeof(float), h->stream);
+    const bool fast = h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h));
+    mcig_launch_fn fn = nullptr;
+    size_t smem = (size_t)kp.fblob_len * sizeof(float);
+    if (fast) {
+        if (!fast_eligible(h)) { return set_err(MCIG_ERR_UNSUPPORTED, "configuration not served by the register-resident kernel"); }
+        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim));
+        smem += (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
+    } else {
+        fn = mcig_generic_launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX);
+    }
+    if (!fn) { return set_err(MCIG_ERR_UNSUPPORTED, "no kernel for this configuration"); }
+    fn(kp, h->movetype, grid, block, smem, h->stream);
     ++h->launches;
     CK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_kernel(mcig_mci *h, int policy)
+{
+    if (policy < 0 || policy > 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "kernel policy must be 0 (auto), 1 (general) or 2 (register-resident)"); }
+    h->kernel_policy = policy;
     return MCIG_OK;
 }
 

@@ -42,6 +42,7 @@ struct PdfDesc {
     int b0, b1;   // GAUSS_BLOCK bounds
     double c;     // GAUSS_BLOCK: 1/(2 w^2)
     int foff;     // float path: offset of this pdf's data in the shared-memory blob
+    int fstride;  // float path: coordinate stride of that data (>= ndim, zero-padded)
 };
 
 struct ObsDesc {

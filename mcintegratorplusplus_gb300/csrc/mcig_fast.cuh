@@ -1,0 +1,404 @@
+// mcig_fast.cuh -- register-resident float sampling kernel for the common
+// configurations: all-coordinate or single-vector moves (uniform / Gaussian),
+// any product of sampling functions, observables without exp(), Philox draws.
+//
+// The walker (x, proposal) lives in registers: MAXD is a compile-time bound on
+// ndim and every coordinate loop is unrolled with compile-time indices, so no
+// per-thread local memory is touched in the step.  Shared memory holds
+//   - the sampling-function blob (Cholesky factor U of a precision matrix with
+//     row stride MAXD, mixture parameters), read with broadcast loads at
+//     compile-time offsets;
+//   - the running sums of Simple/Block accumulators, one slot per observable
+//     value and thread ([slot][thread], conflict-free), float+Kahan or double.
+// Full accumulators store every sample straight to HBM, coalesced across the
+// warp (layout [nstore][nobs][nchains]).
+//
+// Semantics are those of the general kernel (mcig_generic.cuh) in float:
+// log-space Metropolis test log(u) <= log p(x') - log p(x), one Philox stream
+// per chain with the same counter layout, so a chain draws the same numbers in
+// both kernels.
+#pragma once
+
+#include "mcig_common.cuh"
+
+template <int MAXD>
+__device__ __forceinline__ float fast_logp(const KParams &p, const float *x, const float *blob)
+{
+    const int nd = p.ndim;
+    float lp = 0.f;
+    for (int k = 0; k < p.npdf; ++k) {
+        const PdfDesc &d = p.pdf[k];
+        switch (d.kind) {
+        case MCIG_PDF_GAUSS_SUM:
+        case MCIG_PDF_GAUSS: {
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i < nd) { s = fmaf(x[i], x[i], s); }
+            }
+            lp -= s;
+            break;
+        }
+        case MCIG_PDF_EXP: {
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i < nd) { s += fabsf(x[i]); }
+            }
+            lp -= s;
+            break;
+        }
+        case MCIG_PDF_GAUSS_PREC: { // -|U x|^2 / 2, U upper triangular, row stride MAXD
+            const float *U = blob + d.foff;
+            float q = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i < nd) {
+                    float t = 0.f;
+#pragma unroll
+                    for (int j = i; j < MAXD; ++j) { t = fmaf(U[i * MAXD + j], x[j], t); } // zero-padded beyond nd
+                    q = fmaf(t, t, q);
+                }
+            }
+            lp = fmaf(-0.5f, q, lp);
+            break;
+        }
+        case MCIG_PDF_GAUSS_BLOCK: {
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i >= d.b0 && i < d.b1) { s = fmaf(x[i], x[i], s); }
+            }
+            lp = fmaf(-(float)d.c, s, lp);
+            break;
+        }
+        case MCIG_PDF_GAUSS_MIX: { // log sum_c exp(lc_c - |(x - m_c) / s_c|^2 / 2), per component stride 1 + 2 MAXD
+            const float *b = blob + d.foff;
+            const int nc = (int)b[0];
+            float e[16];
+            float mx = -INFINITY;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                if (c < nc) {
+                    const float *cb = b + 1 + c * (1 + 2 * MAXD);
+                    float a = 0.f;
+#pragma unroll
+                    for (int i = 0; i < MAXD; ++i) {
+                        const float z = (x[i] - cb[1 + i]) * cb[1 + MAXD + i]; // zero beyond nd
+                        a = fmaf(z, z, a);
+                    }
+                    a = fmaf(-0.5f, a, cb[0]);
+                    e[c] = a;
+                    mx = fmaxf(mx, a);
+                }
+            }
+            float sum = 0.f;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                if (c < nc) { sum += exp2f((e[c] - mx) * 1.44269504f); }
+            }
+            lp += mx + 0.69314718f * __log2f(sum);
+            break;
+        }
+        default: break;
+        }
+    }
+    return lp;
+}
+
+template <bool KAHAN> struct FastSlot;
+template <> struct FastSlot<true> {
+    using T = float2;
+    __device__ __forceinline__ static void zero(T &v) { v = make_float2(0.f, 0.f); }
+    __device__ __forceinline__ static void add(T &v, float a)
+    { // Kahan: v.x sum, v.y compensation
+        const float y = a - v.y;
+        const float t = v.x + y;
+        v.y = (t - v.x) - y;
+        v.x = t;
+    }
+    __device__ __forceinline__ static double get(const T &v) { return (double)v.x - (double)v.y; }
+};
+template <> struct FastSlot<false> {
+    using T = double;
+    __device__ __forceinline__ static void zero(T &v) { v = 0.; }
+    __device__ __forceinline__ static void add(T &v, float a) { v += (double)a; }
+    __device__ __forceinline__ static double get(const T &v) { return v; }
+};
+
+template <int MAXD, int MOVE, bool KAHAN>
+struct FastSampler {
+    using Slot = FastSlot<KAHAN>;
+    using ST = typename Slot::T;
+    const KParams &p;
+    const int c;
+    const float *blob;
+    ST *slots; // [nobsdim][blockDim]
+    float x[MAXD];
+    float st[MCIG_MAXTYPES];
+    float lp;
+    PhiloxCtx ph;
+    uint64_t ctr;
+
+    __device__ FastSampler(const KParams &pp, int cc, const float *bl, ST *sl) : p(pp), c(cc), blob(bl), slots(sl)
+    {
+#pragma unroll
+        for (int i = 0; i < MAXD; ++i) { x[i] = (i < p.ndim) ? (float)p.x[(size_t)i * p.nchains + c] : 0.f; }
+#pragma unroll
+        for (int t = 0; t < MCIG_MAXTYPES; ++t) { st[t] = (t < p.ntypes) ? (float)p.step[(size_t)t * p.nchains + c] : 0.f; }
+        ctr = p.ctr[c];
+        ph.k0 = p.key0;
+        ph.k1 = p.key1;
+        ph.chain = (uint32_t)c;
+    }
+
+    __device__ __forceinline__ float step_of(int i) const
+    {
+        float s = st[0];
+#pragma unroll
+        for (int t = 1; t < MCIG_MAXTYPES; ++t) {
+            if (t < p.ntypes && i >= p.typeEnds[t - 1]) { s = st[t]; }
+        }
+        return s;
+    }
+
+    // one Metropolis step (MCI::doStepMRT2, MCIntegrator.cpp:326-360)
+    __device__ __forceinline__ bool step()
+    {
+        ph.s0 = (uint32_t)ctr;
+        ph.s1 = (uint32_t)(ctr >> 32);
+        const bool gauss = p.srrd == MCIG_SRRD_GAUSSIAN;
+        float xn[MAXD];
+        int lo = 0, hi = p.ndim;
+        if constexpr (MOVE == MCIG_MOVE_ALL) { // SRRDAllMove::trialMove
+            const bool one_type = p.ntypes == 1;
+#pragma unroll
+            for (int b = 0; b < (MAXD + 3) / 4; ++b) {
+                float d[4] = {0.f, 0.f, 0.f, 0.f};
+                if (b * 4 < p.ndim) { move_draws<float>(ph.block(0, TAG_MOVE, b), gauss, d); }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int i = b * 4 + k;
+                    if (i < MAXD) { xn[i] = (i < p.ndim) ? fmaf(one_type ? st[0] : step_of(i), d[k], x[i]) : 0.f; }
+                }
+            }
+        } else { // SRRDVecMove::trialMove
+            const int nvecs = p.ndim / p.veclen;
+            const int vidx = (int)__umulhi(ph.block(0, TAG_INDEX, 0).a, (uint32_t)nvecs);
+            lo = vidx * p.veclen;
+            hi = lo + p.veclen;
+            const float s = step_of(lo);
+#pragma unroll
+            for (int b = 0; b < (MAXD + 3) / 4; ++b) {
+                float d[4] = {0.f, 0.f, 0.f, 0.f};
+                if (b * 4 < hi && b * 4 + 4 > lo) { move_draws<float>(ph.block(0, TAG_MOVE, b), gauss, d); }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int i = b * 4 + k;
+                    if (i < MAXD) { xn[i] = (i >= lo && i < hi) ? fmaf(s, d[k], x[i]) : x[i]; }
+                }
+            }
+        }
+        if (p.periodic) {
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i >= lo && i < hi) {
+                    const float lb = (float)p.lb[i], ub = (float)p.ub[i], L = ub - lb;
+                    int n = 0;
+                    while (xn[i] < lb && n < MCIG_PERIODIC_MAXWRAP) { xn[i] += L; ++n; }
+                    while (xn[i] > ub && n < MCIG_PERIODIC_MAXWRAP) { xn[i] -= L; ++n; }
+                    if (n >= MCIG_PERIODIC_MAXWRAP) { xn[i] = fminf(fmaxf(xn[i], lb), ub); }
+                }
+            }
+        }
+        const float lpn = fast_logp<MAXD>(p, xn, blob);
+        const float u = u01_f(ph.block(0, TAG_ACCEPT, 0).a);
+        const bool acc = __log2f(u) <= (lpn - lp) * 1.44269504f;
+        if (acc) {
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) { x[i] = xn[i]; }
+            lp = lpn;
+        }
+        ++ctr;
+        return acc;
+    }
+
+    __device__ __forceinline__ ST &slot(int j) { return slots[(size_t)j * blockDim.x + threadIdx.x]; }
+
+    // one value of observable o at accumulation index k
+    __device__ __forceinline__ void emit(const ObsDesc &od, int64_t k, int j, float v)
+    {
+        if (od.acc == MCIG_ACC_FULL) {
+            const size_t idx = ((size_t)k * od.nv + j) * p.nchains + c;
+            if (od.full32) { ((float *)od.data)[idx] = v; }
+            else { ((double *)od.data)[idx] = (double)v; }
+        } else {
+            Slot::add(slot(od.voff + j), v);
+        }
+    }
+
+    // observableFunction of the test classes (oracle obs_eval), in float
+    __device__ void observe(const ObsDesc &od, int64_t k)
+    {
+        const int nd = p.ndim;
+        switch (od.kind) {
+        case MCIG_OBS_X2SUM:
+        case MCIG_OBS_X2MEAN: {
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i < nd) { s = fmaf(x[i], x[i], s); }
+            }
+            emit(od, k, 0, od.kind == MCIG_OBS_X2SUM ? s : s / (float)nd);
+            break;
+        }
+        case MCIG_OBS_XND:
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i < nd) { emit(od, k, i, x[i]); }
+            }
+            break;
+        case MCIG_OBS_X2:
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i < nd) { emit(od, k, i, x[i] * x[i]); }
+            }
+            break;
+        case MCIG_OBS_CONST: emit(od, k, 0, (float)p.params[od.poff]); break;
+        case MCIG_OBS_POLYNOM: {
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                if (i < nd) { s += x[i]; }
+            }
+            emit(od, k, 0, s);
+            break;
+        }
+        case MCIG_OBS_X2BLOCK: {
+            const double *pp = p.params + od.poff;
+            const int nb = (int)pp[0];
+            for (int kb = 0; kb < nb; ++kb) {
+                const int a = (int)pp[1 + kb], b = (int)pp[2 + kb];
+                float s = 0.f;
+#pragma unroll
+                for (int i = 0; i < MAXD; ++i) {
+                    if (i >= a && i < b) { s = fmaf(x[i], x[i], s); }
+                }
+                emit(od, k, kb, s);
+            }
+            break;
+        }
+        default: break;
+        }
+    }
+
+    __device__ void run(int64_t n, bool sample)
+    {
+        lp = fast_logp<MAXD>(p, x, blob);
+        for (int j = 0; j < p.nobsdim && sample; ++j) { Slot::zero(slot(j)); }
+        int64_t na = 0;
+        for (int64_t r = 0; r < n; ++r) {
+            na += step() ? 1 : 0;
+            if (!sample) { continue; }
+            for (int o = 0; o < p.nobs; ++o) {
+                const ObsDesc &od = p.obs[o];
+                if (r % od.nskip != 0) { continue; }
+                const int64_t k = r / od.nskip;
+                observe(od, k);
+                if (od.acc == MCIG_ACC_BLOCK && (k + 1) % od.bs == 0) { // BlockAccumulator, sum * (1./blocksize)
+                    const double normf = 1. / od.bs;
+                    double *dst = (double *)od.data + (size_t)(k / od.bs) * od.nv * p.nchains + c;
+                    for (int j = 0; j < od.nv; ++j) {
+                        dst[(size_t)j * p.nchains] = Slot::get(slot(od.voff + j)) * normf;
+                        Slot::zero(slot(od.voff + j));
+                    }
+                }
+            }
+        }
+        if (sample) {
+            for (int o = 0; o < p.nobs; ++o) { // SimpleAccumulator::_finalize
+                const ObsDesc &od = p.obs[o];
+                if (od.acc != MCIG_ACC_SIMPLE) { continue; }
+                const double normf = 1. / (double)(1 + (n - 1) / od.nskip);
+                double *dst = (double *)od.data + c;
+                for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = Slot::get(slot(od.voff + j)) * normf; }
+            }
+        }
+        p.nacc[c] = na;
+        p.nrej[c] = n - na;
+    }
+
+    // MCI::findMRT2Step (MCIntegrator.cpp:87-168) for this chain alone
+    __device__ void calibrate()
+    {
+        const int64_t MIN_STAT = p.nsteps;
+        int cons = 0, counter = 0;
+        int64_t na = 0;
+        while ((p.nfind < 0 && cons < 5) || counter < p.nfind) {
+            lp = fast_logp<MAXD>(p, x, blob);
+            na = 0;
+            for (int64_t r = 0; r < MIN_STAT; ++r) { na += step() ? 1 : 0; }
+            const double rate = (na > 0) ? (double)na / (double)MIN_STAT : 0.;
+            if (fabs(rate - p.target) < 0.05) { ++cons; } else { cons = 0; }
+            const double f = fmin(2., fmax(0.5, rate / p.target));
+#pragma unroll
+            for (int t = 0; t < MCIG_MAXTYPES; ++t) {
+                if (t < p.ntypes) {
+                    double s = (double)st[t] * f;
+                    double lim = p.step_max;
+                    for (int i = 0; i < p.ndim; ++i) {
+                        int tt = 0;
+                        while (tt + 1 < p.ntypes && i >= p.typeEnds[tt]) { ++tt; }
+                        if (tt == t && p.step_max_i) { lim = fmin(lim, p.step_max_i[i]); }
+                    }
+                    s = fmin(s, lim);
+                    s = fmax(s, 1.1754943508222875e-38);
+                    st[t] = (float)s;
+                }
+            }
+            ++counter;
+            if (p.nfind < 0 && counter >= abs(p.nfind)) { break; }
+        }
+        p.nacc[c] = na;
+        p.nrej[c] = (counter > 0) ? MIN_STAT - na : 0;
+    }
+
+    __device__ void store_state()
+    {
+#pragma unroll
+        for (int i = 0; i < MAXD; ++i) {
+            if (i < p.ndim) { p.x[(size_t)i * p.nchains + c] = (double)x[i]; }
+        }
+#pragma unroll
+        for (int t = 0; t < MCIG_MAXTYPES; ++t) {
+            if (t < p.ntypes) { p.step[(size_t)t * p.nchains + c] = (double)st[t]; }
+        }
+        p.ctr[c] = ctr;
+    }
+};
+
+template <int MAXD, int MOVE, bool KAHAN>
+__global__ void __launch_bounds__(128) mcig_fast_kernel(const KParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using ST = typename FastSlot<KAHAN>::T;
+    ST *slots = (ST *)smem_raw;
+    float *blob = (float *)(smem_raw + (size_t)p.nobsdim * blockDim.x * sizeof(ST));
+    for (int i = threadIdx.x; i < p.fblob_len; i += blockDim.x) { blob[i] = p.fblob[i]; }
+    __syncthreads();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.nchains) { return; }
+    if (p.active && !p.active[c]) { return; }
+    FastSampler<MAXD, MOVE, KAHAN> s(p, c, blob, slots);
+    if (p.mode == KMODE_CALIB) { s.calibrate(); }
+    else { s.run(p.nsteps, p.mode == KMODE_SAMPLE); }
+    s.store_state();
+}
+
+template <int MAXD, int MOVE, bool KAHAN>
+void mcig_fast_launch(const KParams &p, int /*movetype*/, int grid, int block, size_t smem, cudaStream_t st)
+{
+    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN>;
+    if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
+    k<<<grid, block, smem, st>>>(p);
+}

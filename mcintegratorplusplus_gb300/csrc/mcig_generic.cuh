@@ -127,8 +127,8 @@ static __device__ double pdf_value_d(const KParams &p, const PdfDesc &d, const d
 
 // ------------------------------------------------------------------------
 // sampling functions, float (log density; parameter blob in shared memory)
-//   GAUSS_PREC : U[ndim][ndim], upper Cholesky factor of P (x^T P x = |U x|^2)
-//   GAUSS_MIX  : nc, then per component: log-normalisation, m[nd], 1/s[nd]
+//   GAUSS_PREC : U[ndim][fstride], upper Cholesky factor of P (x^T P x = |U x|^2)
+//   GAUSS_MIX  : nc, then per component: log-normalisation, m[fstride], 1/s[fstride]
 // ------------------------------------------------------------------------
 static __device__ float pdf_logp_f(const KParams &p, const PdfDesc &d, const float *x, const float *blob)
 {
@@ -150,7 +150,7 @@ static __device__ float pdf_logp_f(const KParams &p, const PdfDesc &d, const flo
         float q = 0.f;
         for (int i = 0; i < nd; ++i) {
             float t = 0.f;
-            for (int j = i; j < nd; ++j) { t = fmaf(U[i * nd + j], x[j], t); }
+            for (int j = i; j < nd; ++j) { t = fmaf(U[i * d.fstride + j], x[j], t); }
             q = fmaf(t, t, q);
         }
         return -0.5f * q;
@@ -163,14 +163,14 @@ static __device__ float pdf_logp_f(const KParams &p, const PdfDesc &d, const flo
     case MCIG_PDF_GAUSS_MIX: {
         const float *b = blob + d.foff;
         const int nc = (int)b[0];
-        const int stride = 1 + 2 * nd;
+        const int stride = 1 + 2 * d.fstride;
         float e[16];
         float mx = -INFINITY;
         for (int c = 0; c < nc; ++c) {
             const float *cb = b + 1 + c * stride;
             float a = 0.f;
             for (int i = 0; i < nd; ++i) {
-                const float z = (x[i] - cb[1 + i]) * cb[1 + nd + i];
+                const float z = (x[i] - cb[1 + i]) * cb[1 + d.fstride + i];
                 a = fmaf(z, z, a);
             }
             a = fmaf(-0.5f, a, cb[0]);

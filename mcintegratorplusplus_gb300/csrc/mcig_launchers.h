@@ -8,3 +8,7 @@ typedef void (*mcig_launch_fn)(const KParams &p, int movetype, int grid, int blo
 
 // general kernel: precision MCIG_PREC_*, rng RNG_PHILOX / RNG_TAPE (tape: FP64 only)
 mcig_launch_fn mcig_generic_launcher(int precision, int rng);
+
+// register-resident float kernel (mcig_fast.cuh): move MCIG_MOVE_ALL / MCIG_MOVE_VEC,
+// maxd 4, 8, 16 or 32; NULL otherwise
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd);

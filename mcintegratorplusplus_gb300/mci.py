@@ -98,6 +98,10 @@ class MCI:
     def setSeed(self, seed):
         _raise(self.L.mcig_set_seed(self._h, ctypes.c_uint64(int(seed) & ((1 << 64) - 1))))
 
+    def setKernel(self, policy):
+        """0 automatic, 1 general kernel, 2 register-resident float kernel."""
+        _raise(self.L.mcig_set_kernel(self._h, int(policy)))
+
     def setPrecision(self, precision):
         _raise(self.L.mcig_set_precision(self._h, int(precision)))
 

@@ -41,6 +41,13 @@ static int set_err(int code, const char *fmt, ...)
     } while (0)
 
 extern "C" const char *mcig_last_error(void) { return g_err.c_str(); }
+
+// error setter for the other translation units of the library
+int mcig_set_last_error(int code, const char *msg)
+{
+    g_err = msg ? msg : "";
+    return code;
+}
 extern "C" const char *mcig_version(void) { return "mcig 0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------------------
@@ -774,11 +781,12 @@ static int launch(mcig_mci *h, const KParams &kp)
 {
     const int block = 128;
     const int grid = (int)((h->nchains + block - 1) / block);
-    const bool fast = h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h));
+    const bool small_n = kp.nsteps < ((int64_t)1 << 31); // 32-bit step counters in the register-resident kernel
+    const bool fast = h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n);
     mcig_launch_fn fn = nullptr;
     size_t smem = (size_t)kp.fblob_len * sizeof(float);
     if (fast) {
-        if (!fast_eligible(h)) { return set_err(MCIG_ERR_UNSUPPORTED, "configuration not served by the register-resident kernel"); }
+        if (!fast_eligible(h) || !small_n) { return set_err(MCIG_ERR_UNSUPPORTED, "configuration not served by the register-resident kernel"); }
         fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim));
         smem += (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
     } else {
@@ -834,7 +842,8 @@ static int run_estimator(mcig_mci *h, int est, const void *data, int is_float, i
     case MCIG_EST_NOOP: est_noop_kernel<<<grid, block, 0, st>>>(a); break;
     case MCIG_EST_UNCORRELATED:
         if (n < 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[UncorrelatedEstimator] n must be larger than 1"); }
-        est_uncorr_kernel<<<grid, block, 0, st>>>(a);
+        if (is_float) { est_uncorr_f32_kernel<<<grid, block, 0, st>>>(a); }
+        else { est_uncorr_kernel<<<grid, block, 0, st>>>(a); }
         break;
     case MCIG_EST_FCBLOCKER:
         if (n < 50) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "FCBlockerEstimator: n must be >= 50"); }
@@ -1156,6 +1165,8 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
     CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
     KParams kp;
     if ((rc = fill_common(h, kp))) { return rc; }
+    // device buffers first, so that allocation stays outside the timed phases
+    if (nmc > 0 && (rc = alloc_obs_data(h, h->obs, nmc, h->obsdata, h->obs_nstore, h->full32))) { return rc; }
     CK(cudaEventRecord(h->ev[0], h->stream));
     // phase 1: MCI::findMRT2Step (only with a pdf; every move here has step sizes)
     if (!h->pdfs.empty() && do_find && h->nfind != 0) {
@@ -1178,7 +1189,6 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
     }
     CK(cudaEventRecord(h->ev[2], h->stream));
     if (nmc > 0) {
-        if ((rc = alloc_obs_data(h, h->obs, nmc, h->obsdata, h->obs_nstore, h->full32))) { return rc; }
         KParams s = kp;
         s.mode = KMODE_SAMPLE;
         s.nsteps = nmc;

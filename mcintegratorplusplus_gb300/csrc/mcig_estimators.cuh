@@ -57,14 +57,43 @@ __device__ __forceinline__ void uncorr_core(int64_t n, F v, int one_d, double &a
     error = e;
 }
 
-__global__ void est_noop_kernel(EstArgs a)
+// Uncorrelated estimator on float samples (float precision modes): Kahan-compensated
+// float sums of x and x^2 (four float operations per value instead of two
+// double ones), combined in double with the reference's formula.
+static __global__ void est_uncorr_f32_kernel(EstArgs a)
+{
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= (int64_t)a.nv * a.nchains) { return; }
+    const float *d = (const float *)a.data + s;
+    const int64_t stride = (int64_t)a.nv * a.nchains;
+    float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+    for (int64_t i = 0; i < a.n; ++i) {
+        const float x = d[i * stride];
+        float y = x - c1, t = s1 + y;
+        c1 = (t - s1) - y;
+        s1 = t;
+        y = x * x - c2;
+        t = s2 + y;
+        c2 = (t - s2) - y;
+        s2 = t;
+    }
+    const double SMALLEST_ERROR = 1.e-300;
+    const double norm = 1. / a.n;
+    const double average = ((double)s1 - (double)c1) * norm;
+    double e = ((double)s2 - (double)c2) * norm - average * average;
+    if (a.one_d) { e = (e > SMALLEST_ERROR) ? sqrt(e / (a.n - 1.)) : 0.; }
+    else { e = (e > SMALLEST_ERROR) ? sqrt(e * (1. / (a.n - 1.))) : 0.; }
+    est_store(a, s, average, e);
+}
+
+static __global__ void est_noop_kernel(EstArgs a)
 { // NoopEstimator (:289-293): the first row is the result
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= (int64_t)a.nv * a.nchains) { return; }
     est_store(a, s, est_load(a, 0, s), 0.);
 }
 
-__global__ void est_uncorr_kernel(EstArgs a)
+static __global__ void est_uncorr_kernel(EstArgs a)
 {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= (int64_t)a.nv * a.nchains) { return; }
@@ -90,7 +119,7 @@ __device__ __forceinline__ double fc_delta(int mode, const double *e)
 
 // FCBlockerEstimator (Estimators.cpp:82-122 / 191-246): block estimators for 6..50
 // blocks, plateau of the finite-difference slope of the error.
-__global__ void est_fc_kernel(EstArgs a)
+static __global__ void est_fc_kernel(EstArgs a)
 {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= (int64_t)a.nv * a.nchains) { return; }
@@ -129,7 +158,7 @@ __global__ void est_fc_kernel(EstArgs a)
 }
 
 // chi^2 0.95 quantiles, k + 1 degrees of freedom (MJBlocker.cpp:6-13)
-__constant__ double c_mj_quantile[64] = {
+static __constant__ double c_mj_quantile[64] = {
     3.841459, 5.991465, 7.814728, 9.487729, 11.070498, 12.591587, 14.067140, 15.507313,
     16.918978, 18.307038, 19.675138, 21.026070, 22.362032, 23.684791, 24.995790, 26.296228,
     27.587112, 28.869299, 30.143527, 31.410433, 32.670573, 33.924438, 35.172462, 36.415029,
@@ -144,7 +173,7 @@ __constant__ double c_mj_quantile[64] = {
 // X = x - mean is formed on the fly exactly as the reference stores it
 // (:58-65, :100).  When no level passes the test (constant data) the last
 // level is used, where the reference would read one level past its arrays.
-__global__ void est_mj_kernel(EstArgs a)
+static __global__ void est_mj_kernel(EstArgs a)
 {
     const int64_t S = (int64_t)a.nv * a.nchains;
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

@@ -225,20 +225,9 @@ struct FastSampler {
 
     __device__ __forceinline__ ST &slot(int j) { return slots[(size_t)j * blockDim.x + threadIdx.x]; }
 
-    // one value of observable o at accumulation index k
-    __device__ __forceinline__ void emit(const ObsDesc &od, int64_t k, int j, float v)
-    {
-        if (od.acc == MCIG_ACC_FULL) {
-            const size_t idx = ((size_t)k * od.nv + j) * p.nchains + c;
-            if (od.full32) { ((float *)od.data)[idx] = v; }
-            else { ((double *)od.data)[idx] = (double)v; }
-        } else {
-            Slot::add(slot(od.voff + j), v);
-        }
-    }
-
-    // observableFunction of the test classes (oracle obs_eval), in float
-    __device__ void observe(const ObsDesc &od, int64_t k)
+    // observableFunction of the test classes (oracle obs_eval), in float, into
+    // v[0..nv) with compile-time indices; returns nv
+    __device__ __forceinline__ int observe(const ObsDesc &od, float *v) const
     {
         const int nd = p.ndim;
         switch (od.kind) {
@@ -249,70 +238,103 @@ struct FastSampler {
             for (int i = 0; i < MAXD; ++i) {
                 if (i < nd) { s = fmaf(x[i], x[i], s); }
             }
-            emit(od, k, 0, od.kind == MCIG_OBS_X2SUM ? s : s / (float)nd);
-            break;
+            v[0] = od.kind == MCIG_OBS_X2SUM ? s : s / (float)nd;
+            return 1;
         }
         case MCIG_OBS_XND:
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) {
-                if (i < nd) { emit(od, k, i, x[i]); }
-            }
-            break;
+            for (int i = 0; i < MAXD; ++i) { v[i] = x[i]; }
+            return nd;
         case MCIG_OBS_X2:
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) {
-                if (i < nd) { emit(od, k, i, x[i] * x[i]); }
-            }
-            break;
-        case MCIG_OBS_CONST: emit(od, k, 0, (float)p.params[od.poff]); break;
+            for (int i = 0; i < MAXD; ++i) { v[i] = x[i] * x[i]; }
+            return nd;
+        case MCIG_OBS_CONST: v[0] = (float)p.params[od.poff]; return 1;
         case MCIG_OBS_POLYNOM: {
             float s = 0.f;
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) {
                 if (i < nd) { s += x[i]; }
             }
-            emit(od, k, 0, s);
-            break;
+            v[0] = s;
+            return 1;
         }
         case MCIG_OBS_X2BLOCK: {
             const double *pp = p.params + od.poff;
             const int nb = (int)pp[0];
-            for (int kb = 0; kb < nb; ++kb) {
-                const int a = (int)pp[1 + kb], b = (int)pp[2 + kb];
-                float s = 0.f;
 #pragma unroll
-                for (int i = 0; i < MAXD; ++i) {
-                    if (i >= a && i < b) { s = fmaf(x[i], x[i], s); }
+            for (int kb = 0; kb < MAXD; ++kb) {
+                float s = 0.f;
+                if (kb < nb) {
+                    const int a = (int)pp[1 + kb], b = (int)pp[2 + kb];
+#pragma unroll
+                    for (int i = 0; i < MAXD; ++i) {
+                        if (i >= a && i < b) { s = fmaf(x[i], x[i], s); }
+                    }
                 }
-                emit(od, k, kb, s);
+                v[kb] = s;
             }
-            break;
+            return nb;
         }
-        default: break;
+        default: return 0;
         }
     }
 
+    // one accumulation of observable o at accumulation index k (AccumulatorInterface::accumulate)
+    __device__ __forceinline__ void accumulate(const ObsDesc &od, uint32_t k)
+    {
+        float v[MAXD];
+        const int nv = observe(od, v);
+        if (od.acc == MCIG_ACC_FULL) { // FullAccumulator: one coalesced row per value
+            const size_t stride = (size_t)p.nchains;
+            if (od.full32) {
+                float *dst = (float *)od.data + (size_t)k * nv * stride + c;
+#pragma unroll
+                for (int j = 0; j < MAXD; ++j) {
+                    if (j < nv) { dst[j * stride] = v[j]; }
+                }
+            } else {
+                double *dst = (double *)od.data + (size_t)k * nv * stride + c;
+#pragma unroll
+                for (int j = 0; j < MAXD; ++j) {
+                    if (j < nv) { dst[j * stride] = (double)v[j]; }
+                }
+            }
+            return;
+        }
+        ST *sl = slots + (size_t)od.voff * blockDim.x + threadIdx.x;
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j) {
+            if (j < nv) { Slot::add(sl[j * blockDim.x], v[j]); }
+        }
+        if (od.acc == MCIG_ACC_BLOCK && (k + 1) % (uint32_t)od.bs == 0u) { // block mean = sum * (1./blocksize)
+            const double normf = 1. / od.bs;
+            double *dst = (double *)od.data + (size_t)(k / (uint32_t)od.bs) * nv * p.nchains + c;
+#pragma unroll
+            for (int j = 0; j < MAXD; ++j) {
+                if (j < nv) {
+                    dst[(size_t)j * p.nchains] = Slot::get(sl[j * blockDim.x]) * normf;
+                    Slot::zero(sl[j * blockDim.x]);
+                }
+            }
+        }
+    }
+
+    // n < 2^32 (checked on the host); accumulation indices in 32-bit arithmetic
     __device__ void run(int64_t n, bool sample)
     {
         lp = fast_logp<MAXD>(p, x, blob);
         for (int j = 0; j < p.nobsdim && sample; ++j) { Slot::zero(slot(j)); }
-        int64_t na = 0;
-        for (int64_t r = 0; r < n; ++r) {
-            na += step() ? 1 : 0;
+        const uint32_t n32 = (uint32_t)n;
+        uint32_t na = 0;
+        for (uint32_t r = 0; r < n32; ++r) {
+            na += step() ? 1u : 0u;
             if (!sample) { continue; }
             for (int o = 0; o < p.nobs; ++o) {
                 const ObsDesc &od = p.obs[o];
-                if (r % od.nskip != 0) { continue; }
-                const int64_t k = r / od.nskip;
-                observe(od, k);
-                if (od.acc == MCIG_ACC_BLOCK && (k + 1) % od.bs == 0) { // BlockAccumulator, sum * (1./blocksize)
-                    const double normf = 1. / od.bs;
-                    double *dst = (double *)od.data + (size_t)(k / od.bs) * od.nv * p.nchains + c;
-                    for (int j = 0; j < od.nv; ++j) {
-                        dst[(size_t)j * p.nchains] = Slot::get(slot(od.voff + j)) * normf;
-                        Slot::zero(slot(od.voff + j));
-                    }
-                }
+                const uint32_t ns = (uint32_t)od.nskip;
+                if (ns == 1u) { accumulate(od, r); }
+                else if (r % ns == 0u) { accumulate(od, r / ns); }
             }
         }
         if (sample) {
@@ -337,7 +359,7 @@ struct FastSampler {
         while ((p.nfind < 0 && cons < 5) || counter < p.nfind) {
             lp = fast_logp<MAXD>(p, x, blob);
             na = 0;
-            for (int64_t r = 0; r < MIN_STAT; ++r) { na += step() ? 1 : 0; }
+            for (uint32_t r = 0; r < (uint32_t)MIN_STAT; ++r) { na += step() ? 1 : 0; }
             const double rate = (na > 0) ? (double)na / (double)MIN_STAT : 0.;
             if (fabs(rate - p.target) < 0.05) { ++cons; } else { cons = 0; }
             const double f = fmin(2., fmax(0.5, rate / p.target));

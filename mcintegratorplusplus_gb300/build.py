@@ -24,6 +24,8 @@ UNITS = {
     "sample_generic_f32": [],
     "sample_generic_f32d": [],
     "sample_fast_all": [],
+    "sample_fast_all32": [],
+    "sample_fast_all32d": [],
     "sample_fast_vec": [],
     "mcig_noalloc": ["-fmad=false"],
 }

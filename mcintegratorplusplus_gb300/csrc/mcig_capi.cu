@@ -675,6 +675,53 @@ static int build_pdf_desc(mcig_mci *h, const PdfDef &d, std::vector<double> &P, 
     return MCIG_OK;
 }
 
+// (magic, shift) with n / d == umulhi(n, magic) >> shift for every n < 2^31:
+// s = floor(log2 d); a power of two uses magic 2^31 and shift s-1, any other d
+// magic = floor(2^(32+s) / d) + 1 (round-up method; the rounding error of the
+// reciprocal stays below 1/d for 31-bit n).  d <= 1 is never divided by.
+static void magic_div(uint32_t d, uint32_t &magic, uint32_t &shift)
+{
+    if (d <= 1) { magic = 0; shift = 0; return; }
+    uint32_t s = 0;
+    while ((2ull << s) <= d) { ++s; }
+    if (d == (1u << s)) { magic = 1u << 31; shift = s - 1; return; }
+    magic = (uint32_t)(((1ull << (32 + s)) / d) + 1);
+    shift = s;
+}
+
+// float data of the register-resident kernel at its fixed offsets (mcig_fast.cuh)
+static void fill_fast_const(const mcig_mci *h, KParams &kp)
+{
+    const int nd = h->ndim;
+    int md = 4;
+    while (md < nd) { md *= 2; }
+    memset(kp.fconst, 0, sizeof(kp.fconst));
+    for (const PdfDef &d : h->pdfs) {
+        if (d.kind == MCIG_PDF_GAUSS_PREC) {
+            std::vector<double> U;
+            if (!cholesky_upper(nd, d.params.data(), U)) { continue; }
+            for (int i = 0; i < nd; ++i) {
+                for (int j = 0; j < nd; ++j) { kp.fconst[i * md + j] = (float)U[i * nd + j]; }
+            }
+        }
+        if (d.kind == MCIG_PDF_GAUSS_MIX) {
+            const int B = md * md, S = 1 + 2 * md;
+            const int nc = (int)d.params[0];
+            const double *w = d.params.data() + 1, *m = d.params.data() + 1 + nc, *sg = d.params.data() + 1 + nc + nc * nd;
+            kp.fconst[B] = (float)nc;
+            for (int c = 0; c < nc; ++c) {
+                double l = std::log(w[c]) - 0.5 * nd * std::log(2.0 * M_PI);
+                for (int i = 0; i < nd; ++i) { l -= std::log(sg[c * nd + i]); }
+                kp.fconst[B + 1 + c * S] = (float)l;
+                for (int i = 0; i < nd; ++i) {
+                    kp.fconst[B + 1 + c * S + 1 + i] = (float)m[c * nd + i];
+                    kp.fconst[B + 1 + c * S + 1 + md + i] = (float)(1.0 / sg[c * nd + i]);
+                }
+            }
+        }
+    }
+}
+
 static int fill_common(mcig_mci *h, KParams &kp)
 {
     memset(&kp, 0, sizeof(kp));
@@ -754,6 +801,16 @@ static int fill_common(mcig_mci *h, KParams &kp)
     kp.nrej = h->nrej.p;
     kp.key0 = (uint32_t)h->seed;
     kp.key1 = (uint32_t)(h->seed >> 32);
+    for (int r = 0; r < 10; ++r) { // Philox round keys
+        kp.rk[2 * r] = kp.key0 + (uint32_t)r * 0x9E3779B9u;
+        kp.rk[2 * r + 1] = kp.key1 + (uint32_t)r * 0xBB67AE85u;
+    }
+    for (int o = 0; o < kp.nobs; ++o) {
+        ObsDesc &od = kp.obs[o];
+        magic_div((uint32_t)std::max(od.bs, 1), od.bs_magic, od.bs_shift);
+        magic_div((uint32_t)od.nskip, od.sk_magic, od.sk_shift);
+    }
+    fill_fast_const(h, kp);
     if (h->replay) {
         kp.tape = h->tape.p;
         kp.tape_stride = h->tape_stride;
@@ -771,15 +828,25 @@ static bool fast_eligible(const mcig_mci *h)
 {
     if (h->prec == MCIG_PREC_FP64 || h->replay || h->ndim > 32 || h->pdfs.empty()) { return false; }
     if (h->movetype != MCIG_MOVE_ALL && h->movetype != MCIG_MOVE_VEC) { return false; }
+    if (h->movetype == MCIG_MOVE_VEC && h->ndim > 16) { return false; }
     for (auto &o : h->obs) {
         if (o.kind == MCIG_OBS_GAUSSX2) { return false; }
     }
-    return true;
+    int nprec = 0, nmix = 0; // one precision matrix and one mixture (<= 8 components) fit the parameter block
+    for (auto &d : h->pdfs) {
+        nprec += d.kind == MCIG_PDF_GAUSS_PREC;
+        nmix += d.kind == MCIG_PDF_GAUSS_MIX;
+        if (d.kind == MCIG_PDF_GAUSS_MIX && (int)d.params[0] > 8) { return false; }
+    }
+    return nprec <= 1 && nmix <= 1;
 }
 
 static int launch(mcig_mci *h, const KParams &kp)
 {
-    const int block = 128;
+    // 64 threads per block: with ~140 registers per thread seven blocks fit an
+    // SM, so 65,536 chains are resident in one wave, and small batches still
+    // spread over every SM
+    const int block = 64;
     const int grid = (int)((h->nchains + block - 1) / block);
     const bool small_n = kp.nsteps < ((int64_t)1 << 31); // 32-bit step counters in the register-resident kernel
     const bool fast = h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n);
@@ -788,7 +855,7 @@ static int launch(mcig_mci *h, const KParams &kp)
     if (fast) {
         if (!fast_eligible(h) || !small_n) { return set_err(MCIG_ERR_UNSUPPORTED, "configuration not served by the register-resident kernel"); }
         fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim));
-        smem += (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
+        smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
     } else {
         fn = mcig_generic_launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX);
     }

@@ -31,6 +31,7 @@
 #define MCIG_MAXTYPES 4
 #define MCIG_PERIODIC_MAXWRAP 64
 #define MCIG_MAXDIM 64
+#define MCIG_FCONST 2080 // floats of sampling-function data in the parameter block (register-resident kernel)
 
 enum { RNG_PHILOX = 0, RNG_TAPE = 1 };
 enum { KMODE_STEPS = 0, KMODE_SAMPLE = 1, KMODE_CALIB = 2 };
@@ -56,6 +57,8 @@ struct ObsDesc {
     void *data;   // device data (see layout above)
     int64_t nstore;
     int full32;   // Full data stored as float
+    // n / d == __umulhi(n, magic) >> shift for n < 2^31 (register-resident kernel)
+    uint32_t bs_magic, bs_shift, sk_magic, sk_shift;
 };
 
 struct KParams {
@@ -101,6 +104,12 @@ struct KParams {
     const double *step_max_i; // periodic: 0.5*(ub-lb) per index
     // error reporting
     int *status;
+    // register-resident kernel: Philox round keys (key + r*W for r = 0..9) and the
+    // sampling-function data at fixed offsets (Cholesky factor U[MAXD][MAXD] at 0,
+    // mixture [nc, per component: log-normalisation, m[MAXD], 1/s[MAXD]] at MAXD*MAXD),
+    // so that the unrolled loops read them as constant-bank operands
+    uint32_t rk[20];
+    float fconst[MCIG_FCONST];
 };
 
 // ------------------------------------------------------------------------
@@ -131,6 +140,22 @@ __device__ __forceinline__ P4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c
 // move and 1 + s for sub-step s of a MultiStepMove.
 enum { TAG_MOVE = 0, TAG_ACCEPT = 1, TAG_INDEX = 2 };
 
+// the same generator with the round keys precomputed (rk[2r], rk[2r+1] = key + r*W)
+__device__ __forceinline__ P4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const uint32_t *rk)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c0;
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ rk[2 * r];
+        const uint32_t n2 = hi0 ^ c3 ^ rk[2 * r + 1];
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return P4{c0, c1, c2, c3};
+}
+
 struct PhiloxCtx {
     uint32_t k0, k1, s0, s1, chain;
     __device__ __forceinline__ P4 block(uint32_t substep, uint32_t tag, uint32_t b) const
@@ -149,8 +174,9 @@ __device__ __forceinline__ double u01_d(uint32_t hi, uint32_t lo)
 // two standard normals from two uniforms (Box-Muller)
 __device__ __forceinline__ void box_muller_f(uint32_t w0, uint32_t w1, float &z0, float &z1)
 {
-    const float u = u01_open0_f(w0);
-    const float r = sqrtf(-2.0f * 0.69314718f * __log2f(u));
+    const float u = ((float)(w0 >> 8) + 0.5f) * 5.9604644775390625e-08f; // (0,1), never 0 or 1
+    const float t = -1.38629436f * __log2f(u);                            // -2 ln u > 0
+    const float r = t * rsqrtf(t);
     float s, c;
     __sincosf(6.28318530717958648f * (u01_f(w1) - 0.5f), &s, &c);
     z0 = r * c;

@@ -3,28 +3,32 @@
 // any product of sampling functions, observables without exp(), Philox draws.
 //
 // The walker (x, proposal) lives in registers: MAXD is a compile-time bound on
-// ndim and every coordinate loop is unrolled with compile-time indices, so no
-// per-thread local memory is touched in the step.  Shared memory holds
-//   - the sampling-function blob (Cholesky factor U of a precision matrix with
-//     row stride MAXD, mixture parameters), read with broadcast loads at
-//     compile-time offsets;
-//   - the running sums of Simple/Block accumulators, one slot per observable
-//     value and thread ([slot][thread], conflict-free), float+Kahan or double.
+// ndim and every coordinate loop is unrolled with compile-time indices.  The
+// walker is padded to MAXD coordinates whose step size is zero, so no
+// coordinate loop carries a predicate.  The sampling-function data (Cholesky
+// factor U of a precision matrix with row stride MAXD, mixture parameters) sits
+// in the kernel parameter block at fixed offsets, so the unrolled loops take it
+// as constant-bank operands without load instructions; the Philox round keys
+// are precomputed there too.  Shared memory holds the running sums of
+// Simple/Block accumulators, one slot per observable value and thread
+// ([slot][thread], conflict-free), float+Kahan or double.
 // Full accumulators store every sample straight to HBM, coalesced across the
 // warp (layout [nstore][nobs][nchains]).
 //
 // Semantics are those of the general kernel (mcig_generic.cuh) in float:
 // log-space Metropolis test log(u) <= log p(x') - log p(x), one Philox stream
-// per chain with the same counter layout, so a chain draws the same numbers in
+// per chain with the same counter layout, so a chain draws the same uniforms in
 // both kernels.
 #pragma once
 
 #include "mcig_common.cuh"
 
+// log density of the walker (padded to MAXD coordinates with zeros: padded
+// coordinates never move, and the parameter data is zero-padded, so no loop
+// needs a per-coordinate predicate)
 template <int MAXD>
-__device__ __forceinline__ float fast_logp(const KParams &p, const float *x, const float *blob)
+__device__ __forceinline__ float fast_logp(const KParams &p, const float *x)
 {
-    const int nd = p.ndim;
     float lp = 0.f;
     for (int k = 0; k < p.npdf; ++k) {
         const PdfDesc &d = p.pdf[k];
@@ -33,32 +37,25 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const float *x, con
         case MCIG_PDF_GAUSS: {
             float s = 0.f;
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) {
-                if (i < nd) { s = fmaf(x[i], x[i], s); }
-            }
+            for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); }
             lp -= s;
             break;
         }
         case MCIG_PDF_EXP: {
             float s = 0.f;
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) {
-                if (i < nd) { s += fabsf(x[i]); }
-            }
+            for (int i = 0; i < MAXD; ++i) { s += fabsf(x[i]); }
             lp -= s;
             break;
         }
-        case MCIG_PDF_GAUSS_PREC: { // -|U x|^2 / 2, U upper triangular, row stride MAXD
-            const float *U = blob + d.foff;
+        case MCIG_PDF_GAUSS_PREC: { // -|U x|^2 / 2, U upper triangular at fconst[0], row stride MAXD
             float q = 0.f;
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) {
-                if (i < nd) {
-                    float t = 0.f;
+                float t = 0.f;
 #pragma unroll
-                    for (int j = i; j < MAXD; ++j) { t = fmaf(U[i * MAXD + j], x[j], t); } // zero-padded beyond nd
-                    q = fmaf(t, t, q);
-                }
+                for (int j = i; j < MAXD; ++j) { t = fmaf(p.fconst[i * MAXD + j], x[j], t); }
+                q = fmaf(t, t, q);
             }
             lp = fmaf(-0.5f, q, lp);
             break;
@@ -72,29 +69,29 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const float *x, con
             lp = fmaf(-(float)d.c, s, lp);
             break;
         }
-        case MCIG_PDF_GAUSS_MIX: { // log sum_c exp(lc_c - |(x - m_c) / s_c|^2 / 2), per component stride 1 + 2 MAXD
-            const float *b = blob + d.foff;
-            const int nc = (int)b[0];
-            float e[16];
+        case MCIG_PDF_GAUSS_MIX: { // log sum_c exp(lc_c - |(x - m_c) / s_c|^2 / 2) at fconst[MAXD*MAXD], nc <= 8
+            constexpr int B = MAXD * MAXD;
+            const int nc = (int)p.fconst[B];
+            float e[8];
             float mx = -INFINITY;
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
+            for (int c = 0; c < 8; ++c) {
                 if (c < nc) {
-                    const float *cb = b + 1 + c * (1 + 2 * MAXD);
+                    constexpr int S = 1 + 2 * MAXD;
                     float a = 0.f;
 #pragma unroll
                     for (int i = 0; i < MAXD; ++i) {
-                        const float z = (x[i] - cb[1 + i]) * cb[1 + MAXD + i]; // zero beyond nd
+                        const float z = (x[i] - p.fconst[B + 1 + c * S + 1 + i]) * p.fconst[B + 1 + c * S + 1 + MAXD + i];
                         a = fmaf(z, z, a);
                     }
-                    a = fmaf(-0.5f, a, cb[0]);
+                    a = fmaf(-0.5f, a, p.fconst[B + 1 + c * S]);
                     e[c] = a;
                     mx = fmaxf(mx, a);
                 }
             }
             float sum = 0.f;
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
+            for (int c = 0; c < 8; ++c) {
                 if (c < nc) { sum += exp2f((e[c] - mx) * 1.44269504f); }
             }
             lp += mx + 0.69314718f * __log2f(sum);
@@ -104,6 +101,12 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const float *x, con
         }
     }
     return lp;
+}
+
+// n / d for n < 2^31 with the host-computed (magic, shift) of d
+__device__ __forceinline__ uint32_t fast_div(uint32_t n, uint32_t magic, uint32_t shift)
+{
+    return __umulhi(n, magic) >> shift;
 }
 
 template <bool KAHAN> struct FastSlot;
@@ -132,24 +135,31 @@ struct FastSampler {
     using ST = typename Slot::T;
     const KParams &p;
     const int c;
-    const float *blob;
     ST *slots; // [nobsdim][blockDim]
     float x[MAXD];
     float st[MCIG_MAXTYPES];
     float lp;
-    PhiloxCtx ph;
+    uint32_t s0, s1;
     uint64_t ctr;
 
-    __device__ FastSampler(const KParams &pp, int cc, const float *bl, ST *sl) : p(pp), c(cc), blob(bl), slots(sl)
+    __device__ FastSampler(const KParams &pp, int cc, ST *sl) : p(pp), c(cc), slots(sl)
     {
 #pragma unroll
         for (int i = 0; i < MAXD; ++i) { x[i] = (i < p.ndim) ? (float)p.x[(size_t)i * p.nchains + c] : 0.f; }
 #pragma unroll
         for (int t = 0; t < MCIG_MAXTYPES; ++t) { st[t] = (t < p.ntypes) ? (float)p.step[(size_t)t * p.nchains + c] : 0.f; }
         ctr = p.ctr[c];
-        ph.k0 = p.key0;
-        ph.k1 = p.key1;
-        ph.chain = (uint32_t)c;
+    }
+
+    // step size of coordinate i (0 for the padding beyond ndim)
+    __device__ __forceinline__ float step_i(int i) const
+    {
+        return (i < p.ndim) ? (p.ntypes == 1 ? st[0] : step_of(i)) : 0.f;
+    }
+
+    __device__ __forceinline__ P4 block(uint32_t tag, uint32_t b) const
+    {
+        return philox4x32_10_rk(s0, s1, (uint32_t)c, (tag << 12) | b, p.rk);
     }
 
     __device__ __forceinline__ float step_of(int i) const
@@ -165,37 +175,35 @@ struct FastSampler {
     // one Metropolis step (MCI::doStepMRT2, MCIntegrator.cpp:326-360)
     __device__ __forceinline__ bool step()
     {
-        ph.s0 = (uint32_t)ctr;
-        ph.s1 = (uint32_t)(ctr >> 32);
+        s0 = (uint32_t)ctr;
+        s1 = (uint32_t)(ctr >> 32);
         const bool gauss = p.srrd == MCIG_SRRD_GAUSSIAN;
         float xn[MAXD];
         int lo = 0, hi = p.ndim;
         if constexpr (MOVE == MCIG_MOVE_ALL) { // SRRDAllMove::trialMove
-            const bool one_type = p.ntypes == 1;
 #pragma unroll
             for (int b = 0; b < (MAXD + 3) / 4; ++b) {
-                float d[4] = {0.f, 0.f, 0.f, 0.f};
-                if (b * 4 < p.ndim) { move_draws<float>(ph.block(0, TAG_MOVE, b), gauss, d); }
+                float d[4];
+                move_draws<float>(block(TAG_MOVE, b), gauss, d);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int i = b * 4 + k;
-                    if (i < MAXD) { xn[i] = (i < p.ndim) ? fmaf(one_type ? st[0] : step_of(i), d[k], x[i]) : 0.f; }
+                    if (i < MAXD) { xn[i] = fmaf(step_i(i), d[k], x[i]); }
                 }
             }
         } else { // SRRDVecMove::trialMove
             const int nvecs = p.ndim / p.veclen;
-            const int vidx = (int)__umulhi(ph.block(0, TAG_INDEX, 0).a, (uint32_t)nvecs);
+            const int vidx = (int)__umulhi(block(TAG_INDEX, 0).a, (uint32_t)nvecs);
             lo = vidx * p.veclen;
             hi = lo + p.veclen;
-            const float s = step_of(lo);
 #pragma unroll
             for (int b = 0; b < (MAXD + 3) / 4; ++b) {
                 float d[4] = {0.f, 0.f, 0.f, 0.f};
-                if (b * 4 < hi && b * 4 + 4 > lo) { move_draws<float>(ph.block(0, TAG_MOVE, b), gauss, d); }
+                if (b * 4 < hi && b * 4 + 4 > lo) { move_draws<float>(block(TAG_MOVE, b), gauss, d); }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int i = b * 4 + k;
-                    if (i < MAXD) { xn[i] = (i >= lo && i < hi) ? fmaf(s, d[k], x[i]) : x[i]; }
+                    if (i < MAXD) { xn[i] = (i >= lo && i < hi) ? fmaf(step_i(i), d[k], x[i]) : x[i]; }
                 }
             }
         }
@@ -211,8 +219,8 @@ struct FastSampler {
                 }
             }
         }
-        const float lpn = fast_logp<MAXD>(p, xn, blob);
-        const float u = u01_f(ph.block(0, TAG_ACCEPT, 0).a);
+        const float lpn = fast_logp<MAXD>(p, xn);
+        const float u = u01_f(block(TAG_ACCEPT, 0).a);
         const bool acc = __log2f(u) <= (lpn - lp) * 1.44269504f;
         if (acc) {
 #pragma unroll
@@ -235,9 +243,7 @@ struct FastSampler {
         case MCIG_OBS_X2MEAN: {
             float s = 0.f;
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) {
-                if (i < nd) { s = fmaf(x[i], x[i], s); }
-            }
+            for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); } // padded coordinates are 0
             v[0] = od.kind == MCIG_OBS_X2SUM ? s : s / (float)nd;
             return 1;
         }
@@ -253,9 +259,7 @@ struct FastSampler {
         case MCIG_OBS_POLYNOM: {
             float s = 0.f;
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) {
-                if (i < nd) { s += x[i]; }
-            }
+            for (int i = 0; i < MAXD; ++i) { s += x[i]; }
             v[0] = s;
             return 1;
         }
@@ -307,9 +311,11 @@ struct FastSampler {
         for (int j = 0; j < MAXD; ++j) {
             if (j < nv) { Slot::add(sl[j * blockDim.x], v[j]); }
         }
-        if (od.acc == MCIG_ACC_BLOCK && (k + 1) % (uint32_t)od.bs == 0u) { // block mean = sum * (1./blocksize)
+        if (od.acc != MCIG_ACC_BLOCK) { return; }
+        const uint32_t blk = fast_div(k + 1, od.bs_magic, od.bs_shift);
+        if (blk * (uint32_t)od.bs == k + 1) { // block complete: mean = sum * (1./blocksize)
             const double normf = 1. / od.bs;
-            double *dst = (double *)od.data + (size_t)(k / (uint32_t)od.bs) * nv * p.nchains + c;
+            double *dst = (double *)od.data + (size_t)(blk - 1) * nv * p.nchains + c;
 #pragma unroll
             for (int j = 0; j < MAXD; ++j) {
                 if (j < nv) {
@@ -323,7 +329,7 @@ struct FastSampler {
     // n < 2^32 (checked on the host); accumulation indices in 32-bit arithmetic
     __device__ void run(int64_t n, bool sample)
     {
-        lp = fast_logp<MAXD>(p, x, blob);
+        lp = fast_logp<MAXD>(p, x);
         for (int j = 0; j < p.nobsdim && sample; ++j) { Slot::zero(slot(j)); }
         const uint32_t n32 = (uint32_t)n;
         uint32_t na = 0;
@@ -334,7 +340,10 @@ struct FastSampler {
                 const ObsDesc &od = p.obs[o];
                 const uint32_t ns = (uint32_t)od.nskip;
                 if (ns == 1u) { accumulate(od, r); }
-                else if (r % ns == 0u) { accumulate(od, r / ns); }
+                else {
+                    const uint32_t q = fast_div(r, od.sk_magic, od.sk_shift);
+                    if (q * ns == r) { accumulate(od, q); }
+                }
             }
         }
         if (sample) {
@@ -357,7 +366,7 @@ struct FastSampler {
         int cons = 0, counter = 0;
         int64_t na = 0;
         while ((p.nfind < 0 && cons < 5) || counter < p.nfind) {
-            lp = fast_logp<MAXD>(p, x, blob);
+            lp = fast_logp<MAXD>(p, x);
             na = 0;
             for (uint32_t r = 0; r < (uint32_t)MIN_STAT; ++r) { na += step() ? 1 : 0; }
             const double rate = (na > 0) ? (double)na / (double)MIN_STAT : 0.;
@@ -405,13 +414,10 @@ __global__ void __launch_bounds__(128) mcig_fast_kernel(const KParams p)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using ST = typename FastSlot<KAHAN>::T;
     ST *slots = (ST *)smem_raw;
-    float *blob = (float *)(smem_raw + (size_t)p.nobsdim * blockDim.x * sizeof(ST));
-    for (int i = threadIdx.x; i < p.fblob_len; i += blockDim.x) { blob[i] = p.fblob[i]; }
-    __syncthreads();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    FastSampler<MAXD, MOVE, KAHAN> s(p, c, blob, slots);
+    FastSampler<MAXD, MOVE, KAHAN> s(p, c, slots);
     if (p.mode == KMODE_CALIB) { s.calibrate(); }
     else { s.run(p.nsteps, p.mode == KMODE_SAMPLE); }
     s.store_state();

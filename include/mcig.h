@@ -164,6 +164,23 @@ int mcig_get_last_timings(const mcig_mci *h, double *ms4, int64_t *nlaunches);
 /* Philox4x32-10 block (for known-answer tests of the device generator) */
 int mcig_philox_block(int device, const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
+/* MJBlocker estimate of device data that allocates no device memory.  No
+ * counterpart in the reference: it serves callers that cannot call cudaMalloc
+ * (device memory owned by their own pool, allocation forbidden after start-up,
+ * or a loop that must not synchronize the device).  d_x[n][ndim], d_avg[ndim]
+ * and d_err[ndim] are device pointers; the work is queued on `stream`
+ * (cudaStream_t, NULL for the default stream) and the call returns without
+ * waiting.  Scratch is a file-scope device array of MCIG_NOALLOC_MAX_VALUES
+ * doubles (16 MiB on every device that loads the library, until exit):
+ * n*ndim above that is rejected with MCIG_ERR_INVALID_ARGUMENT, as is an n
+ * that is not a power of two.  The first call on a device looks up the
+ * array's device address (make that call before any stream capture).  All
+ * calls share the array, so calls that overlap on the GPU race: order them. */
+#define MCIG_NOALLOC_MAX_VALUES (1 << 21)
+#define MCIG_NOALLOC_MAX_DEVICES 64
+int mcig_mjblocker_estimate_noalloc(const double *d_x, int64_t n, int ndim, double *d_avg, double *d_err,
+                                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,7 @@ SIGNATURES = {
                                      P_double, P_int64]),
     "mcig_get_last_timings": (c_int, [c_void_p, P_double, P_int64]),
     "mcig_philox_block": (c_int, [c_int, P_uint32, P_uint32, P_uint32]),
+    "mcig_mjblocker_estimate_noalloc": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
 }
 
 

@@ -161,6 +161,63 @@ int mcig_accumulate_walk(int device, int obs_kind, const double *params, int npa
  * calibration, burn-in, sampling, estimation) and the number of kernels it launched. */
 int mcig_get_last_timings(const mcig_mci *h, double *ms4, int64_t *nlaunches);
 
+/* ------------------------------------------------------------------------
+ * Learned proposal (no counterpart in the reference's code; the reference's
+ * MCI API is extended by one call).  An affine-coupling normalizing flow
+ * (RealNVP: L coupling layers, MLP hidden width 128, bf16 tensor-core GEMMs
+ * with float accumulation, float master weights trained with Adam by
+ * maximum likelihood on chain states) is used as an independence
+ * Metropolis-Hastings proposal mixed with the local moves, so the target is
+ * unchanged.  Flow definition and parameter layout: oracle/flow_oracle.py.
+ * ------------------------------------------------------------------------ */
+typedef struct mcig_flow mcig_flow;
+int64_t mcig_flow_nparams(int ndim, int nlayers);
+/* ndim even, <= 32; nlayers <= 16; hidden must be 128 */
+int mcig_flow_create(int ndim, int nlayers, int hidden, uint64_t seed, int device, mcig_flow **out);
+int mcig_flow_destroy(mcig_flow *f);
+int mcig_flow_get_params(const mcig_flow *f, float *theta, int64_t *n);
+int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n);
+/* generative direction: x = f(z) and log q(x) for z[n][ndim] (host arrays) */
+int mcig_flow_forward(mcig_flow *f, const double *z, int64_t n, double *x, double *logq);
+/* density direction: z = f^-1(x) and log q(x) */
+int mcig_flow_inverse(mcig_flow *f, const double *x, int64_t n, double *z, double *logq);
+/* loss -mean log q(x) and its gradient (nparams floats) */
+int mcig_flow_loss_grad(mcig_flow *f, const double *x, int64_t n, double *loss, float *grad);
+/* `steps` Adam steps on minibatches of `batch` rows drawn from x[n][ndim] */
+int mcig_flow_train(mcig_flow *f, const double *x, int64_t n, int steps, int batch, double lr, double *last_loss);
+/* MCI::integrate with the learned proposal: calibration and burn-in with the
+ * local move, flow training on the chain states, then every `period` steps
+ * one flow proposal (period - 1 local steps in between; period 5 = 1:4),
+ * retraining every `refresh` steps.  Every observable must use a
+ * FullAccumulator (blocksize 1) with nskip 1.  flow_acceptance receives the
+ * acceptance rate of the flow proposals. */
+int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int period, int64_t refresh, int train_steps, int batch,
+                        double lr, double *average, double *error, int do_find_mrt2step, int do_decorrelation,
+                        double *flow_acceptance);
+
+/* ------------------------------------------------------------------------
+ * Batched integration: many independent MCI::integrate calls (one handle each,
+ * any ndim <= 64, its own sampling functions, move, observables and seed) run
+ * by one persistent kernel per ndim bucket (1-8, 9-16, 17-32, 33-64), whose
+ * warps pull (integral, chain) work units longest-first from an atomic queue;
+ * the launches, the estimators and the read-back are one CUDA graph.
+ * Handles must use MCIG_PREC_FP32, a sampling function, burn-in N >= 0 and
+ * observables with the Uncorrelated (Block/Full, double data) or Noop estimator.
+ * ------------------------------------------------------------------------ */
+typedef struct mcig_batch mcig_batch;
+int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, int do_find_mrt2step, int do_decorrelation,
+                      mcig_batch **out);
+/* one run of every integral; avg/err receive each handle's getNObsDim() values in handle order */
+int mcig_batch_run(mcig_batch *b, double *avg, double *err);
+int mcig_batch_destroy(mcig_batch *b);
+/* device time of the last run (graph launch to completion), milliseconds */
+int mcig_batch_last_ms(const mcig_batch *b, double *ms);
+/* chains per block of each ndim bucket (4 values) */
+int mcig_batch_get_blocks(const mcig_batch *b, int *blocks);
+int mcig_batch_set_blocks(mcig_batch *b, const int *blocks);
+/* time 32/64/128/256 chains per block per bucket, keep the fastest; cache file optional */
+int mcig_batch_autotune(mcig_batch *b, const char *cache_path);
+
 /* Philox4x32-10 block (for known-answer tests of the device generator) */
 int mcig_philox_block(int device, const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -57,6 +57,7 @@ inline Observable XSquared() { return {MCIG_OBS_X2MEAN, {}}; }
 inline Observable Constval(double v = 1.3) { return {MCIG_OBS_CONST, {v}}; }
 inline Observable Polynom() { return {MCIG_OBS_POLYNOM, {}}; }
 inline Observable GaussXSquared() { return {MCIG_OBS_GAUSSX2, {}}; }
+inline Observable XI(int i) { return {MCIG_OBS_XI, {double(i)}}; }
 inline Observable X2Blocks(const std::vector<int> &bounds /* b_0 < ... < b_nb */)
 {
     Observable o{MCIG_OBS_X2BLOCK, {double(bounds.size() - 1)}};

@@ -73,10 +73,11 @@ enum mcig_pdf_kind {
  *  POLYNOM  sum x_i                   [1]     (Polynom, :394-412)
  *  X2BLOCK  sum_{b_k<=i<b_k+1} x_i^2  [nb]    params [nb, b_0 .. b_nb]
  *  GAUSSX2  exp(-r2) r2 / (3 pi^1.5)  [1]     (GaussXSquared, :278-294)
+ *  XI       x_i of one index i        [1]     params [i]
  */
 enum mcig_obs_kind {
     MCIG_OBS_X2SUM = 0, MCIG_OBS_XND = 1, MCIG_OBS_X2 = 2, MCIG_OBS_X2MEAN = 3,
-    MCIG_OBS_CONST = 4, MCIG_OBS_POLYNOM = 5, MCIG_OBS_X2BLOCK = 6, MCIG_OBS_GAUSSX2 = 7
+    MCIG_OBS_CONST = 4, MCIG_OBS_POLYNOM = 5, MCIG_OBS_X2BLOCK = 6, MCIG_OBS_GAUSSX2 = 7, MCIG_OBS_XI = 8
 };
 
 /* arithmetic of the sampling loop on the device */

@@ -72,6 +72,24 @@ SIGNATURES = {
                                      P_double, P_int64]),
     "mcig_get_last_timings": (c_int, [c_void_p, P_double, P_int64]),
     "mcig_philox_block": (c_int, [c_int, P_uint32, P_uint32, P_uint32]),
+    "mcig_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_int, P_int64, c_int, c_int, ctypes.POINTER(c_void_p)]),
+    "mcig_batch_run": (c_int, [c_void_p, P_double, P_double]),
+    "mcig_batch_destroy": (c_int, [c_void_p]),
+    "mcig_batch_last_ms": (c_int, [c_void_p, P_double]),
+    "mcig_batch_get_blocks": (c_int, [c_void_p, P_int]),
+    "mcig_batch_set_blocks": (c_int, [c_void_p, P_int]),
+    "mcig_batch_autotune": (c_int, [c_void_p, ctypes.c_char_p]),
+    "mcig_flow_nparams": (c_int64, [c_int, c_int]),
+    "mcig_flow_create": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_int, ctypes.POINTER(c_void_p)]),
+    "mcig_flow_destroy": (c_int, [c_void_p]),
+    "mcig_flow_get_params": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float), P_int64]),
+    "mcig_flow_set_params": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int64]),
+    "mcig_flow_forward": (c_int, [c_void_p, P_double, c_int64, P_double, P_double]),
+    "mcig_flow_inverse": (c_int, [c_void_p, P_double, c_int64, P_double, P_double]),
+    "mcig_flow_loss_grad": (c_int, [c_void_p, P_double, c_int64, P_double, ctypes.POINTER(ctypes.c_float)]),
+    "mcig_flow_train": (c_int, [c_void_p, P_double, c_int64, c_int, c_int, c_double, P_double]),
+    "mcig_integrate_flow": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_int64, c_int, c_int, c_double, P_double,
+                                    P_double, c_int, c_int, P_double]),
     "mcig_mjblocker_estimate_noalloc": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
 }
 

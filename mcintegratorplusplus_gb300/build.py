@@ -28,6 +28,8 @@ UNITS = {
     "sample_fast_all32d": [],
     "sample_fast_vec": [],
     "mcig_noalloc": ["-fmad=false"],
+    "mcig_flow": [],
+    "sample_batch": [],
 }
 
 

@@ -6,17 +6,23 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <fstream>
+#include <numeric>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/mcig.h"
 #include "mcig_common.cuh"
 #include "mcig_estimators.cuh"
+#include "mcig_generic.cuh"
 #include "mcig_launchers.h"
+#include "mcig_batch.h"
 
 // ------------------------------------------------------------------------
 // errors
@@ -105,6 +111,7 @@ struct mcig_mci {
     int64_t ndecorr = -10000;
     int full32 = 0;
     int kernel_policy = 0; // 0 auto, 1 general kernel, 2 register-resident kernel
+    FastConst fc;          // constant data of the register-resident kernel
     // device chain state
     DBuf<double> x, step;
     DBuf<uint64_t> ctr;
@@ -188,6 +195,10 @@ static int obs_nvals(int ndim, int kind, const double *params, int np, int *nv)
         return MCIG_OK;
     case MCIG_OBS_XND:
     case MCIG_OBS_X2: *nv = ndim; return MCIG_OK;
+    case MCIG_OBS_XI:
+        if (np < 1 || (int)params[0] < 0 || (int)params[0] >= ndim) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "XI needs an index in [0, ndim)"); }
+        *nv = 1;
+        return MCIG_OK;
     case MCIG_OBS_X2BLOCK: {
         if (np < 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "X2BLOCK needs [nb, b0..b_nb]"); }
         const int nb = (int)params[0];
@@ -690,7 +701,7 @@ static void magic_div(uint32_t d, uint32_t &magic, uint32_t &shift)
 }
 
 // float data of the register-resident kernel at its fixed offsets (mcig_fast.cuh)
-static void fill_fast_const(const mcig_mci *h, KParams &kp)
+static void fill_fast_const(const mcig_mci *h, FastConst &kp)
 {
     const int nd = h->ndim;
     int md = 4;
@@ -802,15 +813,15 @@ static int fill_common(mcig_mci *h, KParams &kp)
     kp.key0 = (uint32_t)h->seed;
     kp.key1 = (uint32_t)(h->seed >> 32);
     for (int r = 0; r < 10; ++r) { // Philox round keys
-        kp.rk[2 * r] = kp.key0 + (uint32_t)r * 0x9E3779B9u;
-        kp.rk[2 * r + 1] = kp.key1 + (uint32_t)r * 0xBB67AE85u;
+        h->fc.rk[2 * r] = kp.key0 + (uint32_t)r * 0x9E3779B9u;
+        h->fc.rk[2 * r + 1] = kp.key1 + (uint32_t)r * 0xBB67AE85u;
     }
     for (int o = 0; o < kp.nobs; ++o) {
         ObsDesc &od = kp.obs[o];
         magic_div((uint32_t)std::max(od.bs, 1), od.bs_magic, od.bs_shift);
         magic_div((uint32_t)od.nskip, od.sk_magic, od.sk_shift);
     }
-    fill_fast_const(h, kp);
+    fill_fast_const(h, h->fc);
     if (h->replay) {
         kp.tape = h->tape.p;
         kp.tape_stride = h->tape_stride;
@@ -860,7 +871,7 @@ static int launch(mcig_mci *h, const KParams &kp)
         fn = mcig_generic_launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX);
     }
     if (!fn) { return set_err(MCIG_ERR_UNSUPPORTED, "no kernel for this configuration"); }
-    fn(kp, h->movetype, grid, block, smem, h->stream);
+    fn(kp, &h->fc, h->movetype, grid, block, smem, h->stream);
     ++h->launches;
     CK(cudaGetLastError());
     return MCIG_OK;
@@ -987,6 +998,7 @@ __global__ void walk_accumulate_kernel(int kind, const double *params, int ndim,
                 case MCIG_OBS_X2: for (int k = 0; k < ndim; ++k) { vals[k] = x[k] * x[k]; } break;
                 case MCIG_OBS_X2MEAN: { double s = x[0] * x[0]; for (int k = 1; k < ndim; ++k) { s = s + x[k] * x[k]; } vals[0] = s / ndim; break; }
                 case MCIG_OBS_CONST: vals[0] = params[0]; break;
+                case MCIG_OBS_XI: vals[0] = x[(int)params[0]]; break;
                 case MCIG_OBS_POLYNOM: { double s = 0.; for (int k = 0; k < ndim; ++k) { s = s + x[k]; } vals[0] = s; break; }
                 default: break;
                 }
@@ -1391,4 +1403,505 @@ extern "C" int mcig_philox_block(int device, const uint32_t ctr[4], const uint32
     CK(cudaMemcpy(out, d.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     d.release();
     return MCIG_OK;
+}
+
+// ------------------------------------------------------------------------
+// learned proposal: independence Metropolis-Hastings with the flow (mcig_flow.cu)
+// ------------------------------------------------------------------------
+struct mcig_flow;
+int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, float *d_out, float *d_logq, float *d_tape,
+                          cudaStream_t st);
+int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int steps, int batch, double lr, float *last_loss);
+int mcig_flow_dim(const mcig_flow *f);
+
+enum { TAG_FLOW_Z = 3, TAG_FLOW_ACCEPT = 4 };
+
+// walkers [ndim][nchains] (double) -> rows [nchains][ndim] (float)
+__global__ void walkers_to_rows_kernel(const double *x, int ndim, int nc, float *out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) { return; }
+    for (int i = 0; i < ndim; ++i) { out[(size_t)c * ndim + i] = (float)x[(size_t)i * nc + c]; }
+}
+
+// standard normal z for the flow proposal of cycle `cycle` (Philox, Box-Muller)
+__global__ void flow_z_kernel(KParams p, uint64_t cycle, float *z)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.nchains) { return; }
+    for (int b = 0; b < (p.ndim + 3) / 4; ++b) {
+        const P4 q = philox4x32_10((uint32_t)cycle, (uint32_t)(cycle >> 32), (uint32_t)c, (TAG_FLOW_Z << 12) | b,
+                                   p.key0 ^ 0x6A09E667u, p.key1 ^ 0xBB67AE85u);
+        float d[4];
+        box_muller_f(q.a, q.b, d[0], d[1]);
+        box_muller_f(q.c, q.d, d[2], d[3]);
+        for (int k = 0; k < 4; ++k) {
+            if (b * 4 + k < p.ndim) { z[(size_t)c * p.ndim + b * 4 + k] = d[k]; }
+        }
+    }
+}
+
+// Metropolis-Hastings test of the flow proposal x' for every chain:
+//   log u <= [log p(x') - log p(x)] + [log q(x) - log q(x')],
+// then the Full accumulators record the observables at the chain's position
+// (row `krow`, every observable has nskip 1 in this mode).
+__global__ void flow_accept_kernel(KParams p, const float *xprop, const float *lq_prop, const float *lq_cur, uint64_t cycle,
+                                   int64_t krow, int64_t *nacc_flow)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.nchains) { return; }
+    float x[MCIG_MAXDIM], xp[MCIG_MAXDIM];
+    for (int i = 0; i < p.ndim; ++i) {
+        x[i] = (float)p.x[(size_t)i * p.nchains + c];
+        xp[i] = xprop[(size_t)c * p.ndim + i];
+    }
+    float dl = lq_cur[c] - lq_prop[c];
+    for (int k = 0; k < p.npdf; ++k) { dl += pdf_logp_f(p, p.pdf[k], xp, p.fblob) - pdf_logp_f(p, p.pdf[k], x, p.fblob); }
+    const P4 q = philox4x32_10((uint32_t)cycle, (uint32_t)(cycle >> 32), (uint32_t)c, TAG_FLOW_ACCEPT << 12,
+                               p.key0 ^ 0x6A09E667u, p.key1 ^ 0xBB67AE85u);
+    const bool acc = isfinite(dl) && (__log2f(u01_f(q.a)) <= dl * 1.44269504f);
+    if (acc) {
+        for (int i = 0; i < p.ndim; ++i) {
+            x[i] = xp[i];
+            p.x[(size_t)i * p.nchains + c] = (double)xp[i];
+        }
+        nacc_flow[c] += 1;
+    }
+    float vals[2 * MCIG_MAXDIM + 8];
+    for (int o = 0; o < p.nobs; ++o) {
+        const ObsDesc &od = p.obs[o];
+        obs_eval<float>(p, od, x, vals);
+        const size_t base = (size_t)krow * od.nv * p.nchains + c;
+        for (int j = 0; j < od.nv; ++j) {
+            if (od.full32) { ((float *)od.data)[base + (size_t)j * p.nchains] = vals[j]; }
+            else { ((double *)od.data)[base + (size_t)j * p.nchains] = (double)vals[j]; }
+        }
+    }
+}
+
+extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int period, int64_t refresh, int train_steps,
+                                   int batch, double lr, double *average, double *error, int do_find, int do_decorr,
+                                   double *flow_acceptance)
+{
+    if (!h || !f) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle or flow is NULL"); }
+    if (mcig_flow_dim(f) != h->ndim) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "flow dimension differs from the integrator's"); }
+    if (h->prec == MCIG_PREC_FP64 || h->replay) { return set_err(MCIG_ERR_UNSUPPORTED, "the learned proposal runs in the float precision modes"); }
+    if (h->pdfs.empty()) { return set_err(MCIG_ERR_DOMAIN, "the learned proposal needs a sampling function"); }
+    if (period < 1 || nmc < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "period and nmc must be >= 1"); }
+    for (auto &o : h->obs) {
+        if (o.acc != MCIG_ACC_FULL || o.nskip != 1) {
+            return set_err(MCIG_ERR_UNSUPPORTED, "with the learned proposal every observable uses a FullAccumulator with nskip 1");
+        }
+    }
+    int rc;
+    if ((rc = validate_accumulators(h, nmc))) { return rc; }
+    CK(cudaSetDevice(h->device));
+    h->launches = 0;
+    for (double &m : h->ms) { m = 0.; }
+    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
+    KParams kp;
+    if ((rc = fill_common(h, kp))) { return rc; }
+    if ((rc = alloc_obs_data(h, h->obs, nmc, h->obsdata, h->obs_nstore, h->full32))) { return rc; }
+    const size_t nc = (size_t)h->nchains;
+    const int D = h->ndim;
+    DBuf<float> xf, z, xprop, lq_cur, lq_prop;
+    DBuf<int64_t> nflow;
+    if ((rc = xf.alloc(nc * D)) || (rc = z.alloc(nc * D)) || (rc = xprop.alloc(nc * D)) || (rc = lq_cur.alloc(nc)) ||
+        (rc = lq_prop.alloc(nc)) || (rc = nflow.alloc(nc))) {
+        return rc;
+    }
+    CK(cudaMemsetAsync(nflow.p, 0, nc * sizeof(int64_t), h->stream));
+    // the flow-step kernels read the float parameter blob from global memory
+    CK(cudaEventRecord(h->ev[0], h->stream));
+    if (do_find && h->nfind != 0) {
+        KParams c = kp;
+        c.mode = KMODE_CALIB;
+        c.nsteps = min_stat(h->ndim);
+        if ((rc = launch(h, c))) { return rc; }
+    }
+    CK(cudaEventRecord(h->ev[1], h->stream));
+    if (do_decorr && h->ndecorr > 0) {
+        KParams d = kp;
+        d.mode = KMODE_STEPS;
+        d.nsteps = h->ndecorr;
+        if ((rc = launch(h, d))) { return rc; }
+    }
+    const int tb = 128, tg = (int)((nc + tb - 1) / tb);
+    float loss = 0.f;
+    auto train = [&]() -> int {
+        walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
+        ++h->launches;
+        cudaError_t e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) { return set_err(MCIG_ERR_CUDA, "train: %s", cudaGetErrorString(e)); }
+        return mcig_flow_train_device(f, xf.p, (int64_t)nc, train_steps, batch, lr, &loss);
+    };
+    if (train_steps > 0 && (rc = train())) { return rc; }
+    CK(cudaEventRecord(h->ev[2], h->stream));
+    KParams sp = kp;
+    sp.mode = KMODE_SAMPLE;
+    for (size_t o = 0; o < h->obs.size(); ++o) {
+        sp.obs[o].data = h->obsdata[o].p;
+        sp.obs[o].nstore = h->obs_nstore[o];
+    }
+    int64_t step = 0, next_refresh = refresh > 0 ? refresh : INT64_MAX;
+    uint64_t cycle = 0;
+    std::vector<int64_t> hacc(nc);
+    while (step < nmc) {
+        const int64_t nloc = std::min<int64_t>(period - 1, nmc - step);
+        if (nloc > 0) {
+            KParams l = sp;
+            l.nsteps = nloc;
+            l.acc_offset = step;
+            if ((rc = launch(h, l))) { return rc; }
+            step += nloc;
+        }
+        if (step < nmc) {
+            walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
+            if ((rc = mcig_flow_pass_device(f, 1, xf.p, (int64_t)nc, z.p, lq_cur.p, nullptr, h->stream))) { return rc; }
+            flow_z_kernel<<<tg, tb, 0, h->stream>>>(sp, cycle, z.p);
+            if ((rc = mcig_flow_pass_device(f, 0, z.p, (int64_t)nc, xprop.p, lq_prop.p, nullptr, h->stream))) { return rc; }
+            flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, step, nflow.p);
+            h->launches += 5;
+            CK(cudaGetLastError());
+            ++step;
+            ++cycle;
+        }
+        if (step >= next_refresh && step < nmc) {
+            if (train_steps > 0 && (rc = train())) { return rc; }
+            next_refresh += refresh;
+        }
+    }
+    CK(cudaEventRecord(h->ev[3], h->stream));
+    if ((rc = estimate_all(h, h->obs, h->obsdata, h->obs_nstore, h->full32, h->chain_avg, h->chain_err))) { return rc; }
+    CK(cudaEventRecord(h->ev[4], h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 4; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev[k], h->ev[k + 1]);
+        h->ms[k] = ms;
+    }
+    CK(cudaMemcpy(hacc.data(), nflow.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (flow_acceptance) {
+        int64_t a = 0;
+        for (int64_t v : hacc) { a += v; }
+        *flow_acceptance = cycle > 0 ? (double)a / ((double)cycle * (double)nc) : 0.;
+    }
+    h->h_nacc.resize(nc);
+    h->h_nrej.resize(nc);
+    CK(cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    const int nod = nobsdim(h);
+    for (int i = 0; i < nod; ++i) {
+        double sa = 0., se = 0.;
+        for (size_t c = 0; c < nc; ++c) {
+            sa += h->chain_avg[c * nod + i];
+            se += h->chain_err[c * nod + i] * h->chain_err[c * nod + i];
+        }
+        average[i] = sa / (double)nc;
+        error[i] = std::sqrt(se) / (double)nc;
+    }
+    return MCIG_OK;
+}
+
+// ------------------------------------------------------------------------
+// batched integration of many independent integrals (persistent kernel + graph)
+// ------------------------------------------------------------------------
+#define MCIG_NBUCKETS 4
+static int bucket_of(int ndim) { return ndim <= 8 ? 0 : (ndim <= 16 ? 1 : (ndim <= 32 ? 2 : 3)); }
+
+struct mcig_batch {
+    std::vector<mcig_mci *> hs;
+    std::vector<int64_t> nmc;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaStream_t bst[MCIG_NBUCKETS] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[MCIG_NBUCKETS] = {nullptr, nullptr, nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
+    DBuf<KParams> cfg;
+    DBuf<BatchPhase> ph;
+    DBuf<int2> units[MCIG_NBUCKETS];
+    int nunits[MCIG_NBUCKETS] = {0, 0, 0, 0};
+    int block[MCIG_NBUCKETS] = {64, 64, 64, 64};
+    DBuf<int> counters;
+    DBuf<BatchSeries> series;
+    int nseries = 0;
+    DBuf<double> s_avg, s_err;
+    double *h_avg = nullptr, *h_err = nullptr; // pinned
+    std::vector<int> series_handle, series_slot; // series -> (handle, chain*nod + value)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    float last_ms = 0.f;
+};
+
+static int batch_grid(int nunits, int block)
+{
+    const int warps = (nunits + 31) / 32;
+    const int wpb = block / 32;
+    return std::max(1, std::min((warps + wpb - 1) / wpb, 152 * 16));
+}
+
+static int batch_build_graph(mcig_batch *b)
+{
+    if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(b->counters.p, 0, MCIG_NBUCKETS * sizeof(int), b->st);
+    cudaEventRecord(b->fork, b->st);
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) {
+        if (!b->nunits[k]) { continue; }
+        cudaStreamWaitEvent(b->bst[k], b->fork, 0);
+        mcig_batch_launch(b->cfg.p, b->ph.p, b->units[k].p, b->nunits[k], b->counters.p + k,
+                          batch_grid(b->nunits[k], b->block[k]), b->block[k], b->bst[k]);
+        cudaEventRecord(b->join[k], b->bst[k]);
+        cudaStreamWaitEvent(b->st, b->join[k], 0);
+    }
+    if (b->nseries) {
+        mcig_batch_estimate_launch(b->series.p, b->nseries, b->s_avg.p, b->s_err.p, b->st);
+        cudaMemcpyAsync(b->h_avg, b->s_avg.p, b->nseries * sizeof(double), cudaMemcpyDeviceToHost, b->st);
+        cudaMemcpyAsync(b->h_err, b->s_err.p, b->nseries * sizeof(double), cudaMemcpyDeviceToHost, b->st);
+    }
+    cudaError_t e = cudaStreamEndCapture(b->st, &b->graph);
+    if (e != cudaSuccess) { return set_err(MCIG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e)); }
+    CK(cudaGraphInstantiate(&b->gexec, b->graph, 0));
+    return MCIG_OK;
+}
+
+extern "C" int mcig_batch_destroy(mcig_batch *b)
+{
+    if (!b) { return MCIG_OK; }
+    cudaSetDevice(b->device);
+    if (b->st) { cudaStreamSynchronize(b->st); }
+    if (b->gexec) { cudaGraphExecDestroy(b->gexec); }
+    if (b->graph) { cudaGraphDestroy(b->graph); }
+    b->cfg.release(); b->ph.release(); b->counters.release(); b->series.release(); b->s_avg.release(); b->s_err.release();
+    for (auto &u : b->units) { u.release(); }
+    if (b->h_avg) { cudaFreeHost(b->h_avg); }
+    if (b->h_err) { cudaFreeHost(b->h_err); }
+    for (auto &s : b->bst) { if (s) { cudaStreamDestroy(s); } }
+    for (auto &e : b->join) { if (e) { cudaEventDestroy(e); } }
+    if (b->fork) { cudaEventDestroy(b->fork); }
+    if (b->t0) { cudaEventDestroy(b->t0); }
+    if (b->t1) { cudaEventDestroy(b->t1); }
+    if (b->st) { cudaStreamDestroy(b->st); }
+    delete b;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, int do_find, int do_decorr, mcig_batch **out)
+{
+    if (!handles || !nmc || n < 1 || !out) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: bad arguments"); }
+    *out = nullptr;
+    const int dev = handles[0]->device;
+    for (int i = 0; i < n; ++i) {
+        mcig_mci *h = handles[i];
+        if (!h || h->device != dev) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: every handle must exist on the same device"); }
+        if (h->prec != MCIG_PREC_FP32 || h->replay) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: handles must use MCIG_PREC_FP32 and Philox"); }
+        if (h->pdfs.empty()) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: every integral needs a sampling function"); }
+        if (nmc[i] < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: nmc must be >= 1"); }
+        if (do_decorr && h->ndecorr < 0) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: automatic decorrelation is not batched (use N > 0)"); }
+        for (auto &o : h->obs) {
+            const bool ok = (o.estimator == MCIG_EST_UNCORRELATED && o.acc != MCIG_ACC_SIMPLE) ||
+                            (o.estimator == MCIG_EST_NOOP);
+            if (!ok) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: observables use the Uncorrelated or Noop estimator"); }
+        }
+        int rc = validate_accumulators(h, nmc[i]);
+        if (rc) { return rc; }
+    }
+    CK(cudaSetDevice(dev));
+    mcig_batch *b = new mcig_batch();
+    b->hs.assign(handles, handles + n);
+    b->nmc.assign(nmc, nmc + n);
+    b->device = dev;
+    cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    for (auto &s : b->bst) { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); }
+    cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (auto &e : b->join) { cudaEventCreateWithFlags(&e, cudaEventDisableTiming); }
+    cudaEventCreate(&b->t0);
+    cudaEventCreate(&b->t1);
+    std::vector<KParams> cfg(n);
+    std::vector<BatchPhase> ph(n);
+    std::vector<std::vector<std::pair<double, int2>>> ub(MCIG_NBUCKETS);
+    int rc = MCIG_OK;
+    for (int i = 0; i < n && !rc; ++i) {
+        mcig_mci *h = handles[i];
+        if ((rc = fill_common(h, cfg[i]))) { break; }
+        if ((rc = alloc_obs_data(h, h->obs, nmc[i], h->obsdata, h->obs_nstore, h->full32))) { break; }
+        cudaStreamSynchronize(h->stream); // parameter uploads of the handle's stream
+        KParams &k = cfg[i];
+        k.mode = KMODE_SAMPLE;
+        k.nsteps = nmc[i];
+        for (size_t o = 0; o < h->obs.size(); ++o) {
+            k.obs[o].data = h->obsdata[o].p;
+            k.obs[o].nstore = h->obs_nstore[o];
+        }
+        ph[i].min_stat = min_stat(h->ndim);
+        ph[i].do_find = (do_find && h->nfind != 0) ? 1 : 0;
+        ph[i].ndecorr = do_decorr ? h->ndecorr : 0;
+        ph[i].movetype = h->movetype;
+        const double cost = (double)(nmc[i] + (ph[i].do_find ? 10 * ph[i].min_stat : 0) + ph[i].ndecorr) * (h->ndim + 8) *
+                            (h->movetype == MCIG_MOVE_MULTISTEP ? 1 + h->ms_nsteps : 1);
+        for (int64_t c = 0; c < h->nchains; ++c) { ub[bucket_of(h->ndim)].push_back({cost, make_int2(i, (int)c)}); }
+    }
+    if (!rc) { rc = b->cfg.alloc(n); }
+    if (!rc) { rc = b->ph.alloc(n); }
+    if (!rc) { rc = b->counters.alloc(MCIG_NBUCKETS); }
+    if (rc) { mcig_batch_destroy(b); return rc; }
+    cudaMemcpy(b->cfg.p, cfg.data(), n * sizeof(KParams), cudaMemcpyHostToDevice);
+    cudaMemcpy(b->ph.p, ph.data(), n * sizeof(BatchPhase), cudaMemcpyHostToDevice);
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) { // longest first: the tail of the queue holds the short units
+        std::stable_sort(ub[k].begin(), ub[k].end(), [](const std::pair<double, int2> &a, const std::pair<double, int2> &c) { return a.first > c.first; });
+        std::vector<int2> u(ub[k].size());
+        for (size_t j = 0; j < u.size(); ++j) { u[j] = ub[k][j].second; }
+        b->nunits[k] = (int)u.size();
+        if (!u.empty()) {
+            if ((rc = b->units[k].alloc(u.size()))) { mcig_batch_destroy(b); return rc; }
+            cudaMemcpy(b->units[k].p, u.data(), u.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        }
+    }
+    // estimator series: every (handle, observable, chain, value)
+    std::vector<BatchSeries> ser;
+    for (int i = 0; i < n; ++i) {
+        mcig_mci *h = handles[i];
+        int off = 0;
+        const int nod = nobsdim(h);
+        for (size_t o = 0; o < h->obs.size(); ++o) {
+            const ObsDef &d = h->obs[o];
+            for (int64_t c = 0; c < h->nchains; ++c) {
+                for (int j = 0; j < d.nv; ++j) {
+                    BatchSeries q;
+                    q.data = (const double *)h->obsdata[o].p + (size_t)j * h->nchains + c;
+                    q.n = h->obs_nstore[o];
+                    q.stride = (int64_t)d.nv * h->nchains;
+                    q.one_d = d.nv == 1;
+                    q.noop = d.estimator == MCIG_EST_NOOP;
+                    ser.push_back(q);
+                    b->series_handle.push_back(i);
+                    b->series_slot.push_back((int)(c * nod + off + j));
+                }
+            }
+            if (d.acc == MCIG_ACC_FULL && h->full32) { mcig_batch_destroy(b); return set_err(MCIG_ERR_UNSUPPORTED, "batch: FullAccumulator data must be double"); }
+            off += d.nv;
+        }
+    }
+    b->nseries = (int)ser.size();
+    if (b->nseries) {
+        if ((rc = b->series.alloc(ser.size())) || (rc = b->s_avg.alloc(ser.size())) || (rc = b->s_err.alloc(ser.size()))) {
+            mcig_batch_destroy(b);
+            return rc;
+        }
+        cudaMemcpy(b->series.p, ser.data(), ser.size() * sizeof(BatchSeries), cudaMemcpyHostToDevice);
+        cudaMallocHost(&b->h_avg, ser.size() * sizeof(double));
+        cudaMallocHost(&b->h_err, ser.size() * sizeof(double));
+    }
+    if ((rc = batch_build_graph(b))) { mcig_batch_destroy(b); return rc; }
+    *out = b;
+    return MCIG_OK;
+}
+
+// one run: the graph (persistent kernels + estimators + read-back), then the
+// MPIMCI combination per integral; avg/err hold the integrals' results in order
+extern "C" int mcig_batch_run(mcig_batch *b, double *avg, double *err)
+{
+    CK(cudaSetDevice(b->device));
+    CK(cudaEventRecord(b->t0, b->st));
+    CK(cudaGraphLaunch(b->gexec, b->st));
+    CK(cudaEventRecord(b->t1, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    cudaEventElapsedTime(&b->last_ms, b->t0, b->t1);
+    // per-chain results into the handles, then combination
+    for (auto *h : b->hs) {
+        const int nod = nobsdim(h);
+        h->chain_avg.assign((size_t)h->nchains * nod, 0.);
+        h->chain_err.assign((size_t)h->nchains * nod, 0.);
+    }
+    for (int s = 0; s < b->nseries; ++s) {
+        mcig_mci *h = b->hs[b->series_handle[s]];
+        h->chain_avg[b->series_slot[s]] = b->h_avg[s];
+        h->chain_err[b->series_slot[s]] = b->h_err[s];
+    }
+    size_t off = 0;
+    for (auto *h : b->hs) {
+        const int nod = nobsdim(h);
+        const size_t nc = (size_t)h->nchains;
+        for (int i = 0; i < nod; ++i) {
+            double sa = 0., se = 0.;
+            for (size_t c = 0; c < nc; ++c) {
+                sa += h->chain_avg[c * nod + i];
+                se += h->chain_err[c * nod + i] * h->chain_err[c * nod + i];
+            }
+            if (avg) { avg[off + i] = sa / (double)nc; }
+            if (err) { err[off + i] = std::sqrt(se) / (double)nc; }
+        }
+        off += nod;
+        h->h_nacc.resize(nc);
+        h->h_nrej.resize(nc);
+        cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost);
+        cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_batch_last_ms(const mcig_batch *b, double *ms)
+{
+    *ms = b->last_ms;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_batch_get_blocks(const mcig_batch *b, int *blocks)
+{
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) { blocks[k] = b->block[k]; }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_batch_set_blocks(mcig_batch *b, const int *blocks)
+{
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) {
+        if (blocks[k] < 32 || blocks[k] > 256 || blocks[k] % 32) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: block sizes are multiples of 32 in [32, 256]"); }
+    }
+    CK(cudaSetDevice(b->device));
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) { b->block[k] = blocks[k]; }
+    return batch_build_graph(b);
+}
+
+// Autotuner: for each ndim bucket, time the persistent kernel alone at 32, 64,
+// 128 and 256 chains per block and keep the fastest; the choice is cached in a
+// JSON file keyed by bucket and work size, so later batches of the same shape
+// skip the timing.  Tuning launches advance the chains like any sampling run.
+extern "C" int mcig_batch_autotune(mcig_batch *b, const char *cache_path)
+{
+    CK(cudaSetDevice(b->device));
+    std::map<std::string, int> cache;
+    if (cache_path) {
+        std::ifstream in(cache_path);
+        std::string key;
+        int val;
+        while (in >> key >> val) { cache[key] = val; }
+    }
+    const int cand[] = {32, 64, 128, 256};
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) {
+        if (!b->nunits[k]) { continue; }
+        int lg = 0;
+        while ((1 << lg) < b->nunits[k]) { ++lg; }
+        const std::string key = "bucket" + std::to_string(k) + "_units2^" + std::to_string(lg);
+        if (cache.count(key)) { b->block[k] = cache[key]; continue; }
+        float best = 1e30f;
+        int bestb = b->block[k];
+        for (int bs : cand) {
+            CK(cudaMemsetAsync(b->counters.p + k, 0, sizeof(int), b->st));
+            CK(cudaEventRecord(b->t0, b->st));
+            mcig_batch_launch(b->cfg.p, b->ph.p, b->units[k].p, b->nunits[k], b->counters.p + k,
+                              batch_grid(b->nunits[k], bs), bs, b->st);
+            CK(cudaEventRecord(b->t1, b->st));
+            CK(cudaStreamSynchronize(b->st));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, b->t0, b->t1);
+            if (ms < best) { best = ms; bestb = bs; }
+        }
+        b->block[k] = bestb;
+        cache[key] = bestb;
+    }
+    if (cache_path) {
+        std::ofstream o(cache_path);
+        for (auto &kv : cache) { o << kv.first << " " << kv.second << "\n"; }
+    }
+    return batch_build_graph(b);
 }

@@ -91,6 +91,7 @@ struct KParams {
     int64_t *tpos;          // tape cursor per chain
     int64_t *nacc, *nrej;   // counts of this launch (KMODE_CALIB: of the last iteration)
     uint8_t *bits;          // optional [nsteps][nchains] accept record
+    int64_t acc_offset;     // Full accumulators: row of this launch's first accumulation
     const uint8_t *active;  // optional: chains with active[c] == 0 skip this launch
     // random numbers
     uint32_t key0, key1;
@@ -104,10 +105,14 @@ struct KParams {
     const double *step_max_i; // periodic: 0.5*(ub-lb) per index
     // error reporting
     int *status;
-    // register-resident kernel: Philox round keys (key + r*W for r = 0..9) and the
-    // sampling-function data at fixed offsets (Cholesky factor U[MAXD][MAXD] at 0,
-    // mixture [nc, per component: log-normalisation, m[MAXD], 1/s[MAXD]] at MAXD*MAXD),
-    // so that the unrolled loops read them as constant-bank operands
+};
+
+// Register-resident kernel only: Philox round keys (key + r*W for r = 0..9) and
+// the sampling-function data at fixed offsets (Cholesky factor U[MAXD][MAXD] at
+// 0, mixture [nc, per component: log-normalisation, m[MAXD], 1/s[MAXD]] at
+// MAXD*MAXD), passed as a second kernel parameter so that the unrolled loops
+// read them as constant-bank operands.
+struct FastConst {
     uint32_t rk[20];
     float fconst[MCIG_FCONST];
 };

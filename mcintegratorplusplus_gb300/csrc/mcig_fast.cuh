@@ -27,7 +27,7 @@
 // coordinates never move, and the parameter data is zero-padded, so no loop
 // needs a per-coordinate predicate)
 template <int MAXD>
-__device__ __forceinline__ float fast_logp(const KParams &p, const float *x)
+__device__ __forceinline__ float fast_logp(const KParams &p, const FastConst &fc, const float *x)
 {
     float lp = 0.f;
     for (int k = 0; k < p.npdf; ++k) {
@@ -54,7 +54,7 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const float *x)
             for (int i = 0; i < MAXD; ++i) {
                 float t = 0.f;
 #pragma unroll
-                for (int j = i; j < MAXD; ++j) { t = fmaf(p.fconst[i * MAXD + j], x[j], t); }
+                for (int j = i; j < MAXD; ++j) { t = fmaf(fc.fconst[i * MAXD + j], x[j], t); }
                 q = fmaf(t, t, q);
             }
             lp = fmaf(-0.5f, q, lp);
@@ -71,7 +71,7 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const float *x)
         }
         case MCIG_PDF_GAUSS_MIX: { // log sum_c exp(lc_c - |(x - m_c) / s_c|^2 / 2) at fconst[MAXD*MAXD], nc <= 8
             constexpr int B = MAXD * MAXD;
-            const int nc = (int)p.fconst[B];
+            const int nc = (int)fc.fconst[B];
             float e[8];
             float mx = -INFINITY;
 #pragma unroll
@@ -81,10 +81,10 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const float *x)
                     float a = 0.f;
 #pragma unroll
                     for (int i = 0; i < MAXD; ++i) {
-                        const float z = (x[i] - p.fconst[B + 1 + c * S + 1 + i]) * p.fconst[B + 1 + c * S + 1 + MAXD + i];
+                        const float z = (x[i] - fc.fconst[B + 1 + c * S + 1 + i]) * fc.fconst[B + 1 + c * S + 1 + MAXD + i];
                         a = fmaf(z, z, a);
                     }
-                    a = fmaf(-0.5f, a, p.fconst[B + 1 + c * S]);
+                    a = fmaf(-0.5f, a, fc.fconst[B + 1 + c * S]);
                     e[c] = a;
                     mx = fmaxf(mx, a);
                 }
@@ -134,6 +134,7 @@ struct FastSampler {
     using Slot = FastSlot<KAHAN>;
     using ST = typename Slot::T;
     const KParams &p;
+    const FastConst &fc;
     const int c;
     ST *slots; // [nobsdim][blockDim]
     float x[MAXD];
@@ -142,7 +143,7 @@ struct FastSampler {
     uint32_t s0, s1;
     uint64_t ctr;
 
-    __device__ FastSampler(const KParams &pp, int cc, ST *sl) : p(pp), c(cc), slots(sl)
+    __device__ FastSampler(const KParams &pp, const FastConst &ff, int cc, ST *sl) : p(pp), fc(ff), c(cc), slots(sl)
     {
 #pragma unroll
         for (int i = 0; i < MAXD; ++i) { x[i] = (i < p.ndim) ? (float)p.x[(size_t)i * p.nchains + c] : 0.f; }
@@ -159,7 +160,7 @@ struct FastSampler {
 
     __device__ __forceinline__ P4 block(uint32_t tag, uint32_t b) const
     {
-        return philox4x32_10_rk(s0, s1, (uint32_t)c, (tag << 12) | b, p.rk);
+        return philox4x32_10_rk(s0, s1, (uint32_t)c, (tag << 12) | b, fc.rk);
     }
 
     __device__ __forceinline__ float step_of(int i) const
@@ -219,7 +220,7 @@ struct FastSampler {
                 }
             }
         }
-        const float lpn = fast_logp<MAXD>(p, xn);
+        const float lpn = fast_logp<MAXD>(p, fc, xn);
         const float u = u01_f(block(TAG_ACCEPT, 0).a);
         const bool acc = __log2f(u) <= (lpn - lp) * 1.44269504f;
         if (acc) {
@@ -256,6 +257,14 @@ struct FastSampler {
             for (int i = 0; i < MAXD; ++i) { v[i] = x[i] * x[i]; }
             return nd;
         case MCIG_OBS_CONST: v[0] = (float)p.params[od.poff]; return 1;
+        case MCIG_OBS_XI: {
+            const int idx = (int)p.params[od.poff];
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) { s = (i == idx) ? x[i] : s; }
+            v[0] = s;
+            return 1;
+        }
         case MCIG_OBS_POLYNOM: {
             float s = 0.f;
 #pragma unroll
@@ -291,14 +300,15 @@ struct FastSampler {
         const int nv = observe(od, v);
         if (od.acc == MCIG_ACC_FULL) { // FullAccumulator: one coalesced row per value
             const size_t stride = (size_t)p.nchains;
+            const size_t row = (size_t)p.acc_offset + k;
             if (od.full32) {
-                float *dst = (float *)od.data + (size_t)k * nv * stride + c;
+                float *dst = (float *)od.data + row * nv * stride + c;
 #pragma unroll
                 for (int j = 0; j < MAXD; ++j) {
                     if (j < nv) { dst[j * stride] = v[j]; }
                 }
             } else {
-                double *dst = (double *)od.data + (size_t)k * nv * stride + c;
+                double *dst = (double *)od.data + row * nv * stride + c;
 #pragma unroll
                 for (int j = 0; j < MAXD; ++j) {
                     if (j < nv) { dst[j * stride] = (double)v[j]; }
@@ -329,7 +339,7 @@ struct FastSampler {
     // n < 2^32 (checked on the host); accumulation indices in 32-bit arithmetic
     __device__ void run(int64_t n, bool sample)
     {
-        lp = fast_logp<MAXD>(p, x);
+        lp = fast_logp<MAXD>(p, fc, x);
         for (int j = 0; j < p.nobsdim && sample; ++j) { Slot::zero(slot(j)); }
         const uint32_t n32 = (uint32_t)n;
         uint32_t na = 0;
@@ -366,7 +376,7 @@ struct FastSampler {
         int cons = 0, counter = 0;
         int64_t na = 0;
         while ((p.nfind < 0 && cons < 5) || counter < p.nfind) {
-            lp = fast_logp<MAXD>(p, x);
+            lp = fast_logp<MAXD>(p, fc, x);
             na = 0;
             for (uint32_t r = 0; r < (uint32_t)MIN_STAT; ++r) { na += step() ? 1 : 0; }
             const double rate = (na > 0) ? (double)na / (double)MIN_STAT : 0.;
@@ -409,7 +419,7 @@ struct FastSampler {
 };
 
 template <int MAXD, int MOVE, bool KAHAN>
-__global__ void __launch_bounds__(128) mcig_fast_kernel(const KParams p)
+__global__ void __launch_bounds__(128) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using ST = typename FastSlot<KAHAN>::T;
@@ -417,16 +427,17 @@ __global__ void __launch_bounds__(128) mcig_fast_kernel(const KParams p)
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    FastSampler<MAXD, MOVE, KAHAN> s(p, c, slots);
+    FastSampler<MAXD, MOVE, KAHAN> s(p, fc, c, slots);
     if (p.mode == KMODE_CALIB) { s.calibrate(); }
     else { s.run(p.nsteps, p.mode == KMODE_SAMPLE); }
     s.store_state();
 }
 
 template <int MAXD, int MOVE, bool KAHAN>
-void mcig_fast_launch(const KParams &p, int /*movetype*/, int grid, int block, size_t smem, cudaStream_t st)
+void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, int grid, int block, size_t smem,
+                      cudaStream_t st)
 {
     auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN>;
     if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
-    k<<<grid, block, smem, st>>>(p);
+    k<<<grid, block, smem, st>>>(p, *fc);
 }

@@ -1,0 +1,953 @@
+// mcig_flow.cu -- affine-coupling normalizing flow on BF16 tensor cores, used as an
+// independence Metropolis-Hastings proposal (the learned form of the sampler).
+//
+// The flow (RealNVP couplings) and its parameter layout are defined in
+// oracle/flow_oracle.py, which restates them in numpy as the checker:
+//   layer l: a = y[perm_l[:d]], b = y[perm_l[d:]],
+//            h1 = relu(a W1 + b1), h2 = relu(h1 W2 + b2), o = h2 W3 + b3,
+//            s = S tanh(o[:d]/S), t = o[d:],
+//            generative  b <- b exp(s) + t,   density  b <- (b - t) exp(-s);
+//   base affine x = mu + exp(logsig) y;  log q = log N(z) - sum s - sum logsig.
+// Sizes: D <= 32 even, d = D/2 <= 16, hidden H = 128, L <= 16 layers.
+//
+// Kernels (one CTA = 128 samples, 8 warps; warp w owns rows 16w..16w+15):
+//   flow_pass_kernel     the L layers in one launch, generative or density
+//                        direction; GEMMs with mma.sync.m16n8k16 bf16 -> f32,
+//                        activations and weights staged in shared memory with
+//                        padded rows (conflict-free fragment loads); the density
+//                        direction can save a per-layer tape (a, b, s, t).
+//   flow_backward_kernel gradient of -mean log q through the density direction:
+//                        MLP recomputed from the tape, data gradients and weight
+//                        gradients as bf16 mma GEMMs, weight gradients reduced
+//                        across CTAs with float atomics.
+//   flow_adam_kernel     Adam on the float master parameters; flow_cast_kernel
+//                        rebuilds the bf16 weight copies.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mcig.h"
+#include "mcig_common.cuh"
+
+int mcig_set_last_error(int code, const char *msg); // mcig_capi.cu
+
+#define FLOW_H 128
+#define FLOW_MAXD 32
+#define FLOW_MAXL 16
+#define FLOW_ROWS 128   // samples per CTA
+#define FLOW_THREADS 256
+#define FLOW_SMAX 3.0f
+
+// shared-memory strides (in bf16 elements), padded so that a fragment load of
+// 8 rows x 4 words hits 32 different banks
+#define LDA_S 24   // a-half tile [128][16 (+8)]
+#define LDH_S 136  // hidden tiles [128][128 (+8)]
+#define LDO_S 40   // output-gradient tile [128][32 (+8)]
+
+struct FlowLayerPtrs {
+    const __nv_bfloat16 *W1n; // [H][16]   B operand of a*W1 (n-major, k contiguous)
+    const __nv_bfloat16 *W2n; // [H][H]    B operand of h1*W2
+    const __nv_bfloat16 *W3n; // [32][H]   B operand of h2*W3 (rows >= 2d zero)
+    const __nv_bfloat16 *W3t; // [H][32]   B operand of g_o*W3^T
+    const __nv_bfloat16 *W2t; // [H][H]    B operand of g_h2*W2^T
+    const __nv_bfloat16 *W1t; // [16][H]   B operand of g_h1*W1^T (rows >= d zero)
+    const float *b1, *b2, *b3;
+};
+
+struct FlowArgs {
+    int D, d, L, n;           // dimension, half, layers, samples
+    int dir;                  // 0 generative (z -> x), 1 density (x -> z)
+    const float *in;          // [n][D]
+    float *out;               // [n][D]
+    float *logq;              // [n]
+    const float *mu, *logsig; // base affine
+    const int *perm;          // [L][D]
+    float *tape;              // density direction: [L][n][4d] (a, b, s, t) or null
+    const __nv_bfloat16 *wb;  // bf16 weight copies
+    const float *theta;       // float master parameters
+    int64_t wstride;          // bf16 elements per layer in wb
+    int64_t pstride;          // floats per layer in theta
+};
+
+// ------------------------------------------------------------------------
+// bf16 tensor-core helpers
+// ------------------------------------------------------------------------
+__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16 *p) { return *(const uint32_t *)p; }
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi)
+{
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+// C[16 x 8 NT] += A[rows r0.., K] * B[K, 8 NT]; A row-major (k contiguous, stride lda),
+// B "n-major" (element (k, n) at Bn[n*ldb + k]).
+template <int KSTEPS, int NT>
+__device__ __forceinline__ void warp_gemm(const __nv_bfloat16 *A, int lda, int r0, const __nv_bfloat16 *Bn, int ldb,
+                                          float (&acc)[NT][4])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int ks = 0; ks < KSTEPS; ++ks) {
+        const int k0 = ks * 16 + 2 * t;
+        const uint32_t a0 = ld32(A + (r0 + g) * lda + k0);
+        const uint32_t a1 = ld32(A + (r0 + g + 8) * lda + k0);
+        const uint32_t a2 = ld32(A + (r0 + g) * lda + k0 + 8);
+        const uint32_t a3 = ld32(A + (r0 + g + 8) * lda + k0 + 8);
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const __nv_bfloat16 *bp = Bn + (nt * 8 + g) * ldb + k0;
+            mma_bf16(acc[nt], a0, a1, a2, a3, ld32(bp), ld32(bp + 8));
+        }
+    }
+}
+
+// C[16 rows (feature r0..) x 8 NT cols] += X^T G over the 128 samples of the tile:
+// A(row = feature i, k = sample) = X[sample][i], B(k = sample, n = j) = G[sample][j];
+// both gathered as bf16 pairs from row-major tiles.
+template <int NT>
+__device__ __forceinline__ void warp_gemm_tn(const __nv_bfloat16 *X, int ldx, int r0, const __nv_bfloat16 *Gm, int ldg,
+                                             float (&acc)[NT][4])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll 2
+    for (int ks = 0; ks < FLOW_ROWS / 16; ++ks) {
+        const int s0 = ks * 16 + 2 * t;
+        const uint32_t a0 = pack2(X[s0 * ldx + r0 + g], X[(s0 + 1) * ldx + r0 + g]);
+        const uint32_t a1 = pack2(X[s0 * ldx + r0 + g + 8], X[(s0 + 1) * ldx + r0 + g + 8]);
+        const uint32_t a2 = pack2(X[(s0 + 8) * ldx + r0 + g], X[(s0 + 9) * ldx + r0 + g]);
+        const uint32_t a3 = pack2(X[(s0 + 8) * ldx + r0 + g + 8], X[(s0 + 9) * ldx + r0 + g + 8]);
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const int n = nt * 8 + g;
+            const uint32_t b0 = pack2(Gm[s0 * ldg + n], Gm[(s0 + 1) * ldg + n]);
+            const uint32_t b1 = pack2(Gm[(s0 + 8) * ldg + n], Gm[(s0 + 9) * ldg + n]);
+            mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+        }
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void zero_acc(float (&acc)[NT][4])
+{
+#pragma unroll
+    for (int i = 0; i < NT; ++i) { acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f; }
+}
+
+// epilogue: bias (+ relu) -> bf16 row-major tile
+template <int NT>
+__device__ __forceinline__ void store_act(const float (&acc)[NT][4], const float *bias, bool relu, __nv_bfloat16 *H, int ldh,
+                                          int r0)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        const int c = nt * 8 + 2 * t;
+        float v0 = acc[nt][0] + bias[c], v1 = acc[nt][1] + bias[c + 1];
+        float v2 = acc[nt][2] + bias[c], v3 = acc[nt][3] + bias[c + 1];
+        if (relu) {
+            v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); v2 = fmaxf(v2, 0.f); v3 = fmaxf(v3, 0.f);
+        }
+        *(uint32_t *)(H + (r0 + g) * ldh + c) = pack2(__float2bfloat16_rn(v0), __float2bfloat16_rn(v1));
+        *(uint32_t *)(H + (r0 + g + 8) * ldh + c) = pack2(__float2bfloat16_rn(v2), __float2bfloat16_rn(v3));
+    }
+}
+
+// ------------------------------------------------------------------------
+// shared-memory plan of one CTA
+// ------------------------------------------------------------------------
+struct FlowSmem {
+    float Y[FLOW_ROWS][FLOW_MAXD + 1];
+    float O[FLOW_ROWS][FLOW_MAXD + 1];
+    __nv_bfloat16 A[FLOW_ROWS * LDA_S];
+    __nv_bfloat16 H1[FLOW_ROWS * LDH_S];
+    __nv_bfloat16 H2[FLOW_ROWS * LDH_S];
+    __nv_bfloat16 W1n[FLOW_H * LDA_S];
+    __nv_bfloat16 W2n[FLOW_H * LDH_S];
+    __nv_bfloat16 W3n[32 * LDH_S];
+    float bias[2 * FLOW_H + 32];
+    float logdet[FLOW_ROWS];
+};
+
+// bf16 weight copies per layer (flow_cast_kernel): offsets in elements
+#define WB_W1N 0
+#define WB_W2N (WB_W1N + FLOW_H * 16)
+#define WB_W3N (WB_W2N + FLOW_H * FLOW_H)
+#define WB_W3T (WB_W3N + 32 * FLOW_H)
+#define WB_W2T (WB_W3T + FLOW_H * 32)
+#define WB_W1T (WB_W2T + FLOW_H * FLOW_H)
+#define WB_LAYER (WB_W1T + 16 * FLOW_H)
+
+// float master layout per layer (oracle/flow_oracle.py): W1[d][H] b1[H] W2[H][H] b2[H] W3[H][2d] b3[2d]
+__host__ __device__ __forceinline__ int64_t pl_W1(int) { return 0; }
+__host__ __device__ __forceinline__ int64_t pl_b1(int d) { return (int64_t)d * FLOW_H; }
+__host__ __device__ __forceinline__ int64_t pl_W2(int d) { return pl_b1(d) + FLOW_H; }
+__host__ __device__ __forceinline__ int64_t pl_b2(int d) { return pl_W2(d) + FLOW_H * FLOW_H; }
+__host__ __device__ __forceinline__ int64_t pl_W3(int d) { return pl_b2(d) + FLOW_H; }
+__host__ __device__ __forceinline__ int64_t pl_b3(int d) { return pl_W3(d) + (int64_t)FLOW_H * 2 * d; }
+__host__ __device__ __forceinline__ int64_t pl_size(int d) { return pl_b3(d) + 2 * d; }
+
+__global__ void flow_cast_kernel(const float *theta, __nv_bfloat16 *wb, int d, int L)
+{
+    const int64_t per = WB_LAYER;
+    const int64_t total = per * L;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int l = (int)(i / per);
+        const int64_t e = i % per;
+        const float *P = theta + (int64_t)l * pl_size(d);
+        float v = 0.f;
+        if (e < WB_W2N) { // W1n[n][k] = W1[k][n]
+            const int n = (int)(e / 16), k = (int)(e % 16);
+            v = (k < d) ? P[pl_W1(d) + (int64_t)k * FLOW_H + n] : 0.f;
+        } else if (e < WB_W3N) { // W2n[n][k] = W2[k][n]
+            const int64_t q = e - WB_W2N;
+            const int n = (int)(q / FLOW_H), k = (int)(q % FLOW_H);
+            v = P[pl_W2(d) + (int64_t)k * FLOW_H + n];
+        } else if (e < WB_W3T) { // W3n[n][k] = W3[k][n], n < 2d
+            const int64_t q = e - WB_W3N;
+            const int n = (int)(q / FLOW_H), k = (int)(q % FLOW_H);
+            v = (n < 2 * d) ? P[pl_W3(d) + (int64_t)k * 2 * d + n] : 0.f;
+        } else if (e < WB_W2T) { // W3t[n=h][k=o] = W3[h][o]
+            const int64_t q = e - WB_W3T;
+            const int n = (int)(q / 32), k = (int)(q % 32);
+            v = (k < 2 * d) ? P[pl_W3(d) + (int64_t)n * 2 * d + k] : 0.f;
+        } else if (e < WB_W1T) { // W2t[n=h1][k=h2] = W2[h1][h2]
+            const int64_t q = e - WB_W2T;
+            v = P[pl_W2(d) + q];
+        } else { // W1t[n=a][k=h1] = W1[a][h1]
+            const int64_t q = e - WB_W1T;
+            const int n = (int)(q / FLOW_H), k = (int)(q % FLOW_H);
+            v = (n < d) ? P[pl_W1(d) + (int64_t)n * FLOW_H + k] : 0.f;
+        }
+        wb[i] = __float2bfloat16_rn(v);
+    }
+}
+
+// cooperative copy of a bf16 matrix [rows][cols] (global, dense) into a padded smem tile
+__device__ __forceinline__ void load_tile(__nv_bfloat16 *dst, int ld, const __nv_bfloat16 *src, int rows, int cols)
+{
+    const int words = rows * cols / 2;
+    for (int i = threadIdx.x; i < words; i += blockDim.x) {
+        const int r = (2 * i) / cols, c = (2 * i) % cols;
+        *(uint32_t *)(dst + r * ld + c) = *(const uint32_t *)(src + 2 * i);
+    }
+}
+
+// the MLP of one layer on the a-half in s.A: s.H1, s.H2 (bf16) and, if want_o, s.O (float)
+__device__ void layer_mlp(FlowSmem &s, const float *P, int d, bool want_o)
+{
+    const int warp = threadIdx.x >> 5, r0 = warp * 16;
+    for (int i = threadIdx.x; i < FLOW_H; i += blockDim.x) {
+        s.bias[i] = P[pl_b1(d) + i];
+        s.bias[FLOW_H + i] = P[pl_b2(d) + i];
+    }
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) { s.bias[2 * FLOW_H + i] = (i < 2 * d) ? P[pl_b3(d) + i] : 0.f; }
+    __syncthreads();
+    {
+        float acc[16][4];
+        zero_acc(acc);
+        warp_gemm<1, 16>(s.A, LDA_S, r0, s.W1n, LDA_S, acc);
+        store_act(acc, s.bias, true, s.H1, LDH_S, r0);
+    }
+    __syncthreads();
+    {
+        float acc[16][4];
+        zero_acc(acc);
+        warp_gemm<FLOW_H / 16, 16>(s.H1, LDH_S, r0, s.W2n, LDH_S, acc);
+        store_act(acc, s.bias + FLOW_H, true, s.H2, LDH_S, r0);
+    }
+    __syncthreads();
+    if (want_o) {
+        float acc[4][4];
+        zero_acc(acc);
+        warp_gemm<FLOW_H / 16, 4>(s.H2, LDH_S, r0, s.W3n, LDH_S, acc);
+        const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            const int c = nt * 8 + 2 * t;
+            s.O[r0 + g][c] = acc[nt][0] + s.bias[2 * FLOW_H + c];
+            s.O[r0 + g][c + 1] = acc[nt][1] + s.bias[2 * FLOW_H + c + 1];
+            s.O[r0 + g + 8][c] = acc[nt][2] + s.bias[2 * FLOW_H + c];
+            s.O[r0 + g + 8][c + 1] = acc[nt][3] + s.bias[2 * FLOW_H + c + 1];
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void load_layer_weights(FlowSmem &s, const __nv_bfloat16 *wl)
+{
+    load_tile(s.W1n, LDA_S, wl + WB_W1N, FLOW_H, 16);
+    load_tile(s.W2n, LDH_S, wl + WB_W2N, FLOW_H, FLOW_H);
+    load_tile(s.W3n, LDH_S, wl + WB_W3N, 32, FLOW_H);
+}
+
+__global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FlowSmem &s = *(FlowSmem *)smem_raw;
+    const int base = blockIdx.x * FLOW_ROWS;
+    const int D = f.D, d = f.d;
+    const int rows = min(FLOW_ROWS, f.n - base);
+    // load the tile (rows beyond n are zero)
+    for (int i = threadIdx.x; i < FLOW_ROWS * D; i += blockDim.x) {
+        const int r = i / D, c = i % D;
+        float v = (r < rows) ? f.in[(int64_t)(base + r) * D + c] : 0.f;
+        if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); } // density: undo the base affine first
+        s.Y[r][c] = v;
+    }
+    for (int i = threadIdx.x; i < FLOW_ROWS; i += blockDim.x) { s.logdet[i] = 0.f; }
+    __syncthreads();
+    for (int step = 0; step < f.L; ++step) {
+        const int l = (f.dir == 0) ? step : f.L - 1 - step;
+        const int *perm = f.perm + l * D;
+        load_layer_weights(s, f.wb + (int64_t)l * f.wstride);
+        // a-half as bf16 (columns d..15 zero)
+        for (int i = threadIdx.x; i < FLOW_ROWS * 16; i += blockDim.x) {
+            const int r = i / 16, c = i % 16;
+            s.A[r * LDA_S + c] = __float2bfloat16_rn(c < d ? s.Y[r][perm[c]] : 0.f);
+        }
+        __syncthreads();
+        layer_mlp(s, f.theta + (int64_t)l * f.pstride, d, true);
+        // coupling, one thread per sample
+        for (int r = threadIdx.x; r < FLOW_ROWS; r += blockDim.x) {
+            float ld = 0.f;
+            for (int j = 0; j < d; ++j) {
+                const float sj = FLOW_SMAX * tanhf(s.O[r][j] / FLOW_SMAX);
+                const float tj = s.O[r][d + j];
+                const int bj = perm[d + j];
+                const float bin = s.Y[r][bj];
+                float bout;
+                if (f.dir == 0) { bout = bin * __expf(sj) + tj; }
+                else { bout = (bin - tj) * __expf(-sj); }
+                if (f.tape && r < rows) {
+                    float *tp = f.tape + ((int64_t)l * f.n + base + r) * 4 * d;
+                    tp[j] = s.Y[r][perm[j]];  // a
+                    tp[d + j] = bout;         // b (density direction: the layer's output half)
+                    tp[2 * d + j] = sj;
+                    tp[3 * d + j] = tj;
+                }
+                s.Y[r][bj] = bout;
+                ld += sj;
+            }
+            s.logdet[r] += ld;
+        }
+        __syncthreads();
+    }
+    // output and log q
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+        float zz = 0.f, ls = 0.f;
+        for (int c = 0; c < D; ++c) { ls += f.logsig[c]; }
+        if (f.dir == 0) { // z was the input
+            for (int c = 0; c < D; ++c) {
+                const float z = f.in[(int64_t)(base + r) * D + c];
+                zz += z * z;
+                f.out[(int64_t)(base + r) * D + c] = f.mu[c] + __expf(f.logsig[c]) * s.Y[r][c];
+            }
+        } else {
+            for (int c = 0; c < D; ++c) {
+                const float z = s.Y[r][c];
+                zz += z * z;
+                f.out[(int64_t)(base + r) * D + c] = z;
+            }
+        }
+        f.logq[base + r] = -0.5f * zz - 0.91893853320467274f * D - s.logdet[r] - ls;
+    }
+}
+
+// ------------------------------------------------------------------------
+// backward: gradient of -mean log q through the density direction
+// ------------------------------------------------------------------------
+struct FlowBwdSmem {
+    float G[FLOW_ROWS][FLOW_MAXD + 1];     // d loss / d y of the current level
+    __nv_bfloat16 A[FLOW_ROWS * LDA_S];
+    __nv_bfloat16 H1[FLOW_ROWS * LDH_S];
+    __nv_bfloat16 H2[FLOW_ROWS * LDH_S];
+    __nv_bfloat16 GO[FLOW_ROWS * LDO_S];  // d loss / d o (bf16)
+    __nv_bfloat16 GH2[FLOW_ROWS * LDH_S]; // d loss / d h2 (pre-activation)
+    __nv_bfloat16 GH1[FLOW_ROWS * LDH_S]; // d loss / d h1 (pre-activation)
+    __nv_bfloat16 W1n[FLOW_H * LDA_S];
+    __nv_bfloat16 W2n[FLOW_H * LDH_S];
+    __nv_bfloat16 W3n[FLOW_H * LDO_S];    // W3n [32][LDH_S], later W3t [H][32] with stride LDO_S
+    float bias[2 * FLOW_H + 32];
+    float red[2 * FLOW_H + 32];           // bias-gradient sums of the tile
+};
+
+struct FlowBwdArgs {
+    int D, d, L, n;
+    float inv_batch;
+    const float *z;        // [n][D] output of the density pass
+    const float *tape;     // [L][n][4d]
+    const int *perm;
+    const __nv_bfloat16 *wb;
+    const float *theta;
+    float *grad;           // float gradient, same layout as theta (zeroed by the caller)
+    const float *x;        // [n][D] data (for mu / logsig)
+    const float *mu, *logsig;
+    int64_t wstride, pstride, base_off; // base_off: offset of mu in theta
+};
+
+__global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs f)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FlowBwdSmem &s = *(FlowBwdSmem *)smem_raw;
+    const int base = blockIdx.x * FLOW_ROWS;
+    const int D = f.D, d = f.d;
+    const int rows = min(FLOW_ROWS, f.n - base);
+    const int warp = threadIdx.x >> 5, r0 = warp * 16;
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int i = threadIdx.x; i < FLOW_ROWS * D; i += blockDim.x) {
+        const int r = i / D, c = i % D;
+        s.G[r][c] = (r < rows) ? f.z[(int64_t)(base + r) * D + c] * f.inv_batch : 0.f; // d(0.5|z|^2)/dz / B
+    }
+    __syncthreads();
+    for (int l = 0; l < f.L; ++l) { // reverse of the density direction
+        const int *perm = f.perm + l * D;
+        const float *P = f.theta + (int64_t)l * f.pstride;
+        float *GP = f.grad + (int64_t)l * f.pstride;
+        const __nv_bfloat16 *wl = f.wb + (int64_t)l * f.wstride;
+        load_tile(s.W1n, LDA_S, wl + WB_W1N, FLOW_H, 16);
+        load_tile(s.W2n, LDH_S, wl + WB_W2N, FLOW_H, FLOW_H);
+        load_tile(s.W3n, LDH_S, wl + WB_W3N, 32, FLOW_H);
+        for (int i = threadIdx.x; i < FLOW_ROWS * 16; i += blockDim.x) {
+            const int r = i / 16, c = i % 16;
+            const float v = (r < rows && c < d) ? f.tape[((int64_t)l * f.n + base + r) * 4 * d + c] : 0.f;
+            s.A[r * LDA_S + c] = __float2bfloat16_rn(v);
+        }
+        for (int i = threadIdx.x; i < 2 * FLOW_H + 32; i += blockDim.x) { s.red[i] = 0.f; }
+        __syncthreads();
+        // recompute h1, h2 (same bf16 GEMMs as the pass kernel)
+        for (int i = threadIdx.x; i < FLOW_H; i += blockDim.x) {
+            s.bias[i] = P[pl_b1(d) + i];
+            s.bias[FLOW_H + i] = P[pl_b2(d) + i];
+        }
+        __syncthreads();
+        {
+            float acc[16][4];
+            zero_acc(acc);
+            warp_gemm<1, 16>(s.A, LDA_S, r0, s.W1n, LDA_S, acc);
+            store_act(acc, s.bias, true, s.H1, LDH_S, r0);
+        }
+        __syncthreads();
+        {
+            float acc[16][4];
+            zero_acc(acc);
+            warp_gemm<FLOW_H / 16, 16>(s.H1, LDH_S, r0, s.W2n, LDH_S, acc);
+            store_act(acc, s.bias + FLOW_H, true, s.H2, LDH_S, r0);
+        }
+        __syncthreads();
+        // coupling backward, one thread per sample: g_o = [g_sraw, g_t], g on the b half
+        for (int r = threadIdx.x; r < FLOW_ROWS; r += blockDim.x) {
+            const float *tp = f.tape + ((int64_t)l * f.n + base + (r < rows ? r : 0)) * 4 * d;
+            for (int j = 0; j < 32; ++j) {
+                float go = 0.f;
+                if (r < rows && j < 2 * d) {
+                    const int jj = j < d ? j : j - d;
+                    const int bj = perm[d + jj];
+                    const float gb = s.G[r][bj];
+                    const float sj = tp[2 * d + jj];
+                    const float e = __expf(-sj);
+                    if (j < d) {
+                        const float gs = -gb * tp[d + jj] + f.inv_batch; // d/ds of (b' - t) e^-s, plus the sum(s) term
+                        go = gs * (1.f - (sj / FLOW_SMAX) * (sj / FLOW_SMAX));
+                    } else {
+                        go = -gb * e;
+                    }
+                }
+                s.GO[r * LDO_S + j] = __float2bfloat16_rn(go);
+                atomicAdd(&s.red[2 * FLOW_H + j], go);
+            }
+        }
+        __syncthreads();
+        // b-half gradient passes through: g_b' = g_b e^{-s}
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const float *tp = f.tape + ((int64_t)l * f.n + base + r) * 4 * d;
+            for (int j = 0; j < d; ++j) {
+                const int bj = perm[d + j];
+                s.G[r][bj] = s.G[r][bj] * __expf(-tp[2 * d + j]);
+            }
+        }
+        // g_h2 = (g_o W3^T) * relu'(h2): W3t [H][32] into the W3n buffer with stride LDO_S
+        load_tile(s.W3n, LDO_S, wl + WB_W3T, FLOW_H, 32);
+        __syncthreads();
+        {
+            float acc[16][4];
+            zero_acc(acc);
+            warp_gemm<2, 16>(s.GO, LDO_S, r0, s.W3n, LDO_S, acc);
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                float v[4];
+                v[0] = __bfloat162float(s.H2[(r0 + g) * LDH_S + c]) > 0.f ? acc[nt][0] : 0.f;
+                v[1] = __bfloat162float(s.H2[(r0 + g) * LDH_S + c + 1]) > 0.f ? acc[nt][1] : 0.f;
+                v[2] = __bfloat162float(s.H2[(r0 + g + 8) * LDH_S + c]) > 0.f ? acc[nt][2] : 0.f;
+                v[3] = __bfloat162float(s.H2[(r0 + g + 8) * LDH_S + c + 1]) > 0.f ? acc[nt][3] : 0.f;
+                *(uint32_t *)(s.GH2 + (r0 + g) * LDH_S + c) = pack2(__float2bfloat16_rn(v[0]), __float2bfloat16_rn(v[1]));
+                *(uint32_t *)(s.GH2 + (r0 + g + 8) * LDH_S + c) = pack2(__float2bfloat16_rn(v[2]), __float2bfloat16_rn(v[3]));
+                atomicAdd(&s.red[FLOW_H + c], v[0] + v[2]);
+                atomicAdd(&s.red[FLOW_H + c + 1], v[1] + v[3]);
+            }
+        }
+        __syncthreads();
+        // dW3 = h2^T g_o: rows h (16 per warp), 4 n-tiles over the 32 outputs
+        {
+            float acc[4][4];
+            zero_acc(acc);
+            warp_gemm_tn<4>(s.H2, LDH_S, r0, s.GO, LDO_S, acc);
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                if (c < 2 * d) {
+                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g) * 2 * d + c], acc[nt][0]);
+                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g + 8) * 2 * d + c], acc[nt][2]);
+                }
+                if (c + 1 < 2 * d) {
+                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g) * 2 * d + c + 1], acc[nt][1]);
+                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g + 8) * 2 * d + c + 1], acc[nt][3]);
+                }
+            }
+        }
+        // g_h1 = (g_h2 W2^T) * relu'(h1): W2t [H][H] into the W2n buffer
+        __syncthreads();
+        load_tile(s.W2n, LDH_S, wl + WB_W2T, FLOW_H, FLOW_H);
+        __syncthreads();
+        {
+            float acc[16][4];
+            zero_acc(acc);
+            warp_gemm<FLOW_H / 16, 16>(s.GH2, LDH_S, r0, s.W2n, LDH_S, acc);
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                float v[4];
+                v[0] = __bfloat162float(s.H1[(r0 + g) * LDH_S + c]) > 0.f ? acc[nt][0] : 0.f;
+                v[1] = __bfloat162float(s.H1[(r0 + g) * LDH_S + c + 1]) > 0.f ? acc[nt][1] : 0.f;
+                v[2] = __bfloat162float(s.H1[(r0 + g + 8) * LDH_S + c]) > 0.f ? acc[nt][2] : 0.f;
+                v[3] = __bfloat162float(s.H1[(r0 + g + 8) * LDH_S + c + 1]) > 0.f ? acc[nt][3] : 0.f;
+                *(uint32_t *)(s.GH1 + (r0 + g) * LDH_S + c) = pack2(__float2bfloat16_rn(v[0]), __float2bfloat16_rn(v[1]));
+                *(uint32_t *)(s.GH1 + (r0 + g + 8) * LDH_S + c) = pack2(__float2bfloat16_rn(v[2]), __float2bfloat16_rn(v[3]));
+                atomicAdd(&s.red[c], v[0] + v[2]);
+                atomicAdd(&s.red[c + 1], v[1] + v[3]);
+            }
+        }
+        // dW2 = h1^T g_h2: rows h1 (16 per warp) x 128 outputs
+        {
+            float acc[16][4];
+            zero_acc(acc);
+            warp_gemm_tn<16>(s.H1, LDH_S, r0, s.GH2, LDH_S, acc);
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g) * FLOW_H + c], acc[nt][0]);
+                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g) * FLOW_H + c + 1], acc[nt][1]);
+                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g + 8) * FLOW_H + c], acc[nt][2]);
+                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g + 8) * FLOW_H + c + 1], acc[nt][3]);
+            }
+        }
+        __syncthreads();
+        // g_a = g_h1 W1^T: W1t [16][H] into the W1n buffer region sized [16][LDH_S] (it fits in W2n)
+        load_tile(s.W2n, LDH_S, wl + WB_W1T, 16, FLOW_H);
+        __syncthreads();
+        {
+            float acc[2][4];
+            zero_acc(acc);
+            warp_gemm<FLOW_H / 16, 2>(s.GH1, LDH_S, r0, s.W2n, LDH_S, acc);
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                // accumulate into G on the a-half (direct term already there)
+                if (c < d) {
+                    if (r0 + g < rows) { s.G[r0 + g][perm[c]] += acc[nt][0]; }
+                    if (r0 + g + 8 < rows) { s.G[r0 + g + 8][perm[c]] += acc[nt][2]; }
+                }
+                if (c + 1 < d) {
+                    if (r0 + g < rows) { s.G[r0 + g][perm[c + 1]] += acc[nt][1]; }
+                    if (r0 + g + 8 < rows) { s.G[r0 + g + 8][perm[c + 1]] += acc[nt][3]; }
+                }
+            }
+        }
+        // dW1 = a^T g_h1: only warp rows 0..15 (the padded a-half)
+        if (warp == 0) {
+            float acc[16][4];
+            zero_acc(acc);
+            warp_gemm_tn<16>(s.A, LDA_S, 0, s.GH1, LDH_S, acc);
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                if (g < d) {
+                    atomicAdd(&GP[pl_W1(d) + (int64_t)g * FLOW_H + c], acc[nt][0]);
+                    atomicAdd(&GP[pl_W1(d) + (int64_t)g * FLOW_H + c + 1], acc[nt][1]);
+                }
+                if (g + 8 < d) {
+                    atomicAdd(&GP[pl_W1(d) + (int64_t)(g + 8) * FLOW_H + c], acc[nt][2]);
+                    atomicAdd(&GP[pl_W1(d) + (int64_t)(g + 8) * FLOW_H + c + 1], acc[nt][3]);
+                }
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < FLOW_H; i += blockDim.x) {
+            atomicAdd(&GP[pl_b1(d) + i], s.red[i]);
+            atomicAdd(&GP[pl_b2(d) + i], s.red[FLOW_H + i]);
+        }
+        for (int i = threadIdx.x; i < 2 * d; i += blockDim.x) { atomicAdd(&GP[pl_b3(d) + i], s.red[2 * FLOW_H + i]); }
+        __syncthreads();
+    }
+    // base affine: y_L = (x - mu) exp(-logsig)
+    float *gmu = f.grad + f.base_off, *gls = f.grad + f.base_off + D;
+    for (int c = threadIdx.x; c < D; c += blockDim.x) {
+        float a = 0.f, b = 0.f;
+        for (int r = 0; r < rows; ++r) {
+            const float e = __expf(-f.logsig[c]);
+            const float yl = (f.x[(int64_t)(base + r) * D + c] - f.mu[c]) * e;
+            a += -s.G[r][c] * e;
+            b += -s.G[r][c] * yl;
+        }
+        atomicAdd(&gmu[c], a);
+        atomicAdd(&gls[c], b + (blockIdx.x == 0 ? 1.f : 0.f));
+    }
+}
+
+__global__ void flow_adam_kernel(float *theta, const float *grad, float *m, float *v, int64_t n, float lr, float b1,
+                                 float b2, float eps, float c1, float c2)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float g = grad[i];
+        const float mi = b1 * m[i] + (1.f - b1) * g;
+        const float vi = b2 * v[i] + (1.f - b2) * g * g;
+        m[i] = mi;
+        v[i] = vi;
+        theta[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    }
+}
+
+// training minibatch gather: rows idx of src [nsrc][D] into dst [B][D]
+__global__ void flow_gather_kernel(const float *src, int64_t nsrc, int D, uint32_t seed, uint32_t step, float *dst, int B)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B) { return; }
+    const P4 q = philox4x32_10((uint32_t)i, step, 0x5EEDu, 0x7AAu, seed, 0xF10Au);
+    const int64_t r = (int64_t)(((uint64_t)q.a * (uint64_t)nsrc) >> 32);
+    for (int c = 0; c < D; ++c) { dst[(int64_t)i * D + c] = src[r * D + c]; }
+}
+
+// ------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------
+struct mcig_flow {
+    int D, d, L, device;
+    uint64_t seed;
+    int64_t np, pstride, base_off;
+    float *theta = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *wb = nullptr;
+    int *perm = nullptr;
+    int64_t adam_t = 0;
+    cudaStream_t st = nullptr;
+    // work buffers
+    float *buf_in = nullptr, *buf_out = nullptr, *buf_logq = nullptr, *buf_tape = nullptr, *buf_batch = nullptr;
+    int64_t cap = 0, tape_cap = 0, batch_cap = 0;
+};
+
+static int flow_err(int code, const std::string &m) { return mcig_set_last_error(code, m.c_str()); }
+#define FCK(call)                                                                                           \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess) { return flow_err(MCIG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); } \
+    } while (0)
+
+static std::vector<int> flow_perms(int D, int L, uint64_t seed)
+{ // splitmix64 Fisher-Yates, as oracle/flow_oracle.py permutations()
+    std::vector<int> out;
+    for (int l = 0; l < L; ++l) {
+        uint64_t s = seed * 0x9E3779B97F4A7C15ULL + (uint64_t)l + 1;
+        std::vector<int> p(D);
+        for (int i = 0; i < D; ++i) { p[i] = i; }
+        for (int i = D - 1; i > 0; --i) {
+            s += 0x9E3779B97F4A7C15ULL;
+            uint64_t z = s;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+            z = z ^ (z >> 31);
+            const int j = (int)(z % (uint64_t)(i + 1));
+            std::swap(p[i], p[j]);
+        }
+        out.insert(out.end(), p.begin(), p.end());
+    }
+    return out;
+}
+
+static int flow_ensure(mcig_flow *f, int64_t n, bool tape)
+{
+    if (n > f->cap) {
+        cudaFree(f->buf_in); cudaFree(f->buf_out); cudaFree(f->buf_logq);
+        FCK(cudaMalloc(&f->buf_in, n * f->D * sizeof(float)));
+        FCK(cudaMalloc(&f->buf_out, n * f->D * sizeof(float)));
+        FCK(cudaMalloc(&f->buf_logq, n * sizeof(float)));
+        f->cap = n;
+    }
+    if (tape && n > f->tape_cap) {
+        cudaFree(f->buf_tape);
+        FCK(cudaMalloc(&f->buf_tape, (int64_t)f->L * n * 4 * f->d * sizeof(float)));
+        f->tape_cap = n;
+    }
+    return MCIG_OK;
+}
+
+static int flow_cast(mcig_flow *f)
+{
+    flow_cast_kernel<<<256, 256, 0, f->st>>>(f->theta, f->wb, f->d, f->L);
+    FCK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+extern "C" int64_t mcig_flow_nparams(int ndim, int nlayers)
+{
+    const int d = ndim / 2;
+    return (int64_t)nlayers * pl_size(d) + 2 * (int64_t)ndim;
+}
+
+extern "C" int mcig_flow_create(int ndim, int nlayers, int hidden, uint64_t seed, int device, mcig_flow **out)
+{
+    if (!out) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "out is NULL"); }
+    *out = nullptr;
+    if (ndim < 2 || ndim > FLOW_MAXD || ndim % 2) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: ndim must be even and in [2, 32]"); }
+    if (nlayers < 1 || nlayers > FLOW_MAXL) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: nlayers must be in [1, 16]"); }
+    if (hidden != FLOW_H) { return flow_err(MCIG_ERR_UNSUPPORTED, "flow: hidden width must be 128"); }
+    FCK(cudaSetDevice(device));
+    mcig_flow *f = new mcig_flow();
+    f->D = ndim;
+    f->d = ndim / 2;
+    f->L = nlayers;
+    f->device = device;
+    f->seed = seed;
+    f->pstride = pl_size(f->d);
+    f->base_off = (int64_t)nlayers * f->pstride;
+    f->np = mcig_flow_nparams(ndim, nlayers);
+    cudaStreamCreateWithFlags(&f->st, cudaStreamNonBlocking);
+    FCK(cudaMalloc(&f->theta, f->np * sizeof(float)));
+    FCK(cudaMalloc(&f->grad, f->np * sizeof(float)));
+    FCK(cudaMalloc(&f->m, f->np * sizeof(float)));
+    FCK(cudaMalloc(&f->v, f->np * sizeof(float)));
+    FCK(cudaMalloc(&f->wb, (int64_t)nlayers * WB_LAYER * sizeof(__nv_bfloat16)));
+    FCK(cudaMalloc(&f->perm, (int64_t)nlayers * ndim * sizeof(int)));
+    std::vector<int> p = flow_perms(ndim, nlayers, seed);
+    FCK(cudaMemcpy(f->perm, p.data(), p.size() * sizeof(int), cudaMemcpyHostToDevice));
+    // He-normal hidden weights (Box-Muller on splitmix64), zero output layer: the flow starts as the identity
+    std::vector<float> th((size_t)f->np, 0.f);
+    uint64_t s = seed ^ 0xA5A5A5A5DEADBEEFULL;
+    auto nrm = [&s]() {
+        auto nxt = [&s]() {
+            s += 0x9E3779B97F4A7C15ULL;
+            uint64_t z = s;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+            return (double)((z ^ (z >> 31)) >> 11) * (1.0 / 9007199254740992.0);
+        };
+        const double u1 = 1.0 - nxt(), u2 = nxt();
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2);
+    };
+    for (int l = 0; l < nlayers; ++l) {
+        float *P = th.data() + (int64_t)l * f->pstride;
+        for (int64_t i = 0; i < (int64_t)f->d * FLOW_H; ++i) { P[pl_W1(f->d) + i] = (float)(nrm() * std::sqrt(2.0 / f->d)); }
+        for (int64_t i = 0; i < (int64_t)FLOW_H * FLOW_H; ++i) { P[pl_W2(f->d) + i] = (float)(nrm() * std::sqrt(2.0 / FLOW_H)); }
+    }
+    FCK(cudaMemcpy(f->theta, th.data(), th.size() * sizeof(float), cudaMemcpyHostToDevice));
+    FCK(cudaMemset(f->m, 0, f->np * sizeof(float)));
+    FCK(cudaMemset(f->v, 0, f->np * sizeof(float)));
+    int rc = flow_cast(f);
+    if (rc) { return rc; }
+    FCK(cudaFuncSetAttribute(flow_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowSmem)));
+    FCK(cudaFuncSetAttribute(flow_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowBwdSmem)));
+    FCK(cudaStreamSynchronize(f->st));
+    *out = f;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_destroy(mcig_flow *f)
+{
+    if (!f) { return MCIG_OK; }
+    cudaSetDevice(f->device);
+    cudaStreamSynchronize(f->st);
+    cudaFree(f->theta); cudaFree(f->grad); cudaFree(f->m); cudaFree(f->v); cudaFree(f->wb); cudaFree(f->perm);
+    cudaFree(f->buf_in); cudaFree(f->buf_out); cudaFree(f->buf_logq); cudaFree(f->buf_tape); cudaFree(f->buf_batch);
+    cudaStreamDestroy(f->st);
+    delete f;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_get_params(const mcig_flow *f, float *theta, int64_t *n)
+{
+    *n = f->np;
+    if (theta) {
+        cudaSetDevice(f->device);
+        FCK(cudaMemcpy(theta, f->theta, f->np * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n)
+{
+    if (n != f->np) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: parameter count mismatch"); }
+    cudaSetDevice(f->device);
+    FCK(cudaMemcpy(f->theta, theta, n * sizeof(float), cudaMemcpyHostToDevice));
+    f->adam_t = 0;
+    FCK(cudaMemset(f->m, 0, f->np * sizeof(float)));
+    FCK(cudaMemset(f->v, 0, f->np * sizeof(float)));
+    int rc = flow_cast(f);
+    if (rc) { return rc; }
+    FCK(cudaStreamSynchronize(f->st));
+    return MCIG_OK;
+}
+
+// one pass over device arrays (in [n][D] float -> out, logq); tape optional
+int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, float *d_out, float *d_logq, float *d_tape,
+                          cudaStream_t st)
+{
+    FlowArgs a;
+    a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = dir;
+    a.in = d_in; a.out = d_out; a.logq = d_logq;
+    a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
+    a.perm = f->perm; a.tape = d_tape; a.wb = f->wb; a.theta = f->theta;
+    a.wstride = WB_LAYER; a.pstride = f->pstride;
+    const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
+    flow_pass_kernel<<<grid, FLOW_THREADS, sizeof(FlowSmem), st>>>(a);
+    FCK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+static int flow_host_pass(mcig_flow *f, int dir, const double *in, int64_t n, double *out, double *logq)
+{
+    if (n < 1) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: n must be >= 1"); }
+    cudaSetDevice(f->device);
+    int rc = flow_ensure(f, n, false);
+    if (rc) { return rc; }
+    std::vector<float> h((size_t)n * f->D);
+    for (size_t i = 0; i < h.size(); ++i) { h[i] = (float)in[i]; }
+    FCK(cudaMemcpyAsync(f->buf_in, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, f->st));
+    rc = mcig_flow_pass_device(f, dir, f->buf_in, n, f->buf_out, f->buf_logq, nullptr, f->st);
+    if (rc) { return rc; }
+    std::vector<float> lq((size_t)n);
+    FCK(cudaMemcpyAsync(h.data(), f->buf_out, h.size() * sizeof(float), cudaMemcpyDeviceToHost, f->st));
+    FCK(cudaMemcpyAsync(lq.data(), f->buf_logq, n * sizeof(float), cudaMemcpyDeviceToHost, f->st));
+    FCK(cudaStreamSynchronize(f->st));
+    if (out) { for (size_t i = 0; i < h.size(); ++i) { out[i] = h[i]; } }
+    if (logq) { for (int64_t i = 0; i < n; ++i) { logq[i] = lq[i]; } }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_forward(mcig_flow *f, const double *z, int64_t n, double *x, double *logq)
+{
+    return flow_host_pass(f, 0, z, n, x, logq);
+}
+
+extern "C" int mcig_flow_inverse(mcig_flow *f, const double *x, int64_t n, double *z, double *logq)
+{
+    return flow_host_pass(f, 1, x, n, z, logq);
+}
+
+// loss -mean log q(x) and its gradient on device data d_x [n][D]; gradient left in f->grad
+static int flow_loss_grad_device(mcig_flow *f, const float *d_x, int64_t n, float *loss_host)
+{
+    int rc = flow_ensure(f, n, true);
+    if (rc) { return rc; }
+    rc = mcig_flow_pass_device(f, 1, d_x, n, f->buf_out, f->buf_logq, f->buf_tape, f->st);
+    if (rc) { return rc; }
+    FCK(cudaMemsetAsync(f->grad, 0, f->np * sizeof(float), f->st));
+    FlowBwdArgs b;
+    b.D = f->D; b.d = f->d; b.L = f->L; b.n = (int)n;
+    b.inv_batch = 1.f / (float)n;
+    b.z = f->buf_out; b.tape = f->buf_tape; b.perm = f->perm; b.wb = f->wb; b.theta = f->theta;
+    b.grad = f->grad; b.x = d_x; b.mu = f->theta + f->base_off; b.logsig = f->theta + f->base_off + f->D;
+    b.wstride = WB_LAYER; b.pstride = f->pstride; b.base_off = f->base_off;
+    const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
+    flow_backward_kernel<<<grid, FLOW_THREADS, sizeof(FlowBwdSmem), f->st>>>(b);
+    FCK(cudaGetLastError());
+    if (loss_host) {
+        std::vector<float> lq((size_t)n);
+        FCK(cudaMemcpyAsync(lq.data(), f->buf_logq, n * sizeof(float), cudaMemcpyDeviceToHost, f->st));
+        FCK(cudaStreamSynchronize(f->st));
+        double s = 0.;
+        for (float v : lq) { s += v; }
+        *loss_host = (float)(-s / (double)n);
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_loss_grad(mcig_flow *f, const double *x, int64_t n, double *loss, float *grad)
+{
+    if (n < 1) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: n must be >= 1"); }
+    cudaSetDevice(f->device);
+    int rc = flow_ensure(f, n, true);
+    if (rc) { return rc; }
+    float *d_x = nullptr;
+    FCK(cudaMalloc(&d_x, n * f->D * sizeof(float)));
+    std::vector<float> h((size_t)n * f->D);
+    for (size_t i = 0; i < h.size(); ++i) { h[i] = (float)x[i]; }
+    cudaMemcpyAsync(d_x, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, f->st);
+    float l = 0.f;
+    rc = flow_loss_grad_device(f, d_x, n, &l);
+    if (!rc && grad) {
+        cudaMemcpyAsync(grad, f->grad, f->np * sizeof(float), cudaMemcpyDeviceToHost, f->st);
+        cudaStreamSynchronize(f->st);
+    }
+    cudaFree(d_x);
+    if (loss) { *loss = l; }
+    return rc;
+}
+
+// Adam steps on minibatches drawn from device data d_x [nsrc][D]
+int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int steps, int batch, double lr, float *last_loss)
+{
+    if (batch < 1 || steps < 0) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: bad training arguments"); }
+    if (batch > f->batch_cap) {
+        cudaFree(f->buf_batch);
+        FCK(cudaMalloc(&f->buf_batch, (int64_t)batch * f->D * sizeof(float)));
+        f->batch_cap = batch;
+    }
+    int rc = flow_ensure(f, batch, true);
+    if (rc) { return rc; }
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int it = 0; it < steps; ++it) {
+        flow_gather_kernel<<<(batch + 127) / 128, 128, 0, f->st>>>(d_x, nsrc, f->D, (uint32_t)f->seed, (uint32_t)f->adam_t,
+                                                                   f->buf_batch, batch);
+        rc = flow_loss_grad_device(f, f->buf_batch, batch, (it == steps - 1) ? last_loss : nullptr);
+        if (rc) { return rc; }
+        ++f->adam_t;
+        const float c1 = 1.f / (1.f - powf(b1, (float)f->adam_t)), c2 = 1.f / (1.f - powf(b2, (float)f->adam_t));
+        flow_adam_kernel<<<256, 256, 0, f->st>>>(f->theta, f->grad, f->m, f->v, f->np, (float)lr, b1, b2, eps, c1, c2);
+        FCK(cudaGetLastError());
+        rc = flow_cast(f);
+        if (rc) { return rc; }
+    }
+    FCK(cudaStreamSynchronize(f->st));
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_train(mcig_flow *f, const double *x, int64_t n, int steps, int batch, double lr, double *last_loss)
+{
+    cudaSetDevice(f->device);
+    float *d_x = nullptr;
+    FCK(cudaMalloc(&d_x, n * f->D * sizeof(float)));
+    std::vector<float> h((size_t)n * f->D);
+    for (size_t i = 0; i < h.size(); ++i) { h[i] = (float)x[i]; }
+    cudaMemcpy(d_x, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice);
+    float l = 0.f;
+    const int rc = mcig_flow_train_device(f, d_x, n, steps, batch, lr, &l);
+    cudaFree(d_x);
+    if (last_loss) { *last_loss = l; }
+    return rc;
+}
+
+// accessors for the sampler (mcig_capi.cu)
+int mcig_flow_dim(const mcig_flow *f) { return f->D; }
+cudaStream_t mcig_flow_stream(const mcig_flow *f) { return f->st; }

@@ -212,6 +212,7 @@ __device__ void obs_eval(const KParams &p, const ObsDesc &o, const R *x, R *out)
         break;
     }
     case MCIG_OBS_CONST: out[0] = (R)p.params[o.poff]; break; // Constval (:385-388)
+    case MCIG_OBS_XI: out[0] = x[(int)p.params[o.poff]]; break;
     case MCIG_OBS_POLYNOM: { // Polynom (:403-409)
         R s = (R)0;
         for (int i = 0; i < nd; ++i) { s = s + x[i]; }
@@ -555,11 +556,12 @@ struct GenericSampler {
                 const int64_t k = r / od.nskip; // accumulation index
                 obs_eval<R>(p, od, x, vals);
                 if (od.acc == MCIG_ACC_FULL) { // FullAccumulator::_accumulate (FullAccumulator.cpp:14-18)
+                    const size_t row = (size_t)(p.acc_offset + k);
                     if (od.full32) {
-                        float *dst = (float *)od.data + (size_t)k * od.nv * p.nchains + c;
+                        float *dst = (float *)od.data + row * od.nv * p.nchains + c;
                         for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (float)vals[j]; }
                     } else {
-                        double *dst = (double *)od.data + (size_t)k * od.nv * p.nchains + c;
+                        double *dst = (double *)od.data + row * od.nv * p.nchains + c;
                         for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (double)vals[j]; }
                     }
                 } else {
@@ -588,9 +590,8 @@ struct GenericSampler {
     }
 
     // MCI::findMRT2Step (MCIntegrator.cpp:87-168) for this chain alone
-    __device__ void run_calibration(int movetype)
+    __device__ void run_calibration(int movetype, int64_t MIN_STAT)
     {
-        const int64_t MIN_STAT = p.nsteps;
         const int MIN_CONS = 5;
         const double TOLERANCE = 0.05;
         const double SMALLEST = 1.1754943508222875e-38; // numeric_limits<float>::min()
@@ -635,7 +636,7 @@ __global__ void __launch_bounds__(128) mcig_generic_kernel(const KParams p, int 
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
     GenericSampler<R, RNG, KAHAN> s(p, c, smem_blob);
-    if (p.mode == KMODE_CALIB) { s.run_calibration(movetype); }
+    if (p.mode == KMODE_CALIB) { s.run_calibration(movetype, p.nsteps); }
     else if (p.mode == KMODE_SAMPLE) { s.run_sample(movetype, p.nsteps); }
     else { s.run_steps(movetype, p.nsteps); }
     s.store_state();

@@ -4,7 +4,8 @@
 #include <cuda_runtime.h>
 #include "mcig_common.cuh"
 
-typedef void (*mcig_launch_fn)(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st);
+typedef void (*mcig_launch_fn)(const KParams &p, const FastConst *fc, int movetype, int grid, int block, size_t smem,
+                               cudaStream_t st);
 
 // general kernel: precision MCIG_PREC_*, rng RNG_PHILOX / RNG_TAPE (tape: FP64 only)
 mcig_launch_fn mcig_generic_launcher(int precision, int rng);

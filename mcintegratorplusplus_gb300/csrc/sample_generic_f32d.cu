@@ -3,7 +3,8 @@
 #include "mcig_generic.cuh"
 #include "mcig_launchers.h"
 
-static void launch_f32_acc64(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st)
+static void launch_f32_acc64(const KParams &p, const FastConst *, int movetype, int grid, int block, size_t smem,
+                           cudaStream_t st)
 {
     auto k = mcig_generic_kernel<float, RNG_PHILOX, false>;
     if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }

@@ -4,7 +4,8 @@
 #include "mcig_launchers.h"
 
 template <class R, int RNG, bool KAHAN>
-static void launch_generic(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st)
+static void launch_generic(const KParams &p, const FastConst *, int movetype, int grid, int block, size_t smem,
+                           cudaStream_t st)
 {
     auto k = mcig_generic_kernel<R, RNG, KAHAN>;
     if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }

@@ -30,7 +30,7 @@ SRRD_UNIFORM, SRRD_GAUSSIAN, SRRD_STUDENT, SRRD_CAUCHY, SRRD_EXPONENTIAL, SRRD_G
     SRRD_LOGNORMAL, SRRD_CHISQ, SRRD_FISHER = range(10)
 EST_NOOP, EST_UNCORRELATED, EST_CORRELATED, EST_FCBLOCKER, EST_MJBLOCKER = range(5)
 PDF_GAUSS_SUM, PDF_GAUSS, PDF_EXP, PDF_GAUSS_PREC, PDF_GAUSS_BLOCK, PDF_GAUSS_MIX = range(6)
-OBS_X2SUM, OBS_XND, OBS_X2, OBS_X2MEAN, OBS_CONST, OBS_POLYNOM, OBS_X2BLOCK, OBS_GAUSSX2 = range(8)
+OBS_X2SUM, OBS_XND, OBS_X2, OBS_X2MEAN, OBS_CONST, OBS_POLYNOM, OBS_X2BLOCK, OBS_GAUSSX2, OBS_XI = range(9)
 PREC_FP64, PREC_FP32, PREC_FP32_ACC64 = range(3)
 
 
@@ -315,6 +315,136 @@ class MCI:
 
     def add_observable(self, kind, params=(), blocksize=1, nskip=1, flag_equil=None, estimator=None):
         self.addObservable(kind, params, blocksize, nskip, flag_equil, estimator)
+
+
+class Flow:
+    """Affine-coupling flow on the GPU (include/mcig.h, mcig_flow_*): the learned proposal."""
+
+    def __init__(self, ndim, nlayers=8, hidden=128, seed=0, device=0):
+        self.L = _lib.load()
+        self.ndim = int(ndim)
+        self.nlayers = int(nlayers)
+        h = ctypes.c_void_p()
+        _raise(self.L.mcig_flow_create(self.ndim, self.nlayers, int(hidden), ctypes.c_uint64(seed), int(device),
+                                       ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.L.mcig_flow_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        n = ctypes.c_int64()
+        _raise(self.L.mcig_flow_get_params(self._h, None, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.float32)
+        _raise(self.L.mcig_flow_get_params(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(n)))
+        return out
+
+    def set_params(self, theta):
+        t = np.ascontiguousarray(np.asarray(theta, dtype=np.float32))
+        _raise(self.L.mcig_flow_set_params(self._h, t.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), t.size))
+
+    def _pass(self, fn, a):
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+        out = np.zeros_like(a)
+        lq = np.zeros(a.shape[0])
+        _raise(fn(self._h, _dp(a), a.shape[0], _dp(out), _dp(lq)))
+        return out, lq
+
+    def forward(self, z):
+        return self._pass(self.L.mcig_flow_forward, z)
+
+    def inverse(self, x):
+        return self._pass(self.L.mcig_flow_inverse, x)
+
+    def loss_grad(self, x):
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+        g = np.zeros(self.L.mcig_flow_nparams(self.ndim, self.nlayers), dtype=np.float32)
+        loss = ctypes.c_double()
+        _raise(self.L.mcig_flow_loss_grad(self._h, _dp(x), x.shape[0], ctypes.byref(loss),
+                                          g.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return loss.value, g
+
+    def train(self, x, steps, batch, lr):
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+        loss = ctypes.c_double()
+        _raise(self.L.mcig_flow_train(self._h, _dp(x), x.shape[0], int(steps), int(batch), float(lr), ctypes.byref(loss)))
+        return loss.value
+
+
+def integrate_flow(m, flow, nmc, period=5, refresh=4096, train_steps=200, batch=2048, lr=1e-3, doFindMRT2step=True,
+                   doDecorrelation=True):
+    """MCI::integrate with the learned proposal (mcig_integrate_flow); returns avg, err, flow acceptance."""
+    nod = max(m.getNObsDim(), 1)
+    avg = np.zeros(nod)
+    err = np.zeros(nod)
+    acc = ctypes.c_double()
+    _raise(m.L.mcig_integrate_flow(m._h, flow._h, int(nmc), int(period), int(refresh), int(train_steps), int(batch),
+                                   float(lr), _dp(avg), _dp(err), int(bool(doFindMRT2step)), int(bool(doDecorrelation)),
+                                   ctypes.byref(acc)))
+    return avg[:m.getNObsDim()], err[:m.getNObsDim()], acc.value
+
+
+class Batch:
+    """Many independent integrals (one MCI each) in one persistent launch per ndim bucket (mcig_batch_*)."""
+
+    def __init__(self, mcis, nmc, doFindMRT2step=True, doDecorrelation=True):
+        self.L = _lib.load()
+        self.mcis = list(mcis)
+        arr = (ctypes.c_void_p * len(self.mcis))(*[m._h.value for m in self.mcis])
+        nm = np.ascontiguousarray(np.broadcast_to(np.asarray(nmc, dtype=np.int64), (len(self.mcis),)))
+        h = ctypes.c_void_p()
+        _raise(self.L.mcig_batch_create(arr, len(self.mcis), nm.ctypes.data_as(P_int64), int(bool(doFindMRT2step)),
+                                        int(bool(doDecorrelation)), ctypes.byref(h)))
+        self._h = h
+        self.nod = [m.getNObsDim() for m in self.mcis]
+
+    def run(self):
+        tot = sum(self.nod)
+        avg = np.zeros(max(tot, 1))
+        err = np.zeros(max(tot, 1))
+        _raise(self.L.mcig_batch_run(self._h, _dp(avg), _dp(err)))
+        out, off = [], 0
+        for n in self.nod:
+            out.append((avg[off:off + n].copy(), err[off:off + n].copy()))
+            off += n
+        return out
+
+    def last_ms(self):
+        v = ctypes.c_double()
+        _raise(self.L.mcig_batch_last_ms(self._h, ctypes.byref(v)))
+        return v.value
+
+    def blocks(self):
+        b = (ctypes.c_int * 4)()
+        _raise(self.L.mcig_batch_get_blocks(self._h, b))
+        return list(b)
+
+    def set_blocks(self, blocks):
+        b = (ctypes.c_int * 4)(*[int(v) for v in blocks])
+        _raise(self.L.mcig_batch_set_blocks(self._h, b))
+
+    def autotune(self, cache_path=None):
+        _raise(self.L.mcig_batch_autotune(self._h, cache_path.encode() if cache_path else None))
+        return self.blocks()
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.L.mcig_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def estimate(estimator, x, device=0):

@@ -470,6 +470,10 @@ static int obs_init(obsdef *o, int kind, int ndim, const double *params, int npa
         break;
     case MCIG_OBS_XND:
     case MCIG_OBS_X2: o->nobs = ndim; break;
+    case MCIG_OBS_XI:
+        if (nparams < 1 || (int)params[0] < 0 || (int)params[0] >= ndim) { return fail(MCIG_ERR_INVALID_ARGUMENT, "XI needs an index in [0, ndim)"); }
+        o->nobs = 1;
+        break;
     case MCIG_OBS_X2BLOCK: {
         if (nparams < 2) { return fail(MCIG_ERR_INVALID_ARGUMENT, "X2BLOCK needs [nb, b0..b_nb]"); }
         const int nb = (int)params[0];
@@ -517,6 +521,7 @@ static void obs_eval(const obsdef *o, const double *x, double *out)
         break;
     }
     case MCIG_OBS_CONST: out[0] = o->params[0]; break; /* Constval (:385-388) */
+    case MCIG_OBS_XI: out[0] = x[(int)o->params[0]]; break;
     case MCIG_OBS_POLYNOM: { /* Polynom (:403-409) */
         double s = 0.;
         for (int i = 0; i < nd; ++i) { s = s + x[i]; }

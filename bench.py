@@ -54,13 +54,13 @@ def target(seed=2024):
     return Sigma, 0.5 * (P + P.T)
 
 
-def configure(m, P, nmc):
+def configure(m, P, nmc, nblocks=NBLOCKS):
     """Same configuration for the device MCI and the oracle (MCI-style API)."""
     m.add_sampling_function(3, P)            # GAUSS_PREC
     m.set_trial_move(0, 1, 0)                # all-coordinate, Gaussian
     m.set_nfind_mrt2_iterations(-50)
     m.set_ndecorrelation_steps(BURNIN)
-    bs = nmc // NBLOCKS
+    bs = nmc // nblocks
     m.add_observable(0, (), bs, 1, False, 1)  # x.x, Block, Uncorrelated
     m.add_observable(1, (), bs, 1, False, 1)  # x_i, Block, Uncorrelated
     m.add_observable(0, (), 1, 1, False, 1)   # x.x, Full
@@ -131,7 +131,7 @@ def run_gpu(args):
     m = mcig.MCI(NDIM, nchains, device=0, precision=mcig.PREC_FP32)
     m.setSeed(20241203)
     m.setFullStorage(32)
-    configure(m, P, args.nmc)
+    configure(m, P, args.nmc, args.blocks)
     nod = m.getNObsDim()
     # pinned host buffers: initial walkers in, averages / errors out
     x0 = torch.zeros((nchains, NDIM), dtype=torch.float64).pin_memory()
@@ -177,7 +177,7 @@ def run_gpu(args):
     # dominant kernel: the sampling launch (float Full stores + block sums)
     samp_ms = float(np.mean(kernel_ms))
     full_bytes = nchains * args.nmc * (1 + NDIM) * 4       # Full float stores
-    block_bytes = nchains * NBLOCKS * (1 + NDIM) * 8       # Block means (double)
+    block_bytes = nchains * args.blocks * (1 + NDIM) * 8   # Block means (double)
     state_bytes = nchains * (NDIM * 8 * 2 + 8 * 4)         # walker in/out, step, counter
     algo_bytes = full_bytes + block_bytes + state_bytes
     pk, pk_kind = peaks()
@@ -189,7 +189,7 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded correlated Gaussian target, random-init walkers at 0)",
         "config": {"workload": "C2 batched plain Metropolis", "chains": nchains, "ndim": NDIM,
-                   "nmc": args.nmc, "burnin": BURNIN, "blocks": NBLOCKS, "full_storage": "f32",
+                   "nmc": args.nmc, "burnin": BURNIN, "blocks": args.blocks, "full_storage": "f32",
                    "accumulation": "f32+Kahan", "calibration": "auto per chain (target 0.5)",
                    "l2": "flushed (256 MB write) before each step; Full output > L2"},
         "walker_steps_per_s": steps_total / (ms_dev * 1e-3),
@@ -212,32 +212,43 @@ def run_gpu(args):
     return line
 
 
-def cpu_baseline(args):
-    """The oracle (reference restated: std::mt19937_64, double, one MCI per chain) on host threads."""
+def cpu_baseline(args, target_s=10.0):
+    """The oracle (reference restated: std::mt19937_64, double, one MCI per chain) on host threads.
+
+    A pilot of 2 chains per thread sets the chain count so that the sample takes about
+    `target_s` seconds of wall time on all host threads."""
     from oracle import oracle as orc
     Sigma, P = target()
     var_xx = 2.0 * float(np.trace(Sigma @ Sigma))
     nthreads = os.cpu_count() or 1
-    nch = max(nthreads, args.cpu_chains)
-    m = orc.OracleMCI(NDIM, nch)
-    m.set_seeds(np.arange(1, nch + 1, dtype=np.uint64) * 7919)
-    configure(m, P, args.nmc)
-    t0 = time.perf_counter()
-    avg, err = m.integrate(args.nmc, True, True, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    # the full workload has NCHAINS chains: error scales as 1/sqrt(chains), time as chains/threads
+
+    def sample(nch):
+        m = orc.OracleMCI(NDIM, nch)
+        m.set_seeds(np.arange(1, nch + 1, dtype=np.uint64) * 7919)
+        configure(m, P, args.nmc, args.blocks)
+        t0 = time.perf_counter()
+        avg, err = m.integrate(args.nmc, True, True, nthreads=nthreads)
+        return avg, err, time.perf_counter() - t0
+
+    nch = max(2 * nthreads, args.cpu_chains)
+    avg, err, dt = sample(nch)
+    if dt < 0.5 * target_s:
+        nch = int(min(NCHAINS, max(nch, nch * target_s / max(dt, 1e-3)) // nthreads * nthreads))
+        avg, err, dt = sample(nch)
+    # ESS is proportional to the number of chains, so ESS/s of the sample is that of the full workload
     ess_sample = var_xx / float(err[0]) ** 2
     return {"value": ess_sample / dt, "unit": "effective samples/s", "cores": nthreads, "kind": "port",
             "sample": "%d of the %d chains, full length (calibration, %d burn-in, %d steps), %.1f s" %
                       (nch, NCHAINS, BURNIN, args.nmc, dt),
-            "walker_steps_per_s": nch * args.nmc / dt, "x.x": float(avg[0]), "err": float(err[0])}
+            "walker_steps_per_s": nch * args.nmc / dt, "x.x": float(avg[0]), "err": float(err[0]),
+            "chains": nch}
 
 
 def run_reference(args):
     cb = None
     vals = []
     for _ in range(args.warmup):
-        cpu_baseline(args)
+        args.cpu_chains = cpu_baseline(args)["chains"]  # the first call sizes the sample
     t0 = time.perf_counter()
     for _ in range(args.steps):
         cb = cpu_baseline(args)
@@ -253,6 +264,198 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "effective samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------------------
+# further workloads (--workload c3|c4|c5); the default line is the C2 workload
+# ---------------------------------------------------------------------------
+
+def _timed_device_ms(tm):
+    return tm["calibration_ms"] + tm["burnin_ms"] + tm["sampling_ms"] + tm["estimation_ms"]
+
+
+def run_c3(args):
+    """4,096 uneven integrals in one batch (persistent launch per ndim bucket, CUDA graph).
+
+    Integral i: ndim ~ U{1..64}, NMC_i = 2^U(14,20) samples split over 16 chains, target a
+    product of 2-4 isotropic Gaussians on contiguous coordinate blocks (widths log-uniform on
+    [0.3, 3]), MultiStepMove of 4 single-coordinate sub-moves on the same factors, x.x per
+    block in a BlockAccumulator (16 blocks per chain).  Metric: integrals/s."""
+    import mcintegratorplusplus_gb300 as mcig
+    n, nch = args.integrals, 16
+    rng = np.random.default_rng(33)
+    mcis, exact, nmcs = [], [], []
+    for i in range(n):
+        ndim = int(rng.integers(1, 65))
+        nmc = int(2 ** rng.uniform(14, 20)) // nch // 16 * 16
+        nb = int(min(ndim, rng.integers(2, 5)))
+        cuts = np.sort(rng.choice(np.arange(1, ndim), nb - 1, replace=False)) if nb > 1 else np.array([], int)
+        bounds = [0] + [int(c) for c in cuts] + [ndim]
+        widths = 10.0 ** rng.uniform(np.log10(0.3), np.log10(3.0), nb)
+        m = mcig.MCI(ndim, nch, precision=mcig.PREC_FP32)
+        m.setSeed(1000 + i)
+        for k in range(nb):
+            m.addSamplingFunction(mcig.PDF_GAUSS_BLOCK, [bounds[k], bounds[k + 1], widths[k]])
+        # sub-chain on the full target: every outer step is accepted, so the sub-move
+        # step comes from the widths rather than from calibration
+        m.setMultiStepMove(4, mcig.SRRD_UNIFORM, 1, float(2.0 * np.exp(np.mean(np.log(widths)))))
+        for k in range(nb):
+            m.addMultiStepSamplingFunction(mcig.PDF_GAUSS_BLOCK, [bounds[k], bounds[k + 1], widths[k]])
+        m.setNfindMRT2Iterations(0)
+        m.setNdecorrelationSteps(500)
+        m.addObservable(mcig.OBS_X2BLOCK, [nb] + bounds, nmc // 16, 1, False, mcig.EST_UNCORRELATED)
+        mcis.append(m)
+        exact.append(np.array([(bounds[k + 1] - bounds[k]) * widths[k] ** 2 for k in range(nb)]))
+        nmcs.append(nmc)
+    b = mcig.Batch(mcis, nmcs)
+    blocks = b.autotune(None)
+    for _ in range(args.warmup):
+        b.run()
+    clocks = Clocks()
+    clocks.start()
+    ms, wall = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        res = b.run()
+        wall.append(time.perf_counter() - t0)
+        ms.append(b.last_ms())
+    ck = clocks.stop()
+    z = np.concatenate([np.abs(a - x) / np.maximum(e, 1e-300) for (a, e), x in zip(res, exact)])
+    outer = float(np.sum(nmcs)) * nch
+    t = float(np.mean(ms)) * 1e-3
+    return {"metric": "integrals/s (C3: 4,096 uneven integrals, ndim 1-64, MultiStepMove)", "value": n / t,
+            "unit": "integrals/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "C3 uneven batch", "integrals": n, "chains_per_integral": nch,
+                       "outer_steps": outer, "sub_moves": 4, "block_sizes": blocks,
+                       "l2": "working set (walkers, block sums) below L2; no flush"},
+            "outer_steps_per_s": outer / t,
+            "e2e": {"value": n / float(np.mean(wall)), "unit": "integrals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(2 * 8 * sum(len(x) for x in exact))},
+            "accuracy": {"frac_within_3_sigma": float(np.mean(z < 3.0)), "max_z": float(z.max())},
+            "clocks": ck}
+
+
+C4_NDIM, C4_NCOMP = 32, 8
+
+
+def c4_target(seed=404):
+    rng = np.random.default_rng(seed)
+    means = rng.standard_normal((C4_NCOMP, C4_NDIM)) * 3.0
+    widths = 10.0 ** rng.uniform(np.log10(0.3), np.log10(3.0), (C4_NCOMP, C4_NDIM))
+    w = rng.dirichlet(np.ones(C4_NCOMP))
+    params = np.concatenate([[C4_NCOMP], w, means.ravel(), widths.ravel()])
+    m1 = (w[:, None] * means).sum(0)
+    m2 = (w[:, None] * (widths ** 2 + means ** 2)).sum(0)
+    return params, w, means, widths, m1, m2
+
+
+def run_c4(args):
+    """Precision study: 32-D mixture of 8 anisotropic Gaussians, 16,384 chains x 65,536 steps,
+    observables x.x, x_i, x_i^2 in 64-block BlockAccumulators; float walker with Kahan float
+    block sums against the same walker with double block sums (identical trajectories).
+    Metric: walker steps/s of the Kahan-float run."""
+    import mcintegratorplusplus_gb300 as mcig
+    params, w, means, widths, m1, m2 = c4_target()
+    nch, nmc = args.chains4, args.nmc4
+    rng = np.random.default_rng(1)
+    comp = rng.choice(C4_NCOMP, nch, p=w)
+    x0 = means[comp] + widths[comp] * rng.standard_normal((nch, C4_NDIM))
+    out = {}
+    for name, prec in (("f32_kahan", mcig.PREC_FP32), ("f64_sums", mcig.PREC_FP32_ACC64)):
+        m = mcig.MCI(C4_NDIM, nch, precision=prec)
+        m.setSeed(31)
+        m.addSamplingFunction(mcig.PDF_GAUSS_MIX, params)
+        m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+        m.setNdecorrelationSteps(256)
+        bs = nmc // 64
+        for kind in (mcig.OBS_X2SUM, mcig.OBS_XND, mcig.OBS_X2):
+            m.addObservable(kind, (), bs, 1, False, mcig.EST_UNCORRELATED)
+        ms = []
+        for it in range(args.warmup + args.steps):
+            m.setX(x0)
+            avg, err = m.integrate(nmc)
+            if it >= args.warmup:
+                ms.append(_timed_device_ms(m.getLastTimings()))
+        data = np.concatenate([m.getObsData(o) for o in range(3)], axis=1)
+        ca, _ = m.getChainResults()
+        out[name] = (float(np.mean(ms)), avg, err, data, ca, m.getLastTimings())
+    t_k = out["f32_kahan"][0] * 1e-3
+    dk, dd = out["f32_kahan"][3], out["f64_sums"][3]
+    rel = np.abs(dk - dd) / np.maximum(np.abs(dd), 1e-3)
+    exact = np.concatenate([[m2.sum()], m1, m2])
+    zs = {}
+    for name in out:
+        _, avg, err, _, ca, _ = out[name]
+        sem = ca.std(0) / np.sqrt(nch)
+        zs[name] = float(np.max(np.abs(avg - exact) / sem))
+    return {"metric": "walker steps/s (C4: 16,384 chains x 32-D mixture of 8, float walker, Kahan float sums)",
+            "value": nch * nmc / t_k, "unit": "walker steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_k * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mixture, chains start in exact samples)",
+            "config": {"workload": "C4 precision study", "chains": nch, "ndim": C4_NDIM, "components": C4_NCOMP,
+                       "nmc": nmc, "blocks": 64, "observables": "x.x, x_i, x_i^2",
+                       "l2": "block output below L2; no flush"},
+            "f64_sums_steps_per_s": nch * nmc / (out["f64_sums"][0] * 1e-3),
+            "phases_ms": {k: {p: float(v) for p, v in out[k][5].items() if p.endswith("_ms")} for k in out},
+            "kahan_vs_double_block_means_max_rel": float(rel.max()),
+            "max_z_vs_analytic": zs}
+
+
+def c5_target(seed=2024, ndim=24):
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((ndim, 2)))
+    means = np.stack([3 * Q[:, 0], -3 * Q[:, 0], 3 * Q[:, 1], -3 * Q[:, 1]])
+    params = np.concatenate([[4.0], np.full(4, 0.25), means.ravel(), np.ones(4 * ndim)])
+    var_x1 = 1.0 + (means[:, 0] ** 2).mean()
+    return params, means, var_x1
+
+
+def run_c5(args):
+    """Learned proposal: 24-D mixture of 4 unit Gaussians at +-3 u1, +-3 u2, 16,384 chains,
+    affine-coupling flow (8 layers, hidden 128, bf16 tensor cores) proposing every 5th step,
+    against plain Gaussian Metropolis on the same chains.  ESS of <x_1> from the spread of the
+    chain means (ESS = Var(x_1) * chains / var(chain means)).  Metric: ESS/s with the flow."""
+    import mcintegratorplusplus_gb300 as mcig
+    D, nch, nmc = 24, args.chains5, args.nmc5
+    params, means, var_x1 = c5_target()
+    res = {}
+    for use_flow in (False, True):
+        ms, ess, accs = [], [], []
+        for it in range(args.warmup + args.steps):
+            m = mcig.MCI(D, nch, precision=mcig.PREC_FP32)
+            m.setSeed(77 + it)
+            m.setX(np.random.default_rng(5 + it).standard_normal((nch, D)) * 3.0)
+            m.addSamplingFunction(mcig.PDF_GAUSS_MIX, params)
+            m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+            m.setNdecorrelationSteps(1000)
+            m.setFullStorage(32)
+            m.addObservable(mcig.OBS_XI, [0], 1, 1, False, mcig.EST_UNCORRELATED)
+            if use_flow:
+                f = mcig.Flow(D, 8, 128, seed=6 + it)
+                _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=400,
+                                                batch=4096, lr=2e-3)
+                accs.append(acc)
+            else:
+                m.integrate(nmc)
+            if it >= args.warmup:
+                ms.append(_timed_device_ms(m.getLastTimings()))
+                ca, _ = m.getChainResults()
+                ess.append(var_x1 * nch / float(np.var(ca[:, 0])))
+        t = float(np.mean(ms)) * 1e-3
+        res[use_flow] = (float(np.mean(ess)) / t, t, float(np.mean(ess)), float(np.mean(accs)) if accs else None)
+    ratio = res[True][0] / res[False][0]
+    return {"metric": "effective samples/s of <x_1> (C5: 24-D 4-mode mixture, learned flow proposal)",
+            "value": res[True][0], "unit": "effective samples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res[True][1] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 walker, bf16 flow GEMMs (f32 accumulate)",
+            "data": "synthetic (seeded mixture, random-init flow)",
+            "config": {"workload": "C5 learned proposal", "chains": nch, "ndim": D, "nmc": nmc, "flow_layers": 8,
+                       "hidden": 128, "period": 5, "adaptation_cycles": 400, "refresh": 4096},
+            "plain_mh": {"value": res[False][0], "ms_per_step": res[False][1] * 1e3, "ess": res[False][2]},
+            "flow": {"ess": res[True][2], "acceptance": res[True][3]},
+            "ess_per_s_ratio_flow_over_plain": ratio}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -261,11 +464,22 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--chains", type=int, default=NCHAINS)
     ap.add_argument("--nmc", type=int, default=NMC)
+    ap.add_argument("--blocks", type=int, default=NBLOCKS)
     ap.add_argument("--cpu-chains", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"])
+    ap.add_argument("--integrals", type=int, default=4096)
+    ap.add_argument("--chains4", type=int, default=16384)
+    ap.add_argument("--nmc4", type=int, default=65536)
+    ap.add_argument("--chains5", type=int, default=16384)
+    ap.add_argument("--nmc5", type=int, default=8192)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.workload != "c2" and args.impl != "reference":
+        if rank == 0:
+            print(json.dumps({"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)), flush=True)
+        return
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)), flush=True)

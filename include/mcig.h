@@ -185,12 +185,16 @@ int mcig_flow_inverse(mcig_flow *f, const double *x, int64_t n, double *z, doubl
 int mcig_flow_loss_grad(mcig_flow *f, const double *x, int64_t n, double *loss, float *grad);
 /* `steps` Adam steps on minibatches of `batch` rows drawn from x[n][ndim] */
 int mcig_flow_train(mcig_flow *f, const double *x, int64_t n, int steps, int batch, double lr, double *last_loss);
-/* MCI::integrate with the learned proposal: calibration and burn-in with the
- * local move, flow training on the chain states, then every `period` steps
- * one flow proposal (period - 1 local steps in between; period 5 = 1:4),
- * retraining every `refresh` steps.  Every observable must use a
- * FullAccumulator (blocksize 1) with nskip 1.  flow_acceptance receives the
- * acceptance rate of the flow proposals. */
+/* MCI::integrate with the learned proposal.  Calibration and burn-in with the
+ * local move; then `train_steps` adaptation cycles, each of period - 1 local
+ * steps, a snapshot of the chain positions and one Adam step (learning rate
+ * lr) on `batch` rows drawn from that snapshot, with flow proposals from the
+ * first quarter of the cycles on; then nmc recorded steps, every `period`-th
+ * one a flow proposal (period 5 = 1:4 with the local move).  refresh > 0
+ * adds one Adam step every `refresh` steps while sampling; 0 freezes the
+ * flow.  Every observable must use a FullAccumulator (blocksize 1) with
+ * nskip 1.  flow_acceptance receives the acceptance rate of the recorded
+ * flow proposals. */
 int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int period, int64_t refresh, int train_steps, int batch,
                         double lr, double *average, double *error, int do_find_mrt2step, int do_decorrelation,
                         double *flow_acceptance);

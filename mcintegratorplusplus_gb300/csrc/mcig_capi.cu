@@ -820,6 +820,7 @@ static int fill_common(mcig_mci *h, KParams &kp)
         ObsDesc &od = kp.obs[o];
         magic_div((uint32_t)std::max(od.bs, 1), od.bs_magic, od.bs_shift);
         magic_div((uint32_t)od.nskip, od.sk_magic, od.sk_shift);
+        od.inv_bs = 1. / (double)std::max(od.bs, 1);
     }
     fill_fast_const(h, h->fc);
     if (h->replay) {
@@ -854,10 +855,10 @@ static bool fast_eligible(const mcig_mci *h)
 
 static int launch(mcig_mci *h, const KParams &kp)
 {
-    // 64 threads per block: with ~140 registers per thread seven blocks fit an
-    // SM, so 65,536 chains are resident in one wave, and small batches still
-    // spread over every SM
-    const int block = 64;
+    // 64 threads per block (MCIG_FAST_BLOCK): with ~140 registers per thread
+    // seven blocks fit an SM, so 65,536 chains are resident in one wave, and
+    // small batches still spread over every SM
+    const int block = MCIG_FAST_BLOCK;
     const int grid = (int)((h->nchains + block - 1) / block);
     const bool small_n = kp.nsteps < ((int64_t)1 << 31); // 32-bit step counters in the register-resident kernel
     const bool fast = h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n);
@@ -1411,7 +1412,8 @@ extern "C" int mcig_philox_block(int device, const uint32_t ctr[4], const uint32
 struct mcig_flow;
 int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, float *d_out, float *d_logq, float *d_tape,
                           cudaStream_t st);
-int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int steps, int batch, double lr, float *last_loss);
+int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int steps, int batch, double lr, float *last_loss,
+                           cudaStream_t st);
 int mcig_flow_dim(const mcig_flow *f);
 
 enum { TAG_FLOW_Z = 3, TAG_FLOW_ACCEPT = 4 };
@@ -1444,7 +1446,7 @@ __global__ void flow_z_kernel(KParams p, uint64_t cycle, float *z)
 // Metropolis-Hastings test of the flow proposal x' for every chain:
 //   log u <= [log p(x') - log p(x)] + [log q(x) - log q(x')],
 // then the Full accumulators record the observables at the chain's position
-// (row `krow`, every observable has nskip 1 in this mode).
+// (row `krow`, every observable has nskip 1 in this mode; krow < 0 records nothing).
 __global__ void flow_accept_kernel(KParams p, const float *xprop, const float *lq_prop, const float *lq_cur, uint64_t cycle,
                                    int64_t krow, int64_t *nacc_flow)
 {
@@ -1467,6 +1469,7 @@ __global__ void flow_accept_kernel(KParams p, const float *xprop, const float *l
         }
         nacc_flow[c] += 1;
     }
+    if (krow < 0) { return; }
     float vals[2 * MCIG_MAXDIM + 8];
     for (int o = 0; o < p.nobs; ++o) {
         const ObsDesc &od = p.obs[o];
@@ -1510,8 +1513,6 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
         (rc = lq_prop.alloc(nc)) || (rc = nflow.alloc(nc))) {
         return rc;
     }
-    CK(cudaMemsetAsync(nflow.p, 0, nc * sizeof(int64_t), h->stream));
-    // the flow-step kernels read the float parameter blob from global memory
     CK(cudaEventRecord(h->ev[0], h->stream));
     if (do_find && h->nfind != 0) {
         KParams c = kp;
@@ -1527,24 +1528,50 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
         if ((rc = launch(h, d))) { return rc; }
     }
     const int tb = 128, tg = (int)((nc + tb - 1) / tb);
-    float loss = 0.f;
-    auto train = [&]() -> int {
-        walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
-        ++h->launches;
-        cudaError_t e = cudaStreamSynchronize(h->stream);
-        if (e != cudaSuccess) { return set_err(MCIG_ERR_CUDA, "train: %s", cudaGetErrorString(e)); }
-        return mcig_flow_train_device(f, xf.p, (int64_t)nc, train_steps, batch, lr, &loss);
-    };
-    if (train_steps > 0 && (rc = train())) { return rc; }
-    CK(cudaEventRecord(h->ev[2], h->stream));
     KParams sp = kp;
     sp.mode = KMODE_SAMPLE;
     for (size_t o = 0; o < h->obs.size(); ++o) {
         sp.obs[o].data = h->obsdata[o].p;
         sp.obs[o].nstore = h->obs_nstore[o];
     }
-    int64_t step = 0, next_refresh = refresh > 0 ? refresh : INT64_MAX;
     uint64_t cycle = 0;
+    // one independence proposal for every chain; krow = Full row to record, -1 none.
+    // Leaves the chain positions (before the move) as rows in xf.
+    auto flow_cycle = [&](int64_t krow) -> int {
+        walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
+        int r;
+        if ((r = mcig_flow_pass_device(f, 1, xf.p, (int64_t)nc, z.p, lq_cur.p, nullptr, h->stream))) { return r; }
+        flow_z_kernel<<<tg, tb, 0, h->stream>>>(sp, cycle, z.p);
+        if ((r = mcig_flow_pass_device(f, 0, z.p, (int64_t)nc, xprop.p, lq_prop.p, nullptr, h->stream))) { return r; }
+        flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p);
+        h->launches += 5;
+        CK(cudaGetLastError());
+        ++cycle;
+        return MCIG_OK;
+    };
+    // adaptation: train_steps cycles of period-1 local steps, a snapshot of the chain
+    // positions and one Adam step on `batch` rows drawn from it.  Each step sees new
+    // positions, so the flow does not fit a fixed sample; from the first quarter on
+    // the cycles also make (unrecorded) flow proposals, which carry chains between modes.
+    for (int t = 0; t < train_steps; ++t) {
+        if (period > 1) {
+            KParams l = kp;
+            l.mode = KMODE_STEPS;
+            l.nsteps = period - 1;
+            if ((rc = launch(h, l))) { return rc; }
+        }
+        walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
+        ++h->launches;
+        if ((rc = mcig_flow_train_device(f, xf.p, (int64_t)nc, 1, batch, lr, nullptr, h->stream))) { return rc; }
+        h->launches += 5;
+        if (4 * t >= train_steps && (rc = flow_cycle(-1))) { return rc; }
+    }
+    CK(cudaMemsetAsync(nflow.p, 0, nc * sizeof(int64_t), h->stream));
+    const uint64_t cycle0 = cycle;
+    CK(cudaEventRecord(h->ev[2], h->stream));
+    // sampling: period-1 recorded local steps, then one recorded flow proposal; with
+    // refresh > 0 the flow takes one more Adam step every `refresh` steps
+    int64_t step = 0, next_refresh = refresh > 0 ? refresh : INT64_MAX;
     std::vector<int64_t> hacc(nc);
     while (step < nmc) {
         const int64_t nloc = std::min<int64_t>(period - 1, nmc - step);
@@ -1556,18 +1583,14 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
             step += nloc;
         }
         if (step < nmc) {
-            walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
-            if ((rc = mcig_flow_pass_device(f, 1, xf.p, (int64_t)nc, z.p, lq_cur.p, nullptr, h->stream))) { return rc; }
-            flow_z_kernel<<<tg, tb, 0, h->stream>>>(sp, cycle, z.p);
-            if ((rc = mcig_flow_pass_device(f, 0, z.p, (int64_t)nc, xprop.p, lq_prop.p, nullptr, h->stream))) { return rc; }
-            flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, step, nflow.p);
-            h->launches += 5;
-            CK(cudaGetLastError());
+            if ((rc = flow_cycle(step))) { return rc; }
             ++step;
-            ++cycle;
         }
         if (step >= next_refresh && step < nmc) {
-            if (train_steps > 0 && (rc = train())) { return rc; }
+            if (train_steps > 0 && batch > 0) {
+                if ((rc = mcig_flow_train_device(f, xf.p, (int64_t)nc, 1, batch, lr, nullptr, h->stream))) { return rc; }
+                h->launches += 5;
+            }
             next_refresh += refresh;
         }
     }
@@ -1584,7 +1607,7 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     if (flow_acceptance) {
         int64_t a = 0;
         for (int64_t v : hacc) { a += v; }
-        *flow_acceptance = cycle > 0 ? (double)a / ((double)cycle * (double)nc) : 0.;
+        *flow_acceptance = cycle > cycle0 ? (double)a / ((double)(cycle - cycle0) * (double)nc) : 0.;
     }
     h->h_nacc.resize(nc);
     h->h_nrej.resize(nc);
@@ -1631,6 +1654,27 @@ struct mcig_batch {
     cudaGraphExec_t gexec = nullptr;
     float last_ms = 0.f;
 };
+
+// Uncorrelated/Noop estimator of every batch series, one thread per series, with the
+// estimator code of mcig_integrate (this unit is compiled with -fmad=false), so a
+// batched integral's error is the one its own integrate computes
+static __global__ void batch_estimate_kernel(const BatchSeries *__restrict__ series, int nseries, double *avg,
+                                             double *err)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseries) { return; }
+    const BatchSeries q = series[s];
+    double a = 0., e = 0.;
+    if (q.noop) { a = q.data[0]; }
+    else { uncorr_core(q.n, [&](int64_t i) { return q.data[i * q.stride]; }, q.one_d, a, e); }
+    avg[s] = a;
+    err[s] = e;
+}
+
+void mcig_batch_estimate_launch(const BatchSeries *series, int nseries, double *avg, double *err, cudaStream_t st)
+{
+    batch_estimate_kernel<<<(nseries + 127) / 128, 128, 0, st>>>(series, nseries, avg, err);
+}
 
 static int batch_grid(int nunits, int block)
 {

@@ -31,6 +31,7 @@
 #define MCIG_MAXTYPES 4
 #define MCIG_PERIODIC_MAXWRAP 64
 #define MCIG_MAXDIM 64
+#define MCIG_FAST_BLOCK 64 // threads per block of the register-resident kernel (slot stride)
 #define MCIG_FCONST 2080 // floats of sampling-function data in the parameter block (register-resident kernel)
 
 enum { RNG_PHILOX = 0, RNG_TAPE = 1 };
@@ -59,6 +60,7 @@ struct ObsDesc {
     int full32;   // Full data stored as float
     // n / d == __umulhi(n, magic) >> shift for n < 2^31 (register-resident kernel)
     uint32_t bs_magic, bs_shift, sk_magic, sk_shift;
+    double inv_bs; // 1. / bs (Block normalisation, BlockAccumulator.cpp)
 };
 
 struct KParams {

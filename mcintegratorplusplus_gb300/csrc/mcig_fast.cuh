@@ -23,6 +23,8 @@
 
 #include "mcig_common.cuh"
 
+#define MCIG_FAST_UNROLLED_OBS 4  // observables handled by the unrolled loop
+
 // log density of the walker (padded to MAXD coordinates with zeros: padded
 // coordinates never move, and the parameter data is zero-padded, so no loop
 // needs a per-coordinate predicate)
@@ -136,7 +138,7 @@ struct FastSampler {
     const KParams &p;
     const FastConst &fc;
     const int c;
-    ST *slots; // [nobsdim][blockDim]
+    ST *slots; // [nobsdim][MCIG_FAST_BLOCK]
     float x[MAXD];
     float st[MCIG_MAXTYPES];
     float lp;
@@ -232,49 +234,97 @@ struct FastSampler {
         return acc;
     }
 
-    __device__ __forceinline__ ST &slot(int j) { return slots[(size_t)j * blockDim.x + threadIdx.x]; }
+    __device__ __forceinline__ ST &slot(int j) { return slots[j * MCIG_FAST_BLOCK + threadIdx.x]; }
 
-    // observableFunction of the test classes (oracle obs_eval), in float, into
-    // v[0..nv) with compile-time indices; returns nv
-    __device__ __forceinline__ int observe(const ObsDesc &od, float *v) const
+    // AccumulatorInterface::accumulate of the values v[0..nv) (nv <= NV, compile-time
+    // indices) of observable od at accumulation index k.  Full: one coalesced row
+    // per value.  Simple/Block: running sums in the shared-memory slots; `flush`
+    // marks the last index of block `blk`, whose mean (sum * 1/blocksize) is written
+    // and the sums reset (BlockAccumulator.cpp).
+    template <int NV>
+    __device__ __forceinline__ void put(const ObsDesc &od, uint32_t k, bool flush, uint32_t blk, const float *v, int nv)
     {
-        const int nd = p.ndim;
+        const size_t stride = (size_t)p.nchains;
+        if (od.acc == MCIG_ACC_FULL) {
+            const size_t row = (size_t)p.acc_offset + k;
+            if (od.full32) {
+                float *dst = (float *)od.data + row * (size_t)nv * stride + c;
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    if (NV == 1 || j < nv) { dst[j * stride] = v[j]; }
+                }
+            } else {
+                double *dst = (double *)od.data + row * (size_t)nv * stride + c;
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    if (NV == 1 || j < nv) { dst[j * stride] = (double)v[j]; }
+                }
+            }
+            return;
+        }
+        ST *sl = slots + od.voff * MCIG_FAST_BLOCK + threadIdx.x;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            if (NV == 1 || j < nv) { Slot::add(sl[j * MCIG_FAST_BLOCK], v[j]); }
+        }
+        if (od.acc == MCIG_ACC_BLOCK && flush) {
+            double *dst = (double *)od.data + (size_t)blk * nv * stride + c;
+#pragma unroll
+            for (int j = 0; j < NV; ++j) {
+                if (NV == 1 || j < nv) {
+                    dst[j * stride] = Slot::get(sl[j * MCIG_FAST_BLOCK]) * od.inv_bs;
+                    Slot::zero(sl[j * MCIG_FAST_BLOCK]);
+                }
+            }
+        }
+    }
+
+    // observableFunction of the test classes (oracle obs_eval), in float, then put();
+    // the one-value observables take the one-value path
+    __device__ __forceinline__ void observe_put(const ObsDesc &od, uint32_t k, bool flush, uint32_t blk)
+    {
         switch (od.kind) {
         case MCIG_OBS_X2SUM:
         case MCIG_OBS_X2MEAN: {
             float s = 0.f;
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); } // padded coordinates are 0
-            v[0] = od.kind == MCIG_OBS_X2SUM ? s : s / (float)nd;
-            return 1;
+            const float v = od.kind == MCIG_OBS_X2SUM ? s : s / (float)p.ndim;
+            put<1>(od, k, flush, blk, &v, 1);
+            break;
         }
-        case MCIG_OBS_XND:
-#pragma unroll
-            for (int i = 0; i < MAXD; ++i) { v[i] = x[i]; }
-            return nd;
-        case MCIG_OBS_X2:
+        case MCIG_OBS_XND: put<MAXD>(od, k, flush, blk, x, p.ndim); break;
+        case MCIG_OBS_X2: {
+            float v[MAXD];
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) { v[i] = x[i] * x[i]; }
-            return nd;
-        case MCIG_OBS_CONST: v[0] = (float)p.params[od.poff]; return 1;
+            put<MAXD>(od, k, flush, blk, v, p.ndim);
+            break;
+        }
+        case MCIG_OBS_CONST: {
+            const float v = (float)p.params[od.poff];
+            put<1>(od, k, flush, blk, &v, 1);
+            break;
+        }
         case MCIG_OBS_XI: {
             const int idx = (int)p.params[od.poff];
-            float s = 0.f;
+            float v = 0.f;
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) { s = (i == idx) ? x[i] : s; }
-            v[0] = s;
-            return 1;
+            for (int i = 0; i < MAXD; ++i) { v = (i == idx) ? x[i] : v; }
+            put<1>(od, k, flush, blk, &v, 1);
+            break;
         }
         case MCIG_OBS_POLYNOM: {
-            float s = 0.f;
+            float v = 0.f;
 #pragma unroll
-            for (int i = 0; i < MAXD; ++i) { s += x[i]; }
-            v[0] = s;
-            return 1;
+            for (int i = 0; i < MAXD; ++i) { v += x[i]; }
+            put<1>(od, k, flush, blk, &v, 1);
+            break;
         }
         case MCIG_OBS_X2BLOCK: {
             const double *pp = p.params + od.poff;
             const int nb = (int)pp[0];
+            float v[MAXD];
 #pragma unroll
             for (int kb = 0; kb < MAXD; ++kb) {
                 float s = 0.f;
@@ -287,56 +337,35 @@ struct FastSampler {
                 }
                 v[kb] = s;
             }
-            return nb;
+            put<MAXD>(od, k, flush, blk, v, nb);
+            break;
         }
-        default: return 0;
+        default: break;
         }
     }
 
-    // one accumulation of observable o at accumulation index k (AccumulatorInterface::accumulate)
-    __device__ __forceinline__ void accumulate(const ObsDesc &od, uint32_t k)
+    // observable od after step r: accumulation index k = r / nskip when nskip
+    // divides r (AccumulatorInterface.cpp:31-60), block end when blocksize divides k + 1
+    __device__ __forceinline__ void obs_step(const ObsDesc &od, uint32_t r)
     {
-        float v[MAXD];
-        const int nv = observe(od, v);
-        if (od.acc == MCIG_ACC_FULL) { // FullAccumulator: one coalesced row per value
-            const size_t stride = (size_t)p.nchains;
-            const size_t row = (size_t)p.acc_offset + k;
-            if (od.full32) {
-                float *dst = (float *)od.data + row * nv * stride + c;
-#pragma unroll
-                for (int j = 0; j < MAXD; ++j) {
-                    if (j < nv) { dst[j * stride] = v[j]; }
-                }
-            } else {
-                double *dst = (double *)od.data + row * nv * stride + c;
-#pragma unroll
-                for (int j = 0; j < MAXD; ++j) {
-                    if (j < nv) { dst[j * stride] = (double)v[j]; }
-                }
-            }
-            return;
+        uint32_t k = r;
+        if (od.nskip != 1) {
+            k = fast_div(r, od.sk_magic, od.sk_shift);
+            if (k * (uint32_t)od.nskip != r) { return; }
         }
-        ST *sl = slots + (size_t)od.voff * blockDim.x + threadIdx.x;
-#pragma unroll
-        for (int j = 0; j < MAXD; ++j) {
-            if (j < nv) { Slot::add(sl[j * blockDim.x], v[j]); }
+        uint32_t blk = 0;
+        bool flush = false;
+        if (od.acc == MCIG_ACC_BLOCK) {
+            const uint32_t q = fast_div(k + 1, od.bs_magic, od.bs_shift);
+            flush = q * (uint32_t)od.bs == k + 1;
+            blk = q - 1;
         }
-        if (od.acc != MCIG_ACC_BLOCK) { return; }
-        const uint32_t blk = fast_div(k + 1, od.bs_magic, od.bs_shift);
-        if (blk * (uint32_t)od.bs == k + 1) { // block complete: mean = sum * (1./blocksize)
-            const double normf = 1. / od.bs;
-            double *dst = (double *)od.data + (size_t)(blk - 1) * nv * p.nchains + c;
-#pragma unroll
-            for (int j = 0; j < MAXD; ++j) {
-                if (j < nv) {
-                    dst[(size_t)j * p.nchains] = Slot::get(sl[j * blockDim.x]) * normf;
-                    Slot::zero(sl[j * blockDim.x]);
-                }
-            }
-        }
+        observe_put(od, k, flush, blk);
     }
 
-    // n < 2^32 (checked on the host); accumulation indices in 32-bit arithmetic
+    // n < 2^32 (checked on the host); accumulation indices in 32-bit arithmetic.
+    // The first MCIG_FAST_UNROLLED_OBS observables are unrolled, so their
+    // descriptors are constant-bank operands; any further ones loop.
     __device__ void run(int64_t n, bool sample)
     {
         lp = fast_logp<MAXD>(p, fc, x);
@@ -346,15 +375,8 @@ struct FastSampler {
         for (uint32_t r = 0; r < n32; ++r) {
             na += step() ? 1u : 0u;
             if (!sample) { continue; }
-            for (int o = 0; o < p.nobs; ++o) {
-                const ObsDesc &od = p.obs[o];
-                const uint32_t ns = (uint32_t)od.nskip;
-                if (ns == 1u) { accumulate(od, r); }
-                else {
-                    const uint32_t q = fast_div(r, od.sk_magic, od.sk_shift);
-                    if (q * ns == r) { accumulate(od, q); }
-                }
-            }
+#pragma unroll 1
+            for (int o = 0; o < p.nobs; ++o) { obs_step(p.obs[o], r); }
         }
         if (sample) {
             for (int o = 0; o < p.nobs; ++o) { // SimpleAccumulator::_finalize
@@ -419,7 +441,7 @@ struct FastSampler {
 };
 
 template <int MAXD, int MOVE, bool KAHAN>
-__global__ void __launch_bounds__(128) mcig_fast_kernel(const KParams p, const FastConst fc)
+__global__ void __launch_bounds__(2 * MCIG_FAST_BLOCK) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using ST = typename FastSlot<KAHAN>::T;
@@ -438,6 +460,8 @@ void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, i
                       cudaStream_t st)
 {
     auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN>;
+    // shared memory as large as possible, so the accumulator slots never limit residency
+    cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
     if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
     k<<<grid, block, smem, st>>>(p, *fc);
 }

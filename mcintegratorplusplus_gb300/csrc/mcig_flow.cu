@@ -703,9 +703,9 @@ static int flow_ensure(mcig_flow *f, int64_t n, bool tape)
     return MCIG_OK;
 }
 
-static int flow_cast(mcig_flow *f)
+static int flow_cast(mcig_flow *f, cudaStream_t st)
 {
-    flow_cast_kernel<<<256, 256, 0, f->st>>>(f->theta, f->wb, f->d, f->L);
+    flow_cast_kernel<<<256, 256, 0, st>>>(f->theta, f->wb, f->d, f->L);
     FCK(cudaGetLastError());
     return MCIG_OK;
 }
@@ -764,7 +764,7 @@ extern "C" int mcig_flow_create(int ndim, int nlayers, int hidden, uint64_t seed
     FCK(cudaMemcpy(f->theta, th.data(), th.size() * sizeof(float), cudaMemcpyHostToDevice));
     FCK(cudaMemset(f->m, 0, f->np * sizeof(float)));
     FCK(cudaMemset(f->v, 0, f->np * sizeof(float)));
-    int rc = flow_cast(f);
+    int rc = flow_cast(f, f->st);
     if (rc) { return rc; }
     FCK(cudaFuncSetAttribute(flow_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowSmem)));
     FCK(cudaFuncSetAttribute(flow_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowBwdSmem)));
@@ -803,7 +803,7 @@ extern "C" int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n)
     f->adam_t = 0;
     FCK(cudaMemset(f->m, 0, f->np * sizeof(float)));
     FCK(cudaMemset(f->v, 0, f->np * sizeof(float)));
-    int rc = flow_cast(f);
+    int rc = flow_cast(f, f->st);
     if (rc) { return rc; }
     FCK(cudaStreamSynchronize(f->st));
     return MCIG_OK;
@@ -856,13 +856,13 @@ extern "C" int mcig_flow_inverse(mcig_flow *f, const double *x, int64_t n, doubl
 }
 
 // loss -mean log q(x) and its gradient on device data d_x [n][D]; gradient left in f->grad
-static int flow_loss_grad_device(mcig_flow *f, const float *d_x, int64_t n, float *loss_host)
+static int flow_loss_grad_device(mcig_flow *f, const float *d_x, int64_t n, float *loss_host, cudaStream_t st)
 {
     int rc = flow_ensure(f, n, true);
     if (rc) { return rc; }
-    rc = mcig_flow_pass_device(f, 1, d_x, n, f->buf_out, f->buf_logq, f->buf_tape, f->st);
+    rc = mcig_flow_pass_device(f, 1, d_x, n, f->buf_out, f->buf_logq, f->buf_tape, st);
     if (rc) { return rc; }
-    FCK(cudaMemsetAsync(f->grad, 0, f->np * sizeof(float), f->st));
+    FCK(cudaMemsetAsync(f->grad, 0, f->np * sizeof(float), st));
     FlowBwdArgs b;
     b.D = f->D; b.d = f->d; b.L = f->L; b.n = (int)n;
     b.inv_batch = 1.f / (float)n;
@@ -870,12 +870,12 @@ static int flow_loss_grad_device(mcig_flow *f, const float *d_x, int64_t n, floa
     b.grad = f->grad; b.x = d_x; b.mu = f->theta + f->base_off; b.logsig = f->theta + f->base_off + f->D;
     b.wstride = WB_LAYER; b.pstride = f->pstride; b.base_off = f->base_off;
     const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
-    flow_backward_kernel<<<grid, FLOW_THREADS, sizeof(FlowBwdSmem), f->st>>>(b);
+    flow_backward_kernel<<<grid, FLOW_THREADS, sizeof(FlowBwdSmem), st>>>(b);
     FCK(cudaGetLastError());
     if (loss_host) {
         std::vector<float> lq((size_t)n);
-        FCK(cudaMemcpyAsync(lq.data(), f->buf_logq, n * sizeof(float), cudaMemcpyDeviceToHost, f->st));
-        FCK(cudaStreamSynchronize(f->st));
+        FCK(cudaMemcpyAsync(lq.data(), f->buf_logq, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        FCK(cudaStreamSynchronize(st));
         double s = 0.;
         for (float v : lq) { s += v; }
         *loss_host = (float)(-s / (double)n);
@@ -895,7 +895,7 @@ extern "C" int mcig_flow_loss_grad(mcig_flow *f, const double *x, int64_t n, dou
     for (size_t i = 0; i < h.size(); ++i) { h[i] = (float)x[i]; }
     cudaMemcpyAsync(d_x, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, f->st);
     float l = 0.f;
-    rc = flow_loss_grad_device(f, d_x, n, &l);
+    rc = flow_loss_grad_device(f, d_x, n, &l, f->st);
     if (!rc && grad) {
         cudaMemcpyAsync(grad, f->grad, f->np * sizeof(float), cudaMemcpyDeviceToHost, f->st);
         cudaStreamSynchronize(f->st);
@@ -905,11 +905,14 @@ extern "C" int mcig_flow_loss_grad(mcig_flow *f, const double *x, int64_t n, dou
     return rc;
 }
 
-// Adam steps on minibatches drawn from device data d_x [nsrc][D]
-int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int steps, int batch, double lr, float *last_loss)
+// Adam steps on minibatches drawn from device data d_x [nsrc][D], queued on stream st;
+// with last_loss the call waits for st and returns the loss of the last minibatch
+int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int steps, int batch, double lr, float *last_loss,
+                           cudaStream_t st)
 {
-    if (batch < 1 || steps < 0) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: bad training arguments"); }
+    if (batch < 1 || steps < 0 || nsrc < 1) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow: bad training arguments"); }
     if (batch > f->batch_cap) {
+        FCK(cudaStreamSynchronize(st));
         cudaFree(f->buf_batch);
         FCK(cudaMalloc(&f->buf_batch, (int64_t)batch * f->D * sizeof(float)));
         f->batch_cap = batch;
@@ -918,18 +921,18 @@ int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int ste
     if (rc) { return rc; }
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     for (int it = 0; it < steps; ++it) {
-        flow_gather_kernel<<<(batch + 127) / 128, 128, 0, f->st>>>(d_x, nsrc, f->D, (uint32_t)f->seed, (uint32_t)f->adam_t,
-                                                                   f->buf_batch, batch);
-        rc = flow_loss_grad_device(f, f->buf_batch, batch, (it == steps - 1) ? last_loss : nullptr);
+        flow_gather_kernel<<<(batch + 127) / 128, 128, 0, st>>>(d_x, nsrc, f->D, (uint32_t)f->seed, (uint32_t)f->adam_t,
+                                                               f->buf_batch, batch);
+        rc = flow_loss_grad_device(f, f->buf_batch, batch, (it == steps - 1) ? last_loss : nullptr, st);
         if (rc) { return rc; }
         ++f->adam_t;
         const float c1 = 1.f / (1.f - powf(b1, (float)f->adam_t)), c2 = 1.f / (1.f - powf(b2, (float)f->adam_t));
-        flow_adam_kernel<<<256, 256, 0, f->st>>>(f->theta, f->grad, f->m, f->v, f->np, (float)lr, b1, b2, eps, c1, c2);
+        flow_adam_kernel<<<256, 256, 0, st>>>(f->theta, f->grad, f->m, f->v, f->np, (float)lr, b1, b2, eps, c1, c2);
         FCK(cudaGetLastError());
-        rc = flow_cast(f);
+        rc = flow_cast(f, st);
         if (rc) { return rc; }
     }
-    FCK(cudaStreamSynchronize(f->st));
+    if (last_loss) { FCK(cudaStreamSynchronize(st)); }
     return MCIG_OK;
 }
 
@@ -942,7 +945,7 @@ extern "C" int mcig_flow_train(mcig_flow *f, const double *x, int64_t n, int ste
     for (size_t i = 0; i < h.size(); ++i) { h[i] = (float)x[i]; }
     cudaMemcpy(d_x, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice);
     float l = 0.f;
-    const int rc = mcig_flow_train_device(f, d_x, n, steps, batch, lr, &l);
+    const int rc = mcig_flow_train_device(f, d_x, n, steps, batch, lr, &l, f->st);
     cudaFree(d_x);
     if (last_loss) { *last_loss = l; }
     return rc;

@@ -32,41 +32,8 @@ __global__ void __launch_bounds__(256) mcig_batch_kernel(const KParams *__restri
     }
 }
 
-// Uncorrelated estimator (src/Estimators.cpp:36-56, :125-155) on double data, one
-// thread per series of the batch
-__global__ void mcig_batch_estimate_kernel(const BatchSeries *__restrict__ series, int nseries, double *avg, double *err)
-{
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nseries) { return; }
-    const BatchSeries q = series[s];
-    const double SMALLEST_ERROR = 1.e-300;
-    double a = 0., e = 0.;
-    if (q.noop) {
-        a = q.data[0];
-    } else {
-        double sx = 0., sq = 0.;
-        for (int64_t i = 0; i < q.n; ++i) {
-            const double x = q.data[i * q.stride];
-            sx += x;
-            sq += x * x;
-        }
-        const double norm = 1. / q.n;
-        a = sx * norm;
-        e = sq * norm - a * a;
-        if (q.one_d) { e = (e > SMALLEST_ERROR) ? sqrt(e / (q.n - 1.)) : 0.; }
-        else { e = (e > SMALLEST_ERROR) ? sqrt(e * (1. / (q.n - 1.))) : 0.; }
-    }
-    avg[s] = a;
-    err[s] = e;
-}
-
 void mcig_batch_launch(const KParams *cfg, const BatchPhase *ph, const int2 *units, int nunits, int *counter, int grid,
                        int block, cudaStream_t st)
 {
     mcig_batch_kernel<<<grid, block, 0, st>>>(cfg, ph, units, nunits, counter);
-}
-
-void mcig_batch_estimate_launch(const BatchSeries *series, int nseries, double *avg, double *err, cudaStream_t st)
-{
-    mcig_batch_estimate_kernel<<<(nseries + 127) / 128, 128, 0, st>>>(series, nseries, avg, err);
 }

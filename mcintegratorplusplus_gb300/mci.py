@@ -379,9 +379,11 @@ class Flow:
         return loss.value
 
 
-def integrate_flow(m, flow, nmc, period=5, refresh=4096, train_steps=200, batch=2048, lr=1e-3, doFindMRT2step=True,
+def integrate_flow(m, flow, nmc, period=5, refresh=0, train_steps=400, batch=2048, lr=2e-3, doFindMRT2step=True,
                    doDecorrelation=True):
-    """MCI::integrate with the learned proposal (mcig_integrate_flow); returns avg, err, flow acceptance."""
+    """MCI::integrate with the learned proposal (mcig_integrate_flow): `train_steps` adaptation
+    cycles (period - 1 local steps + one Adam step on the current chain positions), then nmc
+    recorded steps with a flow proposal every `period` steps.  Returns avg, err, flow acceptance."""
     nod = max(m.getNObsDim(), 1)
     avg = np.zeros(nod)
     err = np.zeros(nod)

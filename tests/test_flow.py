@@ -129,7 +129,7 @@ def _run_c5(mcig, use_flow, nchains=2048, nmc=1 << 13):
     m.addObservable(mcig.OBS_XI, [0], 1, 1, False, mcig.EST_MJBLOCKER)
     if use_flow:
         f = mcig.Flow(D, L, H, seed=6)
-        avg, err, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=2048, train_steps=150, batch=2048, lr=2e-3)
+        avg, err, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=2048, train_steps=400, batch=2048, lr=2e-3)
     else:
         avg, err = m.integrate(nmc)
         acc = None

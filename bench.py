@@ -41,7 +41,11 @@ NCHAINS = 65536
 NMC = 10000
 BURNIN = 1000
 NBLOCKS = 100
-METRIC = "effective samples/s of <x.x> (C2: 65,536 chains x 16-D correlated Gaussian, plain MH)"
+METRIC = "effective samples/s on 1 GB300 at matched std-error: learned/batched vs plain MH"
+# ncu figures of the sampling launch (65,536 chains, 600 steps, 6 blocks of 100, four
+# accumulators): DRAM bytes read + written, and warp instructions per warp-step
+CAPTURE_DRAM_BYTES = 11.6e6 + 2.677e9
+INST_PER_WARP_STEP = 1907.0
 
 
 def target(seed=2024):
@@ -182,6 +186,11 @@ def run_gpu(args):
     algo_bytes = full_bytes + block_bytes + state_bytes
     pk, pk_kind = peaks()
     achieved = algo_bytes / (samp_ms * 1e-3) / 1e9
+    traffic = CAPTURE_DRAM_BYTES * (nchains / 65536.0) * (args.nmc / 600.0)
+    # instruction-issue bound: 4 warp-instructions per cycle per SM, 152 SMs
+    sm_mhz = ck["sm_mhz"] or float(pk.get("sm_max_mhz", 2070.0))
+    warp_steps = nchains / 32.0 * args.nmc
+    issue_ms = INST_PER_WARP_STEP * warp_steps / (152 * 4 * sm_mhz * 1e6) * 1e3
     flop_per_step = 2 * (NDIM * (NDIM + 1) // 2 + NDIM) + 2 * NDIM + 4 * (1 + NDIM) + 2 * NDIM
     line = {
         "metric": METRIC, "value": ess / (ms_dev * 1e-3), "unit": "effective samples/s",
@@ -200,13 +209,25 @@ def run_gpu(args):
                 "h2d_bytes_per_step": int(x0.numel() * 8), "d2h_bytes_per_step": int(2 * nod * 8),
                 "ms_per_step": ms_e2e},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": float(pk["hbm_gbs"]), "unit": "GB/s",
-                     "frac": achieved / float(pk["hbm_gbs"]), "traffic": None, "peak_source": pk_kind,
+                     "frac": achieved / float(pk["hbm_gbs"]), "traffic": traffic, "peak_source": pk_kind,
+                     "traffic_source": "ncu dram__bytes_read+write of a 600-step capture of this launch "
+                                       "(65,536 chains), scaled by chains x steps",
                      "kernel": "sampling launch (mcig_fast_kernel<16,ALL,Kahan>)",
                      "algorithmic_bytes_per_launch": algo_bytes, "kernel_ms": samp_ms,
                      "fp32_flop_per_step": flop_per_step},
+        "issue_roofline": {"bound": "instruction issue", "warp_inst_per_warp_step": INST_PER_WARP_STEP,
+                           "issue_limited_ms": issue_ms, "kernel_ms": samp_ms, "frac": issue_ms / samp_ms,
+                           "sm_mhz": sm_mhz, "source": "ncu smsp__inst_executed.sum of the same capture"},
         "gpu_launches": launches,
         "clocks": ck,
     }
+    if args.learned:
+        c5 = run_c5(argparse.Namespace(chains5=16384, nmc5=8192, warmup=1, steps=1))
+        line["learned_proposal"] = {
+            "workload": "C5: 16,384 chains x 24-D 4-mode mixture, 8-layer affine-coupling flow every 5th step",
+            "ess_per_s_flow": c5["value"], "ess_per_s_plain_mh": c5["plain_mh"]["value"],
+            "ratio": c5["ess_per_s_ratio_flow_over_plain"], "flow_acceptance": c5["flow"]["acceptance"],
+            "ms_flow": c5["ms_per_step"], "ms_plain": c5["plain_mh"]["ms_per_step"]}
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     return line
@@ -438,11 +459,13 @@ def run_c5(args):
             else:
                 m.integrate(nmc)
             if it >= args.warmup:
-                ms.append(_timed_device_ms(m.getLastTimings()))
+                tm = m.getLastTimings()
+                ms.append(_timed_device_ms(tm))
                 ca, _ = m.getChainResults()
                 ess.append(var_x1 * nch / float(np.var(ca[:, 0])))
         t = float(np.mean(ms)) * 1e-3
-        res[use_flow] = (float(np.mean(ess)) / t, t, float(np.mean(ess)), float(np.mean(accs)) if accs else None)
+        res[use_flow] = (float(np.mean(ess)) / t, t, float(np.mean(ess)), float(np.mean(accs)) if accs else None,
+                         {k: float(v) for k, v in tm.items()})
     ratio = res[True][0] / res[False][0]
     return {"metric": "effective samples/s of <x_1> (C5: 24-D 4-mode mixture, learned flow proposal)",
             "value": res[True][0], "unit": "effective samples/s", "n_gpus": 1, "steps": args.steps,
@@ -451,8 +474,9 @@ def run_c5(args):
             "data": "synthetic (seeded mixture, random-init flow)",
             "config": {"workload": "C5 learned proposal", "chains": nch, "ndim": D, "nmc": nmc, "flow_layers": 8,
                        "hidden": 128, "period": 5, "adaptation_cycles": 400, "refresh": 4096},
-            "plain_mh": {"value": res[False][0], "ms_per_step": res[False][1] * 1e3, "ess": res[False][2]},
-            "flow": {"ess": res[True][2], "acceptance": res[True][3]},
+            "plain_mh": {"value": res[False][0], "ms_per_step": res[False][1] * 1e3, "ess": res[False][2],
+                         "phases": res[False][4]},
+            "flow": {"ess": res[True][2], "acceptance": res[True][3], "phases": res[True][4]},
             "ess_per_s_ratio_flow_over_plain": ratio}
 
 
@@ -467,6 +491,8 @@ def main():
     ap.add_argument("--blocks", type=int, default=NBLOCKS)
     ap.add_argument("--cpu-chains", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="skip the learned-proposal comparison added to the default line")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"])
     ap.add_argument("--integrals", type=int, default=4096)
     ap.add_argument("--chains4", type=int, default=16384)
@@ -485,6 +511,7 @@ def main():
             print(json.dumps(run_reference(args)), flush=True)
         return
     if world > 1:  # replicas only: every rank runs its own chains, rank 0 reports the max-time aggregate
+        args.learned = False
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))

@@ -416,9 +416,7 @@ extern "C" int mcig_set_ndecorrelation_steps(mcig_mci *h, int64_t n) { h->ndecor
 
 extern "C" int mcig_set_multistep_move(mcig_mci *h, int nsteps, int sub_srrd, int sub_veclen, double sub_step)
 {
-    if (sub_srrd != MCIG_SRRD_UNIFORM && sub_srrd != MCIG_SRRD_GAUSSIAN) {
-        return set_err(MCIG_ERR_UNSUPPORTED, "only uniform and Gaussian sub-moves run on the device");
-    }
+    if (sub_srrd < MCIG_SRRD_UNIFORM || sub_srrd > MCIG_SRRD_FISHER) { return set_err(MCIG_ERR_DOMAIN, "[createSRRDVecMove] Unhandled SRRDType enumerator."); }
     if (sub_veclen < 1 || h->ndim % sub_veclen != 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[MCI::setTrialMove] MCI's number of walkers must be a multiple of passed veclen."); }
     if (nsteps < 0 || nsteps > 65534) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "multi-step move: nsteps must be in [0, 65534]"); }
     h->movetype = MCIG_MOVE_MULTISTEP;
@@ -437,9 +435,6 @@ extern "C" int mcig_set_trial_move(mcig_mci *h, int movetype, int srrd, int vecl
     if (movetype == MCIG_MOVE_MULTISTEP) { return mcig_set_multistep_move(h, h->ndim, MCIG_SRRD_UNIFORM, 1, 0.05); }
     if (movetype != MCIG_MOVE_ALL && movetype != MCIG_MOVE_VEC) { return set_err(MCIG_ERR_DOMAIN, "[createMoveDefault] Unhandled MoveType enumerator."); }
     if (srrd < MCIG_SRRD_UNIFORM || srrd > MCIG_SRRD_FISHER) { return set_err(MCIG_ERR_DOMAIN, "[createSRRDAllMove] Unhandled SRRDType enumerator."); }
-    if (srrd != MCIG_SRRD_UNIFORM && srrd != MCIG_SRRD_GAUSSIAN) {
-        return set_err(MCIG_ERR_UNSUPPORTED, "only the uniform and Gaussian distributions run on the device");
-    }
     if (ntypes < 1) { ntypes = 1; }
     if (ntypes > MCIG_MAXTYPES) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d step-size types on the device", MCIG_MAXTYPES); }
     const int vl = (movetype == MCIG_MOVE_VEC) ? std::max(1, veclen) : 0;
@@ -839,6 +834,7 @@ static int fill_common(mcig_mci *h, KParams &kp)
 static bool fast_eligible(const mcig_mci *h)
 {
     if (h->prec == MCIG_PREC_FP64 || h->replay || h->ndim > 32 || h->pdfs.empty()) { return false; }
+    if (h->srrd != MCIG_SRRD_UNIFORM && h->srrd != MCIG_SRRD_GAUSSIAN) { return false; }
     if (h->movetype != MCIG_MOVE_ALL && h->movetype != MCIG_MOVE_VEC) { return false; }
     if (h->movetype == MCIG_MOVE_VEC && h->ndim > 16) { return false; }
     for (auto &o : h->obs) {

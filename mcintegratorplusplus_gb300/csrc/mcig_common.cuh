@@ -234,6 +234,95 @@ __device__ __forceinline__ void move_draws<double>(P4 q, int gaussian, double *d
     }
 }
 
+// Move draws of every SRRDType with the standard library's default parameters
+// (createSymRRD specialisations, TrialMoveInterface.hpp:113-200, and the
+// SymmetrizedPRRD wrapper :82-98, which flips the sign with probability 1/2):
+//   Student t (n = 1) and Cauchy(0, 1):  tan(pi (u - 1/2))
+//   Fisher F(1, 1) = (z1/z2)^2 = Cauchy^2,  symmetrized
+//   Exponential(1) = Gamma(1, 1) = Weibull(1, 1):  -log u,  symmetrized
+//   Lognormal(0, 1): exp(z),  Chi-squared(1): z^2 (z standard normal),  symmetrized
+// Uniform and Gaussian are move_draws().  float: 4 values per Philox block, double: 2;
+// a symmetrized value takes its sign from a bit of the block that its magnitude leaves
+// unused (the low bits below the 24 / 53 bits of the uniforms).
+template <class R>
+__device__ __forceinline__ void move_draws_srrd(P4 q, int srrd, R *d /* Cpb<R>::v */);
+
+__device__ __forceinline__ float signed_by(uint32_t w, int bit, float v) { return ((w >> bit) & 1u) ? -v : v; }
+__device__ __forceinline__ double signed_by(uint32_t w, int bit, double v) { return ((w >> bit) & 1u) ? -v : v; }
+
+template <>
+__device__ __forceinline__ void move_draws_srrd<float>(P4 q, int srrd, float *d)
+{
+    const uint32_t w[4] = {q.a, q.b, q.c, q.d};
+    switch (srrd) {
+    case MCIG_SRRD_UNIFORM: move_draws<float>(q, 0, d); return;
+    case MCIG_SRRD_GAUSSIAN: move_draws<float>(q, 1, d); return;
+    case MCIG_SRRD_STUDENT:
+    case MCIG_SRRD_CAUCHY:
+    case MCIG_SRRD_FISHER:
+        for (int k = 0; k < 4; ++k) {
+            float sn, cs;
+            sincospif(((float)(w[k] >> 8) + 0.5f) * 5.9604644775390625e-08f - 0.5f, &sn, &cs); // (-1/2, 1/2)
+            const float t = sn / cs;
+            d[k] = (srrd == MCIG_SRRD_FISHER) ? signed_by(w[k], 0, t * t) : t;
+        }
+        return;
+    case MCIG_SRRD_EXPONENTIAL:
+    case MCIG_SRRD_GAMMA:
+    case MCIG_SRRD_WEIBULL:
+        for (int k = 0; k < 4; ++k) {
+            const float u = ((float)(w[k] >> 8) + 0.5f) * 5.9604644775390625e-08f; // (0, 1)
+            d[k] = signed_by(w[k], 0, -logf(u));
+        }
+        return;
+    default: { // LOGNORMAL, CHISQ
+        float z[4];
+        box_muller_f(q.a, q.b, z[0], z[1]);
+        box_muller_f(q.c, q.d, z[2], z[3]);
+        for (int k = 0; k < 4; ++k) {
+            const float m = (srrd == MCIG_SRRD_LOGNORMAL) ? expf(z[k]) : z[k] * z[k];
+            d[k] = signed_by(k < 2 ? q.a : q.c, k & 1, m); // bits 0, 1 of the words whose top 24 bits made u
+        }
+        return;
+    }
+    }
+}
+
+template <>
+__device__ __forceinline__ void move_draws_srrd<double>(P4 q, int srrd, double *d)
+{
+    switch (srrd) {
+    case MCIG_SRRD_UNIFORM: move_draws<double>(q, 0, d); return;
+    case MCIG_SRRD_GAUSSIAN: move_draws<double>(q, 1, d); return;
+    case MCIG_SRRD_STUDENT:
+    case MCIG_SRRD_CAUCHY:
+    case MCIG_SRRD_FISHER: {
+        const double u[2] = {u01_d(q.a, q.b), u01_d(q.c, q.d)};
+        const uint32_t lo[2] = {q.b, q.d};
+        for (int k = 0; k < 2; ++k) {
+            double sn, cs;
+            sincospi((u[k] - 0.5) + 0x1p-54, &sn, &cs); // u in [0, 1): u - 1/2 exact, + 2^-54 in (-1/2, 1/2)
+            const double t = sn / cs;
+            d[k] = (srrd == MCIG_SRRD_FISHER) ? signed_by(lo[k], 0, t * t) : t;
+        }
+        return;
+    }
+    case MCIG_SRRD_EXPONENTIAL:
+    case MCIG_SRRD_GAMMA:
+    case MCIG_SRRD_WEIBULL:
+        d[0] = signed_by(q.b, 0, -log(1.0 - u01_d(q.a, q.b)));
+        d[1] = signed_by(q.d, 0, -log(1.0 - u01_d(q.c, q.d)));
+        return;
+    default: { // LOGNORMAL, CHISQ
+        double z0, z1;
+        box_muller_d(q, z0, z1);
+        d[0] = signed_by(q.b, 0, (srrd == MCIG_SRRD_LOGNORMAL) ? exp(z0) : z0 * z0);
+        d[1] = signed_by(q.d, 0, (srrd == MCIG_SRRD_LOGNORMAL) ? exp(z1) : z1 * z1);
+        return;
+    }
+    }
+}
+
 template <class R>
 __device__ __forceinline__ R accept_draw(P4 q);
 template <>

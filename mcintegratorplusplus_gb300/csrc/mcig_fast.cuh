@@ -375,8 +375,11 @@ struct FastSampler {
         for (uint32_t r = 0; r < n32; ++r) {
             na += step() ? 1u : 0u;
             if (!sample) { continue; }
-#pragma unroll 1
-            for (int o = 0; o < p.nobs; ++o) { obs_step(p.obs[o], r); }
+#pragma unroll
+            for (int o = 0; o < MCIG_FAST_UNROLLED_OBS; ++o) {
+                if (o < p.nobs) { obs_step(p.obs[o], r); }
+            }
+            for (int o = MCIG_FAST_UNROLLED_OBS; o < p.nobs; ++o) { obs_step(p.obs[o], r); }
         }
         if (sample) {
             for (int o = 0; o < p.nobs; ++o) { // SimpleAccumulator::_finalize
@@ -440,8 +443,11 @@ struct FastSampler {
     }
 };
 
+// Up to 16 dimensions the kernel is held to 128 registers per thread: registers are
+// allocated in steps that make 136 or 144 per thread fit only six 64-thread blocks
+// per SM (912 of the 1,024 blocks of 65,536 chains, so a second wave), 128 fits eight.
 template <int MAXD, int MOVE, bool KAHAN>
-__global__ void __launch_bounds__(2 * MCIG_FAST_BLOCK) mcig_fast_kernel(const KParams p, const FastConst fc)
+__global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using ST = typename FastSlot<KAHAN>::T;

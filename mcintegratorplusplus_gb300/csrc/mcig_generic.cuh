@@ -339,7 +339,7 @@ struct GenericSampler {
     // draw j of the move group (substep, TAG_MOVE): coordinate-indexed for Philox
     __device__ __forceinline__ void move_group(int substep, int srrd, int b, R *d)
     {
-        move_draws<R>(ph.block(substep, TAG_MOVE, b), srrd == MCIG_SRRD_GAUSSIAN, d);
+        move_draws_srrd<R>(ph.block(substep, TAG_MOVE, b), srrd, d);
     }
 
     // SRRDAllMove::trialMove (SRRDAllMove.hpp:67-80): xn = x + step(type(i)) * d_i

@@ -231,6 +231,32 @@ def test_vec_and_multistep_moves_statistics(mcig):
         assert np.all(z < 3.5), (setup, avg, err)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_every_srrd_distribution_statistics(mcig, prec):
+    """All ten SRRDType distributions (Factories.hpp:119-133) as all-coordinate and
+    vector moves (and as MultiStepMove sub-moves) sample exp(-x.x): <x_i^2> = 1/2."""
+    p = mcig.PREC_FP64 if prec == "fp64" else mcig.PREC_FP32
+    for srrd in range(10):
+        for mode in ("all", "vec", "multistep"):
+            g = mcig.MCI(4, 256, precision=p)
+            g.setSeed(100 + srrd)
+            g.addSamplingFunction(mcig.PDF_GAUSS)
+            if mode == "all":
+                g.setTrialMove(mcig.MOVE_ALL, srrd)
+            elif mode == "vec":
+                g.setTrialMove(mcig.MOVE_VEC, srrd, 2)
+            else:
+                g.setMultiStepMove(2, srrd, 1, 0.3)
+                g.addMultiStepSamplingFunction(mcig.PDF_EXP)
+                g.setNfindMRT2Iterations(0)
+            g.setNdecorrelationSteps(500)
+            g.addObservable(mcig.OBS_X2, (), 256, 1, False, mcig.EST_UNCORRELATED)
+            avg, err = g.integrate(1 << 14)
+            z = np.abs(avg - 0.5) / err
+            assert np.all(z < 4.0), (srrd, mode, avg, err)
+            assert 0.05 < g.getAcceptanceRate() <= 1.0, (srrd, mode)
+
+
 def test_periodic_and_no_pdf_paths(mcig):
     g = mcig.MCI(3, 256, precision=mcig.PREC_FP64)
     g.setSeed(3)
@@ -256,8 +282,8 @@ def test_error_behaviour(mcig):
         g.addObservable(mcig.OBS_X2SUM, (), 0, 1, True, mcig.EST_NOOP)
     with pytest.raises(ValueError, match="multiple of passed veclen"):
         g.setTrialMove(mcig.MOVE_VEC, 0, 2)
-    with pytest.raises(NotImplementedError):
-        g.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_CAUCHY)
+    with pytest.raises(mcig.DomainError, match="Unhandled SRRDType"):
+        g.setTrialMove(mcig.MOVE_ALL, 10)
     with pytest.raises(ValueError):
         g.addSamplingFunction(mcig.PDF_GAUSS_PREC, np.eye(2))
     g2 = mcig.MCI(3, 1, precision=mcig.PREC_FP64)

@@ -422,6 +422,9 @@ def run_c4(args):
             "max_z_vs_analytic": zs}
 
 
+C5_ADAPT = 200  # adaptation cycles (period - 1 local steps + one Adam step on all chain positions)
+
+
 def c5_target(seed=2024, ndim=24):
     rng = np.random.default_rng(seed)
     Q, _ = np.linalg.qr(rng.standard_normal((ndim, 2)))
@@ -453,8 +456,8 @@ def run_c5(args):
             m.addObservable(mcig.OBS_XI, [0], 1, 1, False, mcig.EST_UNCORRELATED)
             if use_flow:
                 f = mcig.Flow(D, 8, 128, seed=6 + it)
-                _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=400,
-                                                batch=4096, lr=2e-3)
+                _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=C5_ADAPT,
+                                                batch=nch, lr=3e-3)
                 accs.append(acc)
             else:
                 m.integrate(nmc)
@@ -473,7 +476,8 @@ def run_c5(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 walker, bf16 flow GEMMs (f32 accumulate)",
             "data": "synthetic (seeded mixture, random-init flow)",
             "config": {"workload": "C5 learned proposal", "chains": nch, "ndim": D, "nmc": nmc, "flow_layers": 8,
-                       "hidden": 128, "period": 5, "adaptation_cycles": 400, "refresh": 4096},
+                       "hidden": 128, "period": 5, "adaptation_cycles": C5_ADAPT, "adam_batch": nch,
+                       "adam_lr": 3e-3, "refresh": 4096},
             "plain_mh": {"value": res[False][0], "ms_per_step": res[False][1] * 1e3, "ess": res[False][2],
                          "phases": res[False][4]},
             "flow": {"ess": res[True][2], "acceptance": res[True][3], "phases": res[True][4]},

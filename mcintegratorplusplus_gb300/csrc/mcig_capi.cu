@@ -701,6 +701,12 @@ static void fill_fast_const(const mcig_mci *h, FastConst &kp)
     const int nd = h->ndim;
     int md = 4;
     while (md < nd) { md *= 2; }
+    memset(kp.tw, 0, sizeof(kp.tw));
+    for (int i = 0; i < nd && i < 32; ++i) {
+        int t = 0;
+        while (t + 1 < h->ntypes && i >= h->typeEnds[t]) { ++t; }
+        kp.tw[t][i] = 1.f;
+    }
     memset(kp.fconst, 0, sizeof(kp.fconst));
     for (const PdfDef &d : h->pdfs) {
         if (d.kind == MCIG_PDF_GAUSS_PREC) {

@@ -109,13 +109,14 @@ struct KParams {
     int *status;
 };
 
-// Register-resident kernel only: Philox round keys (key + r*W for r = 0..9) and
-// the sampling-function data at fixed offsets (Cholesky factor U[MAXD][MAXD] at
+// Register-resident kernel only: Philox round keys (key + r*W for r = 0..9), the
+// one-hot step-type table of the coordinates, and the sampling-function data at fixed offsets (Cholesky factor U[MAXD][MAXD] at
 // 0, mixture [nc, per component: log-normalisation, m[MAXD], 1/s[MAXD]] at
 // MAXD*MAXD), passed as a second kernel parameter so that the unrolled loops
 // read them as constant-bank operands.
 struct FastConst {
     uint32_t rk[20];
+    float tw[MCIG_MAXTYPES][32]; // tw[t][i] = 1 if coordinate i < ndim has step type t, else 0
     float fconst[MCIG_FCONST];
 };
 

@@ -154,25 +154,21 @@ struct FastSampler {
         ctr = p.ctr[c];
     }
 
-    // step size of coordinate i (0 for the padding beyond ndim)
+    // step size of coordinate i: st[type(i)], 0 for the padding beyond ndim.  The type
+    // table is one-hot in the constant bank, so one step type costs one multiply.
     __device__ __forceinline__ float step_i(int i) const
     {
-        return (i < p.ndim) ? (p.ntypes == 1 ? st[0] : step_of(i)) : 0.f;
+        float s = st[0] * fc.tw[0][i];
+        if (p.ntypes > 1) {
+#pragma unroll
+            for (int t = 1; t < MCIG_MAXTYPES; ++t) { s = fmaf(st[t], fc.tw[t][i], s); }
+        }
+        return s;
     }
 
     __device__ __forceinline__ P4 block(uint32_t tag, uint32_t b) const
     {
         return philox4x32_10_rk(s0, s1, (uint32_t)c, (tag << 12) | b, fc.rk);
-    }
-
-    __device__ __forceinline__ float step_of(int i) const
-    {
-        float s = st[0];
-#pragma unroll
-        for (int t = 1; t < MCIG_MAXTYPES; ++t) {
-            if (t < p.ntypes && i >= p.typeEnds[t - 1]) { s = st[t]; }
-        }
-        return s;
     }
 
     // one Metropolis step (MCI::doStepMRT2, MCIntegrator.cpp:326-360)

@@ -237,14 +237,30 @@ __global__ void flow_cast_kernel(const float *theta, __nv_bfloat16 *wb, int d, i
 }
 
 // cooperative copy of a bf16 matrix [rows][cols] (global, dense) into a padded smem tile
-__device__ __forceinline__ void load_tile(__nv_bfloat16 *dst, int ld, const __nv_bfloat16 *src, int rows, int cols)
+// rows x COLS bf16 from global (row-major, contiguous) into shared memory with row
+// stride ld, 16 bytes per copy (source offsets, ld and the tiles are multiples of 8 elements)
+template <int COLS>
+__device__ __forceinline__ void load_tile(__nv_bfloat16 *dst, int ld, const __nv_bfloat16 *src, int rows)
 {
-    const int words = rows * cols / 2;
-    for (int i = threadIdx.x; i < words; i += blockDim.x) {
-        const int r = (2 * i) / cols, c = (2 * i) % cols;
-        *(uint32_t *)(dst + r * ld + c) = *(const uint32_t *)(src + 2 * i);
+    constexpr int VPR = COLS / 8; // 16-byte vectors per row
+    const int nv = rows * VPR;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        const int r = i / VPR, c = (i % VPR) * 8;
+        *(uint4 *)(dst + r * ld + c) = *(const uint4 *)(src + (size_t)i * 8);
     }
 }
+
+// sum of v over the 8 lanes that share lane & 3 (the accumulator rows of an mma fragment)
+__device__ __forceinline__ float sum_over_g(float v)
+{
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 16);
+    return v;
+}
+
+// paired float atomic add (address 8-byte aligned)
+__device__ __forceinline__ void atomic_add2(float *a, float x, float y) { atomicAdd((float2 *)a, make_float2(x, y)); }
 
 // the MLP of one layer on the a-half in s.A: s.H1, s.H2 (bf16) and, if want_o, s.O (float)
 __device__ void layer_mlp(FlowSmem &s, const float *P, int d, bool want_o)
@@ -289,9 +305,9 @@ __device__ void layer_mlp(FlowSmem &s, const float *P, int d, bool want_o)
 
 __device__ __forceinline__ void load_layer_weights(FlowSmem &s, const __nv_bfloat16 *wl)
 {
-    load_tile(s.W1n, LDA_S, wl + WB_W1N, FLOW_H, 16);
-    load_tile(s.W2n, LDH_S, wl + WB_W2N, FLOW_H, FLOW_H);
-    load_tile(s.W3n, LDH_S, wl + WB_W3N, 32, FLOW_H);
+    load_tile<16>(s.W1n, LDA_S, wl + WB_W1N, FLOW_H);
+    load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W2N, FLOW_H);
+    load_tile<FLOW_H>(s.W3n, LDH_S, wl + WB_W3N, 32);
 }
 
 __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
@@ -418,9 +434,9 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
         const float *P = f.theta + (int64_t)l * f.pstride;
         float *GP = f.grad + (int64_t)l * f.pstride;
         const __nv_bfloat16 *wl = f.wb + (int64_t)l * f.wstride;
-        load_tile(s.W1n, LDA_S, wl + WB_W1N, FLOW_H, 16);
-        load_tile(s.W2n, LDH_S, wl + WB_W2N, FLOW_H, FLOW_H);
-        load_tile(s.W3n, LDH_S, wl + WB_W3N, 32, FLOW_H);
+        load_tile<16>(s.W1n, LDA_S, wl + WB_W1N, FLOW_H);
+        load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W2N, FLOW_H);
+        load_tile<FLOW_H>(s.W3n, LDH_S, wl + WB_W3N, 32);
         for (int i = threadIdx.x; i < FLOW_ROWS * 16; i += blockDim.x) {
             const int r = i / 16, c = i % 16;
             const float v = (r < rows && c < d) ? f.tape[((int64_t)l * f.n + base + r) * 4 * d + c] : 0.f;
@@ -448,27 +464,30 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
             store_act(acc, s.bias + FLOW_H, true, s.H2, LDH_S, r0);
         }
         __syncthreads();
-        // coupling backward, one thread per sample: g_o = [g_sraw, g_t], g on the b half
-        for (int r = threadIdx.x; r < FLOW_ROWS; r += blockDim.x) {
-            const float *tp = f.tape + ((int64_t)l * f.n + base + (r < rows ? r : 0)) * 4 * d;
-            for (int j = 0; j < 32; ++j) {
+        // coupling backward: g_o = [g_sraw, g_t] for the b half.  Warp w takes rows w, w+8, ...;
+        // lane j is output column j, so the tape reads of a row are contiguous and the b3
+        // gradient of column j accumulates in lane j's register.
+        {
+            float gsum = 0.f;
+            const int j = lane;
+            for (int r = warp; r < FLOW_ROWS; r += FLOW_THREADS / 32) {
                 float go = 0.f;
                 if (r < rows && j < 2 * d) {
+                    const float *tp = f.tape + ((int64_t)l * f.n + base + r) * 4 * d;
                     const int jj = j < d ? j : j - d;
-                    const int bj = perm[d + jj];
-                    const float gb = s.G[r][bj];
+                    const float gb = s.G[r][perm[d + jj]];
                     const float sj = tp[2 * d + jj];
-                    const float e = __expf(-sj);
                     if (j < d) {
                         const float gs = -gb * tp[d + jj] + f.inv_batch; // d/ds of (b' - t) e^-s, plus the sum(s) term
                         go = gs * (1.f - (sj / FLOW_SMAX) * (sj / FLOW_SMAX));
                     } else {
-                        go = -gb * e;
+                        go = -gb * __expf(-sj);
                     }
                 }
                 s.GO[r * LDO_S + j] = __float2bfloat16_rn(go);
-                atomicAdd(&s.red[2 * FLOW_H + j], go);
+                gsum += go;
             }
+            atomicAdd(&s.red[2 * FLOW_H + j], gsum);
         }
         __syncthreads();
         // b-half gradient passes through: g_b' = g_b e^{-s}
@@ -480,7 +499,7 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
             }
         }
         // g_h2 = (g_o W3^T) * relu'(h2): W3t [H][32] into the W3n buffer with stride LDO_S
-        load_tile(s.W3n, LDO_S, wl + WB_W3T, FLOW_H, 32);
+        load_tile<32>(s.W3n, LDO_S, wl + WB_W3T, FLOW_H);
         __syncthreads();
         {
             float acc[16][4];
@@ -496,8 +515,11 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
                 v[3] = __bfloat162float(s.H2[(r0 + g + 8) * LDH_S + c + 1]) > 0.f ? acc[nt][3] : 0.f;
                 *(uint32_t *)(s.GH2 + (r0 + g) * LDH_S + c) = pack2(__float2bfloat16_rn(v[0]), __float2bfloat16_rn(v[1]));
                 *(uint32_t *)(s.GH2 + (r0 + g + 8) * LDH_S + c) = pack2(__float2bfloat16_rn(v[2]), __float2bfloat16_rn(v[3]));
-                atomicAdd(&s.red[FLOW_H + c], v[0] + v[2]);
-                atomicAdd(&s.red[FLOW_H + c + 1], v[1] + v[3]);
+                const float b0 = sum_over_g(v[0] + v[2]), b1 = sum_over_g(v[1] + v[3]);
+                if (g == 0) {
+                    atomicAdd(&s.red[FLOW_H + c], b0);
+                    atomicAdd(&s.red[FLOW_H + c + 1], b1);
+                }
             }
         }
         __syncthreads();
@@ -509,19 +531,15 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
                 const int c = nt * 8 + 2 * t;
-                if (c < 2 * d) {
-                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g) * 2 * d + c], acc[nt][0]);
-                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g + 8) * 2 * d + c], acc[nt][2]);
-                }
-                if (c + 1 < 2 * d) {
-                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g) * 2 * d + c + 1], acc[nt][1]);
-                    atomicAdd(&GP[pl_W3(d) + (int64_t)(r0 + g + 8) * 2 * d + c + 1], acc[nt][3]);
+                if (c < 2 * d) { // 2d is even, so c + 1 < 2d too
+                    atomic_add2(&GP[pl_W3(d) + (int64_t)(r0 + g) * 2 * d + c], acc[nt][0], acc[nt][1]);
+                    atomic_add2(&GP[pl_W3(d) + (int64_t)(r0 + g + 8) * 2 * d + c], acc[nt][2], acc[nt][3]);
                 }
             }
         }
         // g_h1 = (g_h2 W2^T) * relu'(h1): W2t [H][H] into the W2n buffer
         __syncthreads();
-        load_tile(s.W2n, LDH_S, wl + WB_W2T, FLOW_H, FLOW_H);
+        load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W2T, FLOW_H);
         __syncthreads();
         {
             float acc[16][4];
@@ -537,8 +555,11 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
                 v[3] = __bfloat162float(s.H1[(r0 + g + 8) * LDH_S + c + 1]) > 0.f ? acc[nt][3] : 0.f;
                 *(uint32_t *)(s.GH1 + (r0 + g) * LDH_S + c) = pack2(__float2bfloat16_rn(v[0]), __float2bfloat16_rn(v[1]));
                 *(uint32_t *)(s.GH1 + (r0 + g + 8) * LDH_S + c) = pack2(__float2bfloat16_rn(v[2]), __float2bfloat16_rn(v[3]));
-                atomicAdd(&s.red[c], v[0] + v[2]);
-                atomicAdd(&s.red[c + 1], v[1] + v[3]);
+                const float b0 = sum_over_g(v[0] + v[2]), b1 = sum_over_g(v[1] + v[3]);
+                if (g == 0) {
+                    atomicAdd(&s.red[c], b0);
+                    atomicAdd(&s.red[c + 1], b1);
+                }
             }
         }
         // dW2 = h1^T g_h2: rows h1 (16 per warp) x 128 outputs
@@ -549,15 +570,13 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
 #pragma unroll
             for (int nt = 0; nt < 16; ++nt) {
                 const int c = nt * 8 + 2 * t;
-                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g) * FLOW_H + c], acc[nt][0]);
-                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g) * FLOW_H + c + 1], acc[nt][1]);
-                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g + 8) * FLOW_H + c], acc[nt][2]);
-                atomicAdd(&GP[pl_W2(d) + (int64_t)(r0 + g + 8) * FLOW_H + c + 1], acc[nt][3]);
+                atomic_add2(&GP[pl_W2(d) + (int64_t)(r0 + g) * FLOW_H + c], acc[nt][0], acc[nt][1]);
+                atomic_add2(&GP[pl_W2(d) + (int64_t)(r0 + g + 8) * FLOW_H + c], acc[nt][2], acc[nt][3]);
             }
         }
         __syncthreads();
         // g_a = g_h1 W1^T: W1t [16][H] into the W1n buffer region sized [16][LDH_S] (it fits in W2n)
-        load_tile(s.W2n, LDH_S, wl + WB_W1T, 16, FLOW_H);
+        load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W1T, 16);
         __syncthreads();
         {
             float acc[2][4];
@@ -585,14 +604,8 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
 #pragma unroll
             for (int nt = 0; nt < 16; ++nt) {
                 const int c = nt * 8 + 2 * t;
-                if (g < d) {
-                    atomicAdd(&GP[pl_W1(d) + (int64_t)g * FLOW_H + c], acc[nt][0]);
-                    atomicAdd(&GP[pl_W1(d) + (int64_t)g * FLOW_H + c + 1], acc[nt][1]);
-                }
-                if (g + 8 < d) {
-                    atomicAdd(&GP[pl_W1(d) + (int64_t)(g + 8) * FLOW_H + c], acc[nt][2]);
-                    atomicAdd(&GP[pl_W1(d) + (int64_t)(g + 8) * FLOW_H + c + 1], acc[nt][3]);
-                }
+                if (g < d) { atomic_add2(&GP[pl_W1(d) + (int64_t)g * FLOW_H + c], acc[nt][0], acc[nt][1]); }
+                if (g + 8 < d) { atomic_add2(&GP[pl_W1(d) + (int64_t)(g + 8) * FLOW_H + c], acc[nt][2], acc[nt][3]); }
             }
         }
         __syncthreads();

@@ -27,6 +27,9 @@ UNITS = {
     "sample_fast_all32": [],
     "sample_fast_all32d": [],
     "sample_fast_vec": [],
+    "sample_fast_pk16": [],
+    "sample_fast_pk32": [],
+    "sample_fast_pk32d": [],
     "mcig_noalloc": ["-fmad=false"],
     "mcig_flow": [],
     "sample_batch": [],

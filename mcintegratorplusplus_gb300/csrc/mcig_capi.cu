@@ -868,7 +868,12 @@ static int launch(mcig_mci *h, const KParams &kp)
     size_t smem = (size_t)kp.fblob_len * sizeof(float);
     if (fast) {
         if (!fast_eligible(h) || !small_n) { return set_err(MCIG_ERR_UNSUPPORTED, "configuration not served by the register-resident kernel"); }
-        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim));
+        int pk = 0; // PK_ANY; a single sampling function of a kind with a kernel of its own
+        if (h->pdfs.size() == 1) {
+            const int k = h->pdfs[0].kind;
+            pk = (k == MCIG_PDF_GAUSS || k == MCIG_PDF_GAUSS_SUM) ? 1 : (k == MCIG_PDF_GAUSS_PREC ? 2 : (k == MCIG_PDF_GAUSS_MIX ? 3 : 0));
+        }
+        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk);
         smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
     } else {
         fn = mcig_generic_launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX);

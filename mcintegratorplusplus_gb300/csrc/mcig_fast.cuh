@@ -28,9 +28,66 @@
 // log density of the walker (padded to MAXD coordinates with zeros: padded
 // coordinates never move, and the parameter data is zero-padded, so no loop
 // needs a per-coordinate predicate)
+// pdf sets with a kernel of their own: the one-pdf configurations get straight-line
+// code for their kind (a runtime switch over every kind would be if-converted and
+// issue all of them)
+enum { PK_ANY = 0, PK_GAUSS = 1, PK_PREC = 2, PK_MIX = 3 };
+
 template <int MAXD>
+__device__ __forceinline__ float fast_logp_prec(const FastConst &fc, const float *x)
+{ // -|U x|^2 / 2, U upper triangular at fconst[0], row stride MAXD
+    float q = 0.f;
+#pragma unroll
+    for (int i = 0; i < MAXD; ++i) {
+        float t = 0.f;
+#pragma unroll
+        for (int j = i; j < MAXD; ++j) { t = fmaf(fc.fconst[i * MAXD + j], x[j], t); }
+        q = fmaf(t, t, q);
+    }
+    return -0.5f * q;
+}
+
+template <int MAXD>
+__device__ __forceinline__ float fast_logp_mix(const FastConst &fc, const float *x)
+{ // log sum_c exp(lc_c - |(x - m_c) / s_c|^2 / 2) at fconst[MAXD*MAXD], nc <= 8
+    constexpr int B = MAXD * MAXD;
+    constexpr int S = 1 + 2 * MAXD;
+    const int nc = (int)fc.fconst[B];
+    float e[8];
+    float mx = -INFINITY;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        if (c < nc) {
+            float a = 0.f;
+#pragma unroll
+            for (int i = 0; i < MAXD; ++i) {
+                const float z = (x[i] - fc.fconst[B + 1 + c * S + 1 + i]) * fc.fconst[B + 1 + c * S + 1 + MAXD + i];
+                a = fmaf(z, z, a);
+            }
+            a = fmaf(-0.5f, a, fc.fconst[B + 1 + c * S]);
+            e[c] = a;
+            mx = fmaxf(mx, a);
+        }
+    }
+    float sum = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        if (c < nc) { sum += exp2f((e[c] - mx) * 1.44269504f); }
+    }
+    return mx + 0.69314718f * __log2f(sum);
+}
+
+template <int MAXD, int PK = PK_ANY>
 __device__ __forceinline__ float fast_logp(const KParams &p, const FastConst &fc, const float *x)
 {
+    if constexpr (PK == PK_PREC) { return fast_logp_prec<MAXD>(fc, x); }
+    if constexpr (PK == PK_MIX) { return fast_logp_mix<MAXD>(fc, x); }
+    if constexpr (PK == PK_GAUSS) { // GAUSS and GAUSS_SUM: -x.x
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); }
+        return -s;
+    }
     float lp = 0.f;
     for (int k = 0; k < p.npdf; ++k) {
         const PdfDesc &d = p.pdf[k];
@@ -50,18 +107,7 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const FastConst &fc
             lp -= s;
             break;
         }
-        case MCIG_PDF_GAUSS_PREC: { // -|U x|^2 / 2, U upper triangular at fconst[0], row stride MAXD
-            float q = 0.f;
-#pragma unroll
-            for (int i = 0; i < MAXD; ++i) {
-                float t = 0.f;
-#pragma unroll
-                for (int j = i; j < MAXD; ++j) { t = fmaf(fc.fconst[i * MAXD + j], x[j], t); }
-                q = fmaf(t, t, q);
-            }
-            lp = fmaf(-0.5f, q, lp);
-            break;
-        }
+        case MCIG_PDF_GAUSS_PREC: lp += fast_logp_prec<MAXD>(fc, x); break;
         case MCIG_PDF_GAUSS_BLOCK: {
             float s = 0.f;
 #pragma unroll
@@ -71,34 +117,7 @@ __device__ __forceinline__ float fast_logp(const KParams &p, const FastConst &fc
             lp = fmaf(-(float)d.c, s, lp);
             break;
         }
-        case MCIG_PDF_GAUSS_MIX: { // log sum_c exp(lc_c - |(x - m_c) / s_c|^2 / 2) at fconst[MAXD*MAXD], nc <= 8
-            constexpr int B = MAXD * MAXD;
-            const int nc = (int)fc.fconst[B];
-            float e[8];
-            float mx = -INFINITY;
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                if (c < nc) {
-                    constexpr int S = 1 + 2 * MAXD;
-                    float a = 0.f;
-#pragma unroll
-                    for (int i = 0; i < MAXD; ++i) {
-                        const float z = (x[i] - fc.fconst[B + 1 + c * S + 1 + i]) * fc.fconst[B + 1 + c * S + 1 + MAXD + i];
-                        a = fmaf(z, z, a);
-                    }
-                    a = fmaf(-0.5f, a, fc.fconst[B + 1 + c * S]);
-                    e[c] = a;
-                    mx = fmaxf(mx, a);
-                }
-            }
-            float sum = 0.f;
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                if (c < nc) { sum += exp2f((e[c] - mx) * 1.44269504f); }
-            }
-            lp += mx + 0.69314718f * __log2f(sum);
-            break;
-        }
+        case MCIG_PDF_GAUSS_MIX: lp += fast_logp_mix<MAXD>(fc, x); break;
         default: break;
         }
     }
@@ -131,7 +150,7 @@ template <> struct FastSlot<false> {
     __device__ __forceinline__ static double get(const T &v) { return v; }
 };
 
-template <int MAXD, int MOVE, bool KAHAN>
+template <int MAXD, int MOVE, bool KAHAN, int PK>
 struct FastSampler {
     using Slot = FastSlot<KAHAN>;
     using ST = typename Slot::T;
@@ -218,7 +237,7 @@ struct FastSampler {
                 }
             }
         }
-        const float lpn = fast_logp<MAXD>(p, fc, xn);
+        const float lpn = fast_logp<MAXD, PK>(p, fc, xn);
         const float u = u01_f(block(TAG_ACCEPT, 0).a);
         const bool acc = __log2f(u) <= (lpn - lp) * 1.44269504f;
         if (acc) {
@@ -364,7 +383,7 @@ struct FastSampler {
     // descriptors are constant-bank operands; any further ones loop.
     __device__ void run(int64_t n, bool sample)
     {
-        lp = fast_logp<MAXD>(p, fc, x);
+        lp = fast_logp<MAXD, PK>(p, fc, x);
         for (int j = 0; j < p.nobsdim && sample; ++j) { Slot::zero(slot(j)); }
         const uint32_t n32 = (uint32_t)n;
         uint32_t na = 0;
@@ -397,7 +416,7 @@ struct FastSampler {
         int cons = 0, counter = 0;
         int64_t na = 0;
         while ((p.nfind < 0 && cons < 5) || counter < p.nfind) {
-            lp = fast_logp<MAXD>(p, fc, x);
+            lp = fast_logp<MAXD, PK>(p, fc, x);
             na = 0;
             for (uint32_t r = 0; r < (uint32_t)MIN_STAT; ++r) { na += step() ? 1 : 0; }
             const double rate = (na > 0) ? (double)na / (double)MIN_STAT : 0.;
@@ -442,7 +461,7 @@ struct FastSampler {
 // Up to 16 dimensions the kernel is held to 128 registers per thread: registers are
 // allocated in steps that make 136 or 144 per thread fit only six 64-thread blocks
 // per SM (912 of the 1,024 blocks of 65,536 chains, so a second wave), 128 fits eight.
-template <int MAXD, int MOVE, bool KAHAN>
+template <int MAXD, int MOVE, bool KAHAN, int PK>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -451,17 +470,17 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    FastSampler<MAXD, MOVE, KAHAN> s(p, fc, c, slots);
+    FastSampler<MAXD, MOVE, KAHAN, PK> s(p, fc, c, slots);
     if (p.mode == KMODE_CALIB) { s.calibrate(); }
     else { s.run(p.nsteps, p.mode == KMODE_SAMPLE); }
     s.store_state();
 }
 
-template <int MAXD, int MOVE, bool KAHAN>
+template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY>
 void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, int grid, int block, size_t smem,
                       cudaStream_t st)
 {
-    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN>;
+    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK>;
     // shared memory as large as possible, so the accumulator slots never limit residency
     cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
     if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }

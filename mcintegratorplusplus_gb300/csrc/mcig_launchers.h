@@ -1,5 +1,5 @@
 // mcig_launchers.h -- launch entry points of the sampling kernels, one per
-// translation unit (sample_generic_f64.cu, sample_generic_f32.cu, sample_fast_f32.cu).
+// translation unit (sample_generic_*.cu, sample_fast_*.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include "mcig_common.cuh"
@@ -11,5 +11,6 @@ typedef void (*mcig_launch_fn)(const KParams &p, const FastConst *fc, int movety
 mcig_launch_fn mcig_generic_launcher(int precision, int rng);
 
 // register-resident float kernel (mcig_fast.cuh): move MCIG_MOVE_ALL / MCIG_MOVE_VEC,
-// maxd 4, 8, 16 or 32; NULL otherwise
-mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd);
+// maxd 4, 8, 16 or 32, pdf set pk (PK_ANY, or PK_GAUSS / PK_PREC / PK_MIX for a single
+// sampling function of that kind); NULL otherwise
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk);

@@ -5,6 +5,8 @@
 
 mcig_launch_fn mcig_fast_launcher_all32(int kahan);
 mcig_launch_fn mcig_fast_launcher_vec(int kahan, int maxd);
+mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk);
+mcig_launch_fn mcig_fast_launcher_pk32(int kahan, int pk);
 
 static mcig_launch_fn launcher_all(int kahan, int maxd)
 {
@@ -17,8 +19,12 @@ static mcig_launch_fn launcher_all(int kahan, int maxd)
     }
 }
 
-mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd)
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk)
 {
+    if (move == MCIG_MOVE_ALL && pk != PK_ANY) { // one-pdf kernels where they exist
+        mcig_launch_fn f = maxd == 16 ? mcig_fast_launcher_pk16(kahan, pk) : (maxd == 32 ? mcig_fast_launcher_pk32(kahan, pk) : nullptr);
+        if (f) { return f; }
+    }
     if (move == MCIG_MOVE_ALL) { return launcher_all(kahan, maxd); }
     if (move == MCIG_MOVE_VEC) { return mcig_fast_launcher_vec(kahan, maxd); }
     return nullptr;

@@ -1,0 +1,15 @@
+// Register-resident float sampling kernels for one-pdf configurations, all-coordinate
+// move, up to 16 dimensions: the log density is straight-line code for its kind
+// (mcig_fast.cuh, PK_*), with Kahan float or double block sums.
+#include "mcig_fast.cuh"
+#include "mcig_launchers.h"
+
+mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk)
+{
+    switch (pk) {
+    case PK_GAUSS: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_GAUSS> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_GAUSS>;
+    case PK_PREC: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_PREC> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_PREC>;
+    case PK_MIX: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_MIX> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_MIX>;
+    default: return nullptr;
+    }
+}

@@ -44,8 +44,8 @@ NBLOCKS = 100
 METRIC = "effective samples/s on 1 GB300 at matched std-error: learned/batched vs plain MH"
 # ncu figures of the sampling launch (65,536 chains, 600 steps, 6 blocks of 100, four
 # accumulators): DRAM bytes read + written, and warp instructions per warp-step
-CAPTURE_DRAM_BYTES = 11.6e6 + 2.677e9
-INST_PER_WARP_STEP = 1372.0
+CAPTURE_DRAM_BYTES = 9.58e6 + 2.6767e9
+INST_PER_WARP_STEP = 1146.0
 
 
 def target(seed=2024):
@@ -484,6 +484,36 @@ def run_c5(args):
             "ess_per_s_ratio_flow_over_plain": ratio}
 
 
+def run_c2_parts(args):
+    """Cost of the parts of a C2 step: one sampling launch (65,536 chains x 1,000 steps,
+    fixed step size, no calibration or burn-in) per configuration, from the bare step to the
+    bench's four accumulators.  Under ncu each launch is one configuration, in this order."""
+    import mcintegratorplusplus_gb300 as mcig
+    Sigma, P = target()
+    all4 = [(0, 100), (1, 100), (0, 1), (1, 1)]
+    cases = [("gauss_move_gauss_pdf", mcig.SRRD_GAUSSIAN, "gauss", []),
+             ("uniform_move_gauss_pdf", mcig.SRRD_UNIFORM, "gauss", []),
+             ("gauss_move_precision_pdf", mcig.SRRD_GAUSSIAN, "prec", []),
+             ("+ x.x Block", mcig.SRRD_GAUSSIAN, "prec", [(0, 100)]),
+             ("+ x_i Full", mcig.SRRD_GAUSSIAN, "prec", [(1, 1)]),
+             ("+ x.x, x_i Block and Full (bench)", mcig.SRRD_GAUSSIAN, "prec", all4)]
+    out = []
+    for name, srrd, pdf, obs in cases:
+        m = mcig.MCI(NDIM, args.chains, precision=mcig.PREC_FP32)
+        m.setSeed(1)
+        m.addSamplingFunction(mcig.PDF_GAUSS_PREC, P) if pdf == "prec" else m.addSamplingFunction(mcig.PDF_GAUSS)
+        m.setTrialMove(mcig.MOVE_ALL, srrd)
+        m.setMRT2Step(0.3)
+        m.setNfindMRT2Iterations(0)
+        m.setNdecorrelationSteps(0)
+        m.setFullStorage(32)
+        for kind, bs in obs:
+            m.addObservable(kind, (), bs, 1, False, mcig.EST_UNCORRELATED)
+        m.integrate(1000)
+        out.append({"configuration": name, "sampling_ms": float(m.getLastTimings()["sampling_ms"])})
+    return {"workload": "C2 step parts", "chains": args.chains, "steps": 1000, "parts": out}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -497,7 +527,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned-proposal comparison added to the default line")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "c2_parts"])
     ap.add_argument("--integrals", type=int, default=4096)
     ap.add_argument("--chains4", type=int, default=16384)
     ap.add_argument("--nmc4", type=int, default=65536)
@@ -508,7 +538,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.workload != "c2" and args.impl != "reference":
         if rank == 0:
-            print(json.dumps({"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)), flush=True)
+            print(json.dumps({"c3": run_c3, "c4": run_c4, "c5": run_c5,
+                              "c2_parts": run_c2_parts}[args.workload](args)), flush=True)
         return
     if args.impl == "reference":
         if rank == 0:

@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # unit -> extra flags
 UNITS = {
-    "mcig_capi": ["-fmad=false"],
+    "mcig_capi": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],  # host sums as the device's, unfused
     "sample_generic_f64": ["-fmad=false"],
     "sample_generic_f32": [],
     "sample_generic_f32d": [],

@@ -117,7 +117,7 @@ struct mcig_mci {
     DBuf<uint64_t> ctr;
     DBuf<int64_t> tpos, nacc, nrej, tape_len;
     DBuf<int> status;
-    DBuf<double> params, lbub, stepmax;
+    DBuf<double> params, lbub, stepmax, xstage;
     DBuf<float> fblob;
     DBuf<double> tape;
     int64_t tape_stride = 0;
@@ -127,9 +127,15 @@ struct mcig_mci {
     std::vector<int64_t> obs_nstore;
     DBuf<double> est_avg, est_err, scratch;
     DBuf<uint8_t> active;
-    // results
-    std::vector<double> chain_avg, chain_err;
-    std::vector<int64_t> h_nacc, h_nrej;
+    // results.  After an integrate the per-chain estimates (est_avg/est_err, scaled by
+    // chain_scale) and the counts stay on the device; the host copies are made when
+    // asked for (host_results()).
+    mutable std::vector<double> chain_avg, chain_err;
+    mutable std::vector<int64_t> h_nacc, h_nrej;
+    mutable bool chains_on_device = false, counts_on_device = false;
+    double chain_scale = 1.;
+    DBuf<double> comb;      // combined average[nod], error[nod]
+    double *h_comb = nullptr; // pinned staging of comb
     bool record = false;
     DBuf<uint8_t> bits;
     int64_t bits_steps = 0;
@@ -284,6 +290,9 @@ extern "C" int mcig_destroy(mcig_mci *h)
     h->x.release(); h->step.release(); h->ctr.release(); h->tpos.release(); h->nacc.release(); h->nrej.release();
     h->tape_len.release(); h->status.release(); h->params.release(); h->lbub.release(); h->stepmax.release();
     h->fblob.release(); h->tape.release(); h->est_avg.release(); h->est_err.release(); h->scratch.release();
+    h->comb.release();
+    h->xstage.release();
+    if (h->h_comb) { cudaFreeHost(h->h_comb); h->h_comb = nullptr; }
     h->active.release(); h->bits.release();
     for (auto &b : h->obsdata) { b.release(); }
     for (auto &ev : h->ev) { if (ev) { cudaEventDestroy(ev); } }
@@ -322,11 +331,29 @@ static void apply_domain_host(const mcig_mci *h, double *x)
     }
 }
 
+// rows x[n][ndim] (n == 1: one row for every chain) -> walkers [ndim][nchains]
+static __global__ void rows_to_walkers_kernel(const double *__restrict__ rows, int64_t n, int ndim, int64_t nc, double *x)
+{
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= nc) { return; }
+    const double *src = rows + (n == 1 ? 0 : c * ndim);
+    for (int i = 0; i < ndim; ++i) { x[(size_t)i * nc + c] = src[i]; }
+}
+
 extern "C" int mcig_set_x(mcig_mci *h, const double *x, int64_t n)
 {
     if (!x) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "x is NULL"); }
     if (n != 1 && n != h->nchains) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "set_x: n must be 1 or nchains"); }
     cudaSetDevice(h->device);
+    if (!h->periodic) { // the unbound domain leaves x as it is: copy the rows and transpose on the device
+        int rc;
+        if ((rc = h->xstage.alloc((size_t)n * h->ndim))) { return rc; }
+        CK(cudaMemcpyAsync(h->xstage.p, x, (size_t)n * h->ndim * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        rows_to_walkers_kernel<<<(int)((h->nchains + 255) / 256), 256, 0, h->stream>>>(h->xstage.p, n, h->ndim, h->nchains, h->x.p);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(h->stream)); // the caller may reuse x on return
+        return MCIG_OK;
+    }
     const size_t nc = (size_t)h->nchains;
     std::vector<double> t(nc * h->ndim);
     std::vector<double> v(h->ndim);
@@ -1133,7 +1160,8 @@ static int validate_accumulators(const mcig_mci *h, int64_t nmc)
 
 // estimators of all observables -> per-chain avg/err (host vectors [nchains][nod])
 static int estimate_all(mcig_mci *h, const std::vector<ObsDef> &obs, const std::vector<DBuf<char>> &bufs,
-                        const std::vector<int64_t> &nstore, int full32, std::vector<double> &cavg, std::vector<double> &cerr)
+                        const std::vector<int64_t> &nstore, int full32, std::vector<double> &cavg, std::vector<double> &cerr,
+                        bool to_host = true)
 {
     int nod = 0;
     for (auto &o : obs) { nod += o.nv; }
@@ -1148,6 +1176,7 @@ static int estimate_all(mcig_mci *h, const std::vector<ObsDef> &obs, const std::
         if (rc) { return rc; }
         off += obs[o].nv;
     }
+    if (!to_host) { return MCIG_OK; }
     cavg.resize(nc * nod);
     cerr.resize(nc * nod);
     if (nod > 0) {
@@ -1155,6 +1184,77 @@ static int estimate_all(mcig_mci *h, const std::vector<ObsDef> &obs, const std::
         CK(cudaMemcpyAsync(cerr.data(), h->est_err.p, nc * nod * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     }
     CK(cudaStreamSynchronize(h->stream));
+    return MCIG_OK;
+}
+
+// MPIMCI::integrate reduction (src/MPIMCI.cpp:85-92) of the per-chain estimates, one
+// thread per value summing the chains in order, so the result is the host loop's
+// (this unit is compiled with -fmad=false); scale: volume factor of the no-pdf path
+static __global__ void combine_chains_kernel(const double *__restrict__ avg, const double *__restrict__ err, int64_t nc,
+                                             int nod, int scale, double vol, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nod) { return; }
+    double sa = 0., se = 0.;
+    for (int64_t c = 0; c < nc; ++c) {
+        sa += avg[c * nod + i];
+        se += err[c * nod + i] * err[c * nod + i];
+    }
+    double a = sa / (double)nc, e = sqrt(se) / (double)nc;
+    if (scale) {
+        a *= vol;
+        e *= vol;
+    }
+    out[i] = a;
+    out[nod + i] = e;
+}
+
+// combination of the estimates in est_avg/est_err into average/error (host arrays)
+static int combine_on_device(mcig_mci *h, int nod, double *average, double *error, int scale, double vol)
+{
+    int rc;
+    if ((rc = h->comb.alloc(2 * (size_t)std::max(nod, 1)))) { return rc; }
+    if (!h->h_comb) { CK(cudaMallocHost(&h->h_comb, 2 * MCIG_MAXOBS * (2 * MCIG_MAXDIM + 8) * sizeof(double))); }
+    combine_chains_kernel<<<(nod + 127) / 128, 128, 0, h->stream>>>(h->est_avg.p, h->est_err.p, h->nchains, nod, scale, vol,
+                                                                  h->comb.p);
+    ++h->launches;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_comb, h->comb.p, 2 * (size_t)nod * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    std::copy(h->h_comb, h->h_comb + nod, average);
+    std::copy(h->h_comb + nod, h->h_comb + 2 * nod, error);
+    return MCIG_OK;
+}
+
+// host copies of the last integrate's per-chain estimates and counts, made on demand
+static int host_results(const mcig_mci *h)
+{
+    const size_t nc = (size_t)h->nchains;
+    if (h->counts_on_device) {
+        h->h_nacc.resize(nc);
+        h->h_nrej.resize(nc);
+        CK(cudaSetDevice(h->device));
+        CK(cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        h->counts_on_device = false;
+    }
+    if (h->chains_on_device) {
+        const size_t n = nc * (size_t)nobsdim(h);
+        h->chain_avg.resize(n);
+        h->chain_err.resize(n);
+        CK(cudaSetDevice(h->device));
+        if (n > 0) {
+            CK(cudaMemcpy(h->chain_avg.data(), h->est_avg.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(h->chain_err.data(), h->est_err.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+        if (h->chain_scale != 1.) {
+            for (size_t k = 0; k < n; ++k) {
+                h->chain_avg[k] *= h->chain_scale;
+                h->chain_err[k] *= h->chain_scale;
+            }
+        }
+        h->chains_on_device = false;
+    }
     return MCIG_OK;
 }
 
@@ -1292,7 +1392,9 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
     }
     CK(cudaEventRecord(h->ev[3], h->stream));
     if (nmc > 0) {
-        if ((rc = estimate_all(h, h->obs, h->obsdata, h->obs_nstore, h->full32, h->chain_avg, h->chain_err))) { return rc; }
+        if ((rc = estimate_all(h, h->obs, h->obsdata, h->obs_nstore, h->full32, h->chain_avg, h->chain_err, false))) {
+            return rc;
+        }
     }
     CK(cudaEventRecord(h->ev[4], h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1302,41 +1404,25 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
         cudaEventElapsedTime(&ms, h->ev[k], h->ev[k + 1]);
         h->ms[k] = ms;
     }
-    const size_t nc = (size_t)h->nchains;
-    h->h_nacc.resize(nc);
-    h->h_nrej.resize(nc);
-    CK(cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    h->counts_on_device = true;
     if (nmc > 0) {
-        const int nod = nobsdim(h);
-        // MPIMCI::integrate reduction (src/MPIMCI.cpp:85-92), chains in order
-        for (int i = 0; i < nod; ++i) {
-            double sa = 0., se = 0.;
-            for (size_t c = 0; c < nc; ++c) {
-                sa += h->chain_avg[c * nod + i];
-                se += h->chain_err[c * nod + i] * h->chain_err[c * nod + i];
-            }
-            average[i] = sa / (double)nc;
-            error[i] = std::sqrt(se) / (double)nc;
-        }
-        if (h->pdfs.empty()) { // volume scaling (MCIntegrator.cpp:70-77)
-            double vol = 1.;
+        // volume scaling of the no-pdf path (MCIntegrator.cpp:70-77)
+        double vol = 1.;
+        if (h->pdfs.empty()) {
             for (int i = 0; i < h->ndim; ++i) { vol *= (h->ub[i] - h->lb[i]); }
-            for (int i = 0; i < nod; ++i) {
-                average[i] *= vol;
-                error[i] *= vol;
-            }
-            for (size_t k = 0; k < h->chain_avg.size(); ++k) {
-                h->chain_avg[k] *= vol;
-                h->chain_err[k] *= vol;
-            }
         }
+        h->chain_scale = h->pdfs.empty() ? vol : 1.;
+        h->chains_on_device = true;
+        const int nod = nobsdim(h);
+        if (nod > 0 && (rc = combine_on_device(h, nod, average, error, h->pdfs.empty() ? 1 : 0, vol))) { return rc; }
     }
     return MCIG_OK;
 }
 
 extern "C" int mcig_get_chain_results(const mcig_mci *h, double *chain_avg, double *chain_err)
 {
+    int rc = host_results(h);
+    if (rc) { return rc; }
     if (chain_avg) { std::copy(h->chain_avg.begin(), h->chain_avg.end(), chain_avg); }
     if (chain_err) { std::copy(h->chain_err.begin(), h->chain_err.end(), chain_err); }
     return MCIG_OK;
@@ -1344,6 +1430,8 @@ extern "C" int mcig_get_chain_results(const mcig_mci *h, double *chain_avg, doub
 
 extern "C" int mcig_get_acceptance_rate(const mcig_mci *h, double *rate)
 {
+    int rc = host_results(h);
+    if (rc) { return rc; }
     int64_t a = 0, r = 0;
     for (size_t c = 0; c < h->h_nacc.size(); ++c) {
         a += h->h_nacc[c];
@@ -1355,6 +1443,8 @@ extern "C" int mcig_get_acceptance_rate(const mcig_mci *h, double *rate)
 
 extern "C" int mcig_get_counts(const mcig_mci *h, int64_t *acc, int64_t *rej)
 {
+    int rc = host_results(h);
+    if (rc) { return rc; }
     std::copy(h->h_nacc.begin(), h->h_nacc.end(), acc);
     std::copy(h->h_nrej.begin(), h->h_nrej.end(), rej);
     return MCIG_OK;
@@ -1620,6 +1710,8 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     h->h_nrej.resize(nc);
     CK(cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    h->counts_on_device = h->chains_on_device = false; // the host copies above are current
+    h->chain_scale = 1.;
     const int nod = nobsdim(h);
     for (int i = 0; i < nod; ++i) {
         double sa = 0., se = 0.;
@@ -1887,6 +1979,8 @@ extern "C" int mcig_batch_run(mcig_batch *b, double *avg, double *err)
         h->h_nrej.resize(nc);
         cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost);
         cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost);
+        h->counts_on_device = h->chains_on_device = false; // the host copies above are current
+        h->chain_scale = 1.;
     }
     return MCIG_OK;
 }

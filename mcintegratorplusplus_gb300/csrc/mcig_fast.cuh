@@ -259,35 +259,48 @@ struct FastSampler {
     template <int NV>
     __device__ __forceinline__ void put(const ObsDesc &od, uint32_t k, bool flush, uint32_t blk, const float *v, int nv)
     {
-        const size_t stride = (size_t)p.nchains;
+        // every value is written (predicate-free) when the observable has NV values,
+        // the common case of x and x^2 at ndim == MAXD
+        const bool all = (NV == 1) || (nv == NV);
+        const uint32_t nc = (uint32_t)p.nchains; // value stride; j * nc < 2^32 for any device array
         if (od.acc == MCIG_ACC_FULL) {
             const size_t row = (size_t)p.acc_offset + k;
             if (od.full32) {
-                float *dst = (float *)od.data + row * (size_t)nv * stride + c;
+                float *dst = (float *)od.data + row * (size_t)nv * nc + c;
+                if (all) {
 #pragma unroll
-                for (int j = 0; j < NV; ++j) {
-                    if (NV == 1 || j < nv) { dst[j * stride] = v[j]; }
+                    for (int j = 0; j < NV; ++j) { dst[j * nc] = v[j]; }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NV; ++j) {
+                        if (j < nv) { dst[j * nc] = v[j]; }
+                    }
                 }
             } else {
-                double *dst = (double *)od.data + row * (size_t)nv * stride + c;
+                double *dst = (double *)od.data + row * (size_t)nv * nc + c;
 #pragma unroll
                 for (int j = 0; j < NV; ++j) {
-                    if (NV == 1 || j < nv) { dst[j * stride] = (double)v[j]; }
+                    if (all || j < nv) { dst[j * nc] = (double)v[j]; }
                 }
             }
             return;
         }
         ST *sl = slots + od.voff * MCIG_FAST_BLOCK + threadIdx.x;
+        if (all) {
 #pragma unroll
-        for (int j = 0; j < NV; ++j) {
-            if (NV == 1 || j < nv) { Slot::add(sl[j * MCIG_FAST_BLOCK], v[j]); }
-        }
-        if (od.acc == MCIG_ACC_BLOCK && flush) {
-            double *dst = (double *)od.data + (size_t)blk * nv * stride + c;
+            for (int j = 0; j < NV; ++j) { Slot::add(sl[j * MCIG_FAST_BLOCK], v[j]); }
+        } else {
 #pragma unroll
             for (int j = 0; j < NV; ++j) {
-                if (NV == 1 || j < nv) {
-                    dst[j * stride] = Slot::get(sl[j * MCIG_FAST_BLOCK]) * od.inv_bs;
+                if (j < nv) { Slot::add(sl[j * MCIG_FAST_BLOCK], v[j]); }
+            }
+        }
+        if (od.acc == MCIG_ACC_BLOCK && flush) {
+            double *dst = (double *)od.data + (size_t)blk * nv * nc + c;
+#pragma unroll
+            for (int j = 0; j < NV; ++j) {
+                if (all || j < nv) {
+                    dst[j * nc] = Slot::get(sl[j * MCIG_FAST_BLOCK]) * od.inv_bs;
                     Slot::zero(sl[j * MCIG_FAST_BLOCK]);
                 }
             }

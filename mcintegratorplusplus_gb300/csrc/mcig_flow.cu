@@ -93,49 +93,67 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi)
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
+// four 8x8 bf16 matrices from shared memory in mma fragment order: thread t gives the
+// address of row t % 8 of matrix t / 8 (16-byte aligned rows)
+__device__ __forceinline__ void ldmatrix_x4(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3, const __nv_bfloat16 *p)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+
 // C[16 x 8 NT] += A[rows r0.., K] * B[K, 8 NT]; A row-major (k contiguous, stride lda),
-// B "n-major" (element (k, n) at Bn[n*ldb + k]).
+// B "n-major" (element (k, n) at Bn[n*ldb + k]).  Fragments come from ldmatrix: one x4
+// for the A tile of a k-step, one x4 for the B tiles of two n-tiles.  NT is even.
 template <int KSTEPS, int NT>
 __device__ __forceinline__ void warp_gemm(const __nv_bfloat16 *A, int lda, int r0, const __nv_bfloat16 *Bn, int ldb,
                                           float (&acc)[NT][4])
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int lane = threadIdx.x & 31, mi = lane >> 3, rr = lane & 7;
 #pragma unroll
     for (int ks = 0; ks < KSTEPS; ++ks) {
-        const int k0 = ks * 16 + 2 * t;
-        const uint32_t a0 = ld32(A + (r0 + g) * lda + k0);
-        const uint32_t a1 = ld32(A + (r0 + g + 8) * lda + k0);
-        const uint32_t a2 = ld32(A + (r0 + g) * lda + k0 + 8);
-        const uint32_t a3 = ld32(A + (r0 + g + 8) * lda + k0 + 8);
+        const int kb = ks * 16;
+        uint32_t a0, a1, a2, a3; // matrices: rows 0-7 / 8-15 x k 0-7, then x k 8-15
+        ldmatrix_x4(a0, a1, a2, a3, A + (r0 + (mi & 1) * 8 + rr) * lda + kb + (mi >> 1) * 8);
 #pragma unroll
-        for (int nt = 0; nt < NT; ++nt) {
-            const __nv_bfloat16 *bp = Bn + (nt * 8 + g) * ldb + k0;
-            mma_bf16(acc[nt], a0, a1, a2, a3, ld32(bp), ld32(bp + 8));
+        for (int nt = 0; nt < NT; nt += 2) {
+            uint32_t b0, b1, b2, b3; // matrices: n-tile nt x k 0-7 / 8-15, then n-tile nt + 1
+            ldmatrix_x4(b0, b1, b2, b3, Bn + ((nt + (mi >> 1)) * 8 + rr) * ldb + kb + (mi & 1) * 8);
+            mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+            mma_bf16(acc[nt + 1], a0, a1, a2, a3, b2, b3);
         }
     }
 }
 
+__device__ __forceinline__ void ldmatrix_x4_trans(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3,
+                                                  const __nv_bfloat16 *p)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+
 // C[16 rows (feature r0..) x 8 NT cols] += X^T G over the 128 samples of the tile:
 // A(row = feature i, k = sample) = X[sample][i], B(k = sample, n = j) = G[sample][j];
-// both gathered as bf16 pairs from row-major tiles.
+// both row-major by sample, so their fragments are transposed ldmatrix loads.  NT is even.
 template <int NT>
 __device__ __forceinline__ void warp_gemm_tn(const __nv_bfloat16 *X, int ldx, int r0, const __nv_bfloat16 *Gm, int ldg,
                                              float (&acc)[NT][4])
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int lane = threadIdx.x & 31, mi = lane >> 3, rr = lane & 7;
 #pragma unroll 2
     for (int ks = 0; ks < FLOW_ROWS / 16; ++ks) {
-        const int s0 = ks * 16 + 2 * t;
-        const uint32_t a0 = pack2(X[s0 * ldx + r0 + g], X[(s0 + 1) * ldx + r0 + g]);
-        const uint32_t a1 = pack2(X[s0 * ldx + r0 + g + 8], X[(s0 + 1) * ldx + r0 + g + 8]);
-        const uint32_t a2 = pack2(X[(s0 + 8) * ldx + r0 + g], X[(s0 + 9) * ldx + r0 + g]);
-        const uint32_t a3 = pack2(X[(s0 + 8) * ldx + r0 + g + 8], X[(s0 + 9) * ldx + r0 + g + 8]);
+        const int s0 = ks * 16;
+        uint32_t a0, a1, a2, a3; // (features 0-7 / 8-15) x (samples 0-7), then samples 8-15
+        ldmatrix_x4_trans(a0, a1, a2, a3, X + (s0 + (mi >> 1) * 8 + rr) * ldx + r0 + (mi & 1) * 8);
 #pragma unroll
-        for (int nt = 0; nt < NT; ++nt) {
-            const int n = nt * 8 + g;
-            const uint32_t b0 = pack2(Gm[s0 * ldg + n], Gm[(s0 + 1) * ldg + n]);
-            const uint32_t b1 = pack2(Gm[(s0 + 8) * ldg + n], Gm[(s0 + 9) * ldg + n]);
+        for (int nt = 0; nt < NT; nt += 2) {
+            uint32_t b0, b1, b2, b3; // n-tile nt x samples 0-7 / 8-15, then n-tile nt + 1
+            ldmatrix_x4_trans(b0, b1, b2, b3, Gm + (s0 + (mi & 1) * 8 + rr) * ldg + (nt + (mi >> 1)) * 8);
             mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+            mma_bf16(acc[nt + 1], a0, a1, a2, a3, b2, b3);
         }
     }
 }
@@ -175,10 +193,10 @@ struct FlowSmem {
     __nv_bfloat16 A[FLOW_ROWS * LDA_S];
     __nv_bfloat16 H1[FLOW_ROWS * LDH_S];
     __nv_bfloat16 H2[FLOW_ROWS * LDH_S];
-    __nv_bfloat16 W1n[FLOW_H * LDA_S];
-    __nv_bfloat16 W2n[FLOW_H * LDH_S];
-    __nv_bfloat16 W3n[32 * LDH_S];
-    float bias[2 * FLOW_H + 32];
+    __nv_bfloat16 W1n[2][FLOW_H * LDA_S]; // two buffers: layer l computes while layer l+1 arrives
+    __nv_bfloat16 W2n[2][FLOW_H * LDH_S];
+    __nv_bfloat16 W3n[2][32 * LDH_S];
+    float bias[2][2 * FLOW_H + 32];       // b1, b2, b3 of the layer in weight buffer of the same index
     float logdet[FLOW_ROWS];
 };
 
@@ -262,54 +280,93 @@ __device__ __forceinline__ float sum_over_g(float v)
 // paired float atomic add (address 8-byte aligned)
 __device__ __forceinline__ void atomic_add2(float *a, float x, float y) { atomicAdd((float2 *)a, make_float2(x, y)); }
 
-// the MLP of one layer on the a-half in s.A: s.H1, s.H2 (bf16) and, if want_o, s.O (float)
-__device__ void layer_mlp(FlowSmem &s, const float *P, int d, bool want_o)
+// The MLP of one layer for the 16 rows r0.. of one warp: a-half in s.A -> s.H1, s.H2
+// (bf16) -> s.O (float).  Every tile row belongs to one warp, so the stages need only
+// warp synchronisation; the weights and biases of buffer buf are read-only.
+__device__ __forceinline__ void warp_layer_mlp(FlowSmem &s, int r0, int buf)
 {
-    const int warp = threadIdx.x >> 5, r0 = warp * 16;
-    for (int i = threadIdx.x; i < FLOW_H; i += blockDim.x) {
-        s.bias[i] = P[pl_b1(d) + i];
-        s.bias[FLOW_H + i] = P[pl_b2(d) + i];
-    }
-    for (int i = threadIdx.x; i < 32; i += blockDim.x) { s.bias[2 * FLOW_H + i] = (i < 2 * d) ? P[pl_b3(d) + i] : 0.f; }
-    __syncthreads();
+    const float *bias = s.bias[buf];
     {
         float acc[16][4];
         zero_acc(acc);
-        warp_gemm<1, 16>(s.A, LDA_S, r0, s.W1n, LDA_S, acc);
-        store_act(acc, s.bias, true, s.H1, LDH_S, r0);
+        warp_gemm<1, 16>(s.A, LDA_S, r0, s.W1n[buf], LDA_S, acc);
+        store_act(acc, bias, true, s.H1, LDH_S, r0);
     }
-    __syncthreads();
+    __syncwarp();
     {
         float acc[16][4];
         zero_acc(acc);
-        warp_gemm<FLOW_H / 16, 16>(s.H1, LDH_S, r0, s.W2n, LDH_S, acc);
-        store_act(acc, s.bias + FLOW_H, true, s.H2, LDH_S, r0);
+        warp_gemm<FLOW_H / 16, 16>(s.H1, LDH_S, r0, s.W2n[buf], LDH_S, acc);
+        store_act(acc, bias + FLOW_H, true, s.H2, LDH_S, r0);
     }
-    __syncthreads();
-    if (want_o) {
+    __syncwarp();
+    {
         float acc[4][4];
         zero_acc(acc);
-        warp_gemm<FLOW_H / 16, 4>(s.H2, LDH_S, r0, s.W3n, LDH_S, acc);
+        warp_gemm<FLOW_H / 16, 4>(s.H2, LDH_S, r0, s.W3n[buf], LDH_S, acc);
         const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll
         for (int nt = 0; nt < 4; ++nt) {
             const int c = nt * 8 + 2 * t;
-            s.O[r0 + g][c] = acc[nt][0] + s.bias[2 * FLOW_H + c];
-            s.O[r0 + g][c + 1] = acc[nt][1] + s.bias[2 * FLOW_H + c + 1];
-            s.O[r0 + g + 8][c] = acc[nt][2] + s.bias[2 * FLOW_H + c];
-            s.O[r0 + g + 8][c + 1] = acc[nt][3] + s.bias[2 * FLOW_H + c + 1];
+            s.O[r0 + g][c] = acc[nt][0] + bias[2 * FLOW_H + c];
+            s.O[r0 + g][c + 1] = acc[nt][1] + bias[2 * FLOW_H + c + 1];
+            s.O[r0 + g + 8][c] = acc[nt][2] + bias[2 * FLOW_H + c];
+            s.O[r0 + g + 8][c + 1] = acc[nt][3] + bias[2 * FLOW_H + c + 1];
         }
     }
-    __syncthreads();
+    __syncwarp();
 }
 
-__device__ __forceinline__ void load_layer_weights(FlowSmem &s, const __nv_bfloat16 *wl)
+// 16-byte asynchronous global -> shared copies (cp.async, completion per thread)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
-    load_tile<16>(s.W1n, LDA_S, wl + WB_W1N, FLOW_H);
-    load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W2N, FLOW_H);
-    load_tile<FLOW_H>(s.W3n, LDH_S, wl + WB_W3N, 32);
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int COLS>
+__device__ __forceinline__ void load_tile_async(__nv_bfloat16 *dst, int ld, const __nv_bfloat16 *src, int rows)
+{
+    constexpr int VPR = COLS / 8;
+    const int nv = rows * VPR;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        const int r = i / VPR, c = (i % VPR) * 8;
+        cp_async16(dst + r * ld + c, src + (size_t)i * 8);
+    }
 }
 
+// the generative-direction weights of one layer into weight buffer buf, as one copy group
+__device__ __forceinline__ void load_layer_weights_async(FlowSmem &s, const __nv_bfloat16 *wl, int buf)
+{
+    load_tile_async<16>(s.W1n[buf], LDA_S, wl + WB_W1N, FLOW_H);
+    load_tile_async<FLOW_H>(s.W2n[buf], LDH_S, wl + WB_W2N, FLOW_H);
+    load_tile_async<FLOW_H>(s.W3n[buf], LDH_S, wl + WB_W3N, 32);
+    cp_async_commit();
+}
+
+// S tanh(o / S) with one exponential: tanh|u| = 1 - 2 / (e^{2|u|} + 1), sign restored
+__device__ __forceinline__ float soft_clamp(float o)
+{
+    const float u = fabsf(o) * (2.f / FLOW_SMAX);
+    const float th = 1.f - __fdividef(2.f, __expf(u) + 1.f);
+    return copysignf(FLOW_SMAX * th, o);
+}
+
+// sum over the 32 lanes of a warp
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) { v += __shfl_xor_sync(0xffffffffu, v, m); }
+    return v;
+}
+
+// Each warp owns 16 rows of the tile through all layers (load, MLP, coupling, output),
+// so within a layer it only synchronises with itself; one block barrier per layer
+// publishes the layer's weights (prefetched with cp.async during the previous layer)
+// and frees the other weight buffer for the next prefetch.
 __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -317,69 +374,90 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
     const int base = blockIdx.x * FLOW_ROWS;
     const int D = f.D, d = f.d;
     const int rows = min(FLOW_ROWS, f.n - base);
-    // load the tile (rows beyond n are zero)
-    for (int i = threadIdx.x; i < FLOW_ROWS * D; i += blockDim.x) {
-        const int r = i / D, c = i % D;
-        float v = (r < rows) ? f.in[(int64_t)(base + r) * D + c] : 0.f;
-        if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); } // density: undo the base affine first
-        s.Y[r][c] = v;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, r0 = warp * 16;
+    const float invd = 1.f / (float)d;
+    // the warp's rows of the tile (rows beyond n are zero)
+    for (int r = r0; r < r0 + 16; ++r) {
+        if (lane < D) {
+            float v = (r < rows) ? f.in[(int64_t)(base + r) * D + lane] : 0.f;
+            if (f.dir == 1) { v = (v - f.mu[lane]) * __expf(-f.logsig[lane]); } // density: undo the base affine first
+            s.Y[r][lane] = v;
+        }
     }
-    for (int i = threadIdx.x; i < FLOW_ROWS; i += blockDim.x) { s.logdet[i] = 0.f; }
-    __syncthreads();
+    if (lane < 16) { s.logdet[r0 + lane] = 0.f; }
+    auto layer_of = [&](int step) { return (f.dir == 0) ? step : f.L - 1 - step; };
+    load_layer_weights_async(s, f.wb + (int64_t)layer_of(0) * f.wstride, 0);
     for (int step = 0; step < f.L; ++step) {
-        const int l = (f.dir == 0) ? step : f.L - 1 - step;
+        const int l = layer_of(step);
+        const int buf = step & 1;
         const int *perm = f.perm + l * D;
-        load_layer_weights(s, f.wb + (int64_t)l * f.wstride);
-        // a-half as bf16 (columns d..15 zero)
-        for (int i = threadIdx.x; i < FLOW_ROWS * 16; i += blockDim.x) {
-            const int r = i / 16, c = i % 16;
-            s.A[r * LDA_S + c] = __float2bfloat16_rn(c < d ? s.Y[r][perm[c]] : 0.f);
+        const float *P = f.theta + (int64_t)l * f.pstride;
+        // biases of this layer into bias buffer buf (last read in layer step - 2)
+        for (int i = threadIdx.x; i < 2 * FLOW_H + 32; i += blockDim.x) {
+            float v = 0.f;
+            if (i < FLOW_H) { v = P[pl_b1(d) + i]; }
+            else if (i < 2 * FLOW_H) { v = P[pl_b2(d) + i - FLOW_H]; }
+            else if (i - 2 * FLOW_H < 2 * d) { v = P[pl_b3(d) + i - 2 * FLOW_H]; }
+            s.bias[buf][i] = v;
         }
-        __syncthreads();
-        layer_mlp(s, f.theta + (int64_t)l * f.pstride, d, true);
-        // coupling, one thread per sample
-        for (int r = threadIdx.x; r < FLOW_ROWS; r += blockDim.x) {
+        cp_async_wait<0>(); // this layer's weights (issued during the previous layer) have arrived
+        __syncthreads();    // ... for every thread; and every warp has left the previous layer
+        if (step + 1 < f.L) { load_layer_weights_async(s, f.wb + (int64_t)layer_of(step + 1) * f.wstride, buf ^ 1); }
+        // a-half of the warp's rows as bf16 (columns d..15 zero)
+        {
+            const int pa = (lane & 15) < d ? perm[lane & 15] : 0;
+            for (int r = r0 + (lane >> 4); r < r0 + 16; r += 2) {
+                const int c = lane & 15;
+                s.A[r * LDA_S + c] = __float2bfloat16_rn(c < d ? s.Y[r][pa] : 0.f);
+            }
+        }
+        __syncwarp();
+        warp_layer_mlp(s, r0, buf);
+        // coupling of the warp's 16 rows x d columns, (row, column) pairs spread over the lanes
+        for (int i = lane; i < 16 * d; i += 32) {
+            const int q = (int)(((float)i + 0.5f) * invd);
+            const int r = r0 + q, j = i - q * d;
+            const float sj = soft_clamp(s.O[r][j]);
+            const float tj = s.O[r][d + j];
+            const int pb = perm[d + j];
+            const float bin = s.Y[r][pb];
+            const float bout = (f.dir == 0) ? fmaf(bin, __expf(sj), tj) : (bin - tj) * __expf(-sj);
+            if (f.tape && r < rows) {
+                float *tp = f.tape + ((int64_t)l * f.n + base + r) * 4 * d;
+                tp[j] = s.Y[r][perm[j]];  // a
+                tp[d + j] = bout;         // b (density direction: the layer's output half)
+                tp[2 * d + j] = sj;
+                tp[3 * d + j] = tj;
+            }
+            s.Y[r][pb] = bout;
+            s.O[r][j] = sj; // kept for the row's log-determinant below
+        }
+        __syncwarp();
+        if (lane < 16) {
             float ld = 0.f;
-            for (int j = 0; j < d; ++j) {
-                const float sj = FLOW_SMAX * tanhf(s.O[r][j] / FLOW_SMAX);
-                const float tj = s.O[r][d + j];
-                const int bj = perm[d + j];
-                const float bin = s.Y[r][bj];
-                float bout;
-                if (f.dir == 0) { bout = bin * __expf(sj) + tj; }
-                else { bout = (bin - tj) * __expf(-sj); }
-                if (f.tape && r < rows) {
-                    float *tp = f.tape + ((int64_t)l * f.n + base + r) * 4 * d;
-                    tp[j] = s.Y[r][perm[j]];  // a
-                    tp[d + j] = bout;         // b (density direction: the layer's output half)
-                    tp[2 * d + j] = sj;
-                    tp[3 * d + j] = tj;
-                }
-                s.Y[r][bj] = bout;
-                ld += sj;
-            }
-            s.logdet[r] += ld;
+            for (int j = 0; j < d; ++j) { ld += s.O[r0 + lane][j]; }
+            s.logdet[r0 + lane] += ld;
         }
-        __syncthreads();
+        __syncwarp();
     }
-    // output and log q
-    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-        float zz = 0.f, ls = 0.f;
-        for (int c = 0; c < D; ++c) { ls += f.logsig[c]; }
-        if (f.dir == 0) { // z was the input
-            for (int c = 0; c < D; ++c) {
-                const float z = f.in[(int64_t)(base + r) * D + c];
-                zz += z * z;
-                f.out[(int64_t)(base + r) * D + c] = f.mu[c] + __expf(f.logsig[c]) * s.Y[r][c];
-            }
-        } else {
-            for (int c = 0; c < D; ++c) {
-                const float z = s.Y[r][c];
-                zz += z * z;
-                f.out[(int64_t)(base + r) * D + c] = z;
+    // output and log q of the warp's rows
+    float ls = 0.f;
+    for (int c = 0; c < D; ++c) { ls += f.logsig[c]; }
+    for (int r = r0; r < min(r0 + 16, rows); ++r) {
+        float zz = 0.f;
+        if (lane < D) {
+            if (f.dir == 0) { // z was the input
+                const float z = f.in[(int64_t)(base + r) * D + lane];
+                zz = z * z;
+                f.out[(int64_t)(base + r) * D + lane] = f.mu[lane] + __expf(f.logsig[lane]) * s.Y[r][lane];
+            } else {
+                const float z = s.Y[r][lane];
+                zz = z * z;
+                f.out[(int64_t)(base + r) * D + lane] = z;
             }
         }
-        f.logq[base + r] = -0.5f * zz - 0.91893853320467274f * D - s.logdet[r] - ls;
+        zz = warp_sum(zz);
+        if (lane == 0) { f.logq[base + r] = -0.5f * zz - 0.91893853320467274f * D - s.logdet[r] - ls; }
     }
 }
 
@@ -424,9 +502,9 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
     const int rows = min(FLOW_ROWS, f.n - base);
     const int warp = threadIdx.x >> 5, r0 = warp * 16;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    for (int i = threadIdx.x; i < FLOW_ROWS * D; i += blockDim.x) {
-        const int r = i / D, c = i % D;
-        s.G[r][c] = (r < rows) ? f.z[(int64_t)(base + r) * D + c] * f.inv_batch : 0.f; // d(0.5|z|^2)/dz / B
+    constexpr int NW = FLOW_THREADS / 32;
+    for (int r = warp; r < FLOW_ROWS; r += NW) { // d(0.5|z|^2)/dz / B
+        if (lane < D) { s.G[r][lane] = (r < rows) ? f.z[(int64_t)(base + r) * D + lane] * f.inv_batch : 0.f; }
     }
     __syncthreads();
     for (int l = 0; l < f.L; ++l) { // reverse of the density direction
@@ -490,12 +568,11 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
             atomicAdd(&s.red[2 * FLOW_H + j], gsum);
         }
         __syncthreads();
-        // b-half gradient passes through: g_b' = g_b e^{-s}
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const float *tp = f.tape + ((int64_t)l * f.n + base + r) * 4 * d;
-            for (int j = 0; j < d; ++j) {
-                const int bj = perm[d + j];
-                s.G[r][bj] = s.G[r][bj] * __expf(-tp[2 * d + j]);
+        // b-half gradient passes through: g_b' = g_b e^{-s} (warp per row, lane j)
+        for (int r = warp; r < rows; r += NW) {
+            if (lane < d) {
+                const int bj = perm[d + lane];
+                s.G[r][bj] = s.G[r][bj] * __expf(-f.tape[((int64_t)l * f.n + base + r) * 4 * d + 2 * d + lane]);
             }
         }
         // g_h2 = (g_o W3^T) * relu'(h2): W3t [H][32] into the W3n buffer with stride LDO_S
@@ -616,18 +693,28 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
         for (int i = threadIdx.x; i < 2 * d; i += blockDim.x) { atomicAdd(&GP[pl_b3(d) + i], s.red[2 * FLOW_H + i]); }
         __syncthreads();
     }
-    // base affine: y_L = (x - mu) exp(-logsig)
+    // base affine: y_L = (x - mu) exp(-logsig); warp per row, lane c, sums in registers
     float *gmu = f.grad + f.base_off, *gls = f.grad + f.base_off + D;
-    for (int c = threadIdx.x; c < D; c += blockDim.x) {
-        float a = 0.f, b = 0.f;
-        for (int r = 0; r < rows; ++r) {
-            const float e = __expf(-f.logsig[c]);
-            const float yl = (f.x[(int64_t)(base + r) * D + c] - f.mu[c]) * e;
-            a += -s.G[r][c] * e;
-            b += -s.G[r][c] * yl;
+    float a = 0.f, b = 0.f;
+    if (lane < D) {
+        const float e = __expf(-f.logsig[lane]);
+        for (int r = warp; r < rows; r += NW) {
+            const float yl = (f.x[(int64_t)(base + r) * D + lane] - f.mu[lane]) * e;
+            a += -s.G[r][lane] * e;
+            b += -s.G[r][lane] * yl;
         }
-        atomicAdd(&gmu[c], a);
-        atomicAdd(&gls[c], b + (blockIdx.x == 0 ? 1.f : 0.f));
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * FLOW_MAXD) { s.red[threadIdx.x] = 0.f; }
+    __syncthreads();
+    if (lane < D) {
+        atomicAdd(&s.red[lane], a);
+        atomicAdd(&s.red[FLOW_MAXD + lane], b);
+    }
+    __syncthreads();
+    if (threadIdx.x < D) {
+        atomicAdd(&gmu[threadIdx.x], s.red[threadIdx.x]);
+        atomicAdd(&gls[threadIdx.x], s.red[FLOW_MAXD + threadIdx.x] + (blockIdx.x == 0 ? 1.f : 0.f));
     }
 }
 

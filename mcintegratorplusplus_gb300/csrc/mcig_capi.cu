@@ -1511,6 +1511,8 @@ int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, f
                           cudaStream_t st);
 int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int steps, int batch, double lr, float *last_loss,
                            cudaStream_t st);
+int mcig_flow_pass_device_cm(mcig_flow *f, int dir, const float *d_in, const double *in_cm, int64_t nstride, int64_t n,
+                             float *out_cm, float *d_logq, cudaStream_t st);
 int mcig_flow_dim(const mcig_flow *f);
 
 enum { TAG_FLOW_Z = 3, TAG_FLOW_ACCEPT = 4 };
@@ -1550,9 +1552,9 @@ __global__ void flow_accept_kernel(KParams p, const float *xprop, const float *l
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     float x[MCIG_MAXDIM], xp[MCIG_MAXDIM];
-    for (int i = 0; i < p.ndim; ++i) {
+    for (int i = 0; i < p.ndim; ++i) { // both chain-minor
         x[i] = (float)p.x[(size_t)i * p.nchains + c];
-        xp[i] = xprop[(size_t)c * p.ndim + i];
+        xp[i] = xprop[(size_t)i * p.nchains + c];
     }
     float dl = lq_cur[c] - lq_prop[c];
     for (int k = 0; k < p.npdf; ++k) { dl += pdf_logp_f(p, p.pdf[k], xp, p.fblob) - pdf_logp_f(p, p.pdf[k], x, p.fblob); }
@@ -1632,16 +1634,18 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
         sp.obs[o].nstore = h->obs_nstore[o];
     }
     uint64_t cycle = 0;
-    // one independence proposal for every chain; krow = Full row to record, -1 none.
-    // Leaves the chain positions (before the move) as rows in xf.
+    // one independence proposal for every chain; krow = Full row to record, -1 none
     auto flow_cycle = [&](int64_t krow) -> int {
-        walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
-        int r;
-        if ((r = mcig_flow_pass_device(f, 1, xf.p, (int64_t)nc, z.p, lq_cur.p, nullptr, h->stream))) { return r; }
+        int r; // log q of the current walkers (read chain-minor), proposal x' = f(z) (written chain-minor)
+        if ((r = mcig_flow_pass_device_cm(f, 1, nullptr, h->x.p, (int64_t)nc, (int64_t)nc, nullptr, lq_cur.p, h->stream))) {
+            return r;
+        }
         flow_z_kernel<<<tg, tb, 0, h->stream>>>(sp, cycle, z.p);
-        if ((r = mcig_flow_pass_device(f, 0, z.p, (int64_t)nc, xprop.p, lq_prop.p, nullptr, h->stream))) { return r; }
+        if ((r = mcig_flow_pass_device_cm(f, 0, z.p, nullptr, (int64_t)nc, (int64_t)nc, xprop.p, lq_prop.p, h->stream))) {
+            return r;
+        }
         flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p);
-        h->launches += 5;
+        h->launches += 4;
         CK(cudaGetLastError());
         ++cycle;
         return MCIG_OK;
@@ -1685,8 +1689,9 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
         }
         if (step >= next_refresh && step < nmc) {
             if (train_steps > 0 && batch > 0) {
+                walkers_to_rows_kernel<<<tg, tb, 0, h->stream>>>(h->x.p, D, (int)nc, xf.p);
                 if ((rc = mcig_flow_train_device(f, xf.p, (int64_t)nc, 1, batch, lr, nullptr, h->stream))) { return rc; }
-                h->launches += 5;
+                h->launches += 6;
             }
             next_refresh += refresh;
         }

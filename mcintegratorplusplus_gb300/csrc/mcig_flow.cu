@@ -72,6 +72,11 @@ struct FlowArgs {
     const float *theta;       // float master parameters
     int64_t wstride;          // bf16 elements per layer in wb
     int64_t pstride;          // floats per layer in theta
+    // chain-minor alternatives: input in_cm[c * cm_stride + row] (double, replaces in) and
+    // output out_cm[c * cm_stride + row] (float, besides or instead of out)
+    const double *in_cm;
+    float *out_cm;
+    int64_t cm_stride;
 };
 
 // ------------------------------------------------------------------------
@@ -376,12 +381,21 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
     const int rows = min(FLOW_ROWS, f.n - base);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, r0 = warp * 16;
     const float invd = 1.f / (float)d;
-    // the warp's rows of the tile (rows beyond n are zero)
-    for (int r = r0; r < r0 + 16; ++r) {
-        if (lane < D) {
-            float v = (r < rows) ? f.in[(int64_t)(base + r) * D + lane] : 0.f;
-            if (f.dir == 1) { v = (v - f.mu[lane]) * __expf(-f.logsig[lane]); } // density: undo the base affine first
-            s.Y[r][lane] = v;
+    if (f.in_cm) { // chain-minor walkers: coalesced over the rows, one coordinate at a time
+        for (int i = threadIdx.x; i < D * FLOW_ROWS; i += blockDim.x) {
+            const int c = i / FLOW_ROWS, r = i % FLOW_ROWS;
+            float v = (r < rows) ? (float)f.in_cm[(int64_t)c * f.cm_stride + base + r] : 0.f;
+            if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); }
+            s.Y[r][c] = v;
+        }
+        __syncthreads();
+    } else { // the warp's rows of the tile (rows beyond n are zero)
+        for (int r = r0; r < r0 + 16; ++r) {
+            if (lane < D) {
+                float v = (r < rows) ? f.in[(int64_t)(base + r) * D + lane] : 0.f;
+                if (f.dir == 1) { v = (v - f.mu[lane]) * __expf(-f.logsig[lane]); } // density: undo the base affine first
+                s.Y[r][lane] = v;
+            }
         }
     }
     if (lane < 16) { s.logdet[r0 + lane] = 0.f; }
@@ -446,18 +460,27 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
     for (int r = r0; r < min(r0 + 16, rows); ++r) {
         float zz = 0.f;
         if (lane < D) {
+            float z, o;
             if (f.dir == 0) { // z was the input
-                const float z = f.in[(int64_t)(base + r) * D + lane];
-                zz = z * z;
-                f.out[(int64_t)(base + r) * D + lane] = f.mu[lane] + __expf(f.logsig[lane]) * s.Y[r][lane];
+                z = f.in_cm ? (float)f.in_cm[(int64_t)lane * f.cm_stride + base + r] : f.in[(int64_t)(base + r) * D + lane];
+                o = f.mu[lane] + __expf(f.logsig[lane]) * s.Y[r][lane];
             } else {
-                const float z = s.Y[r][lane];
-                zz = z * z;
-                f.out[(int64_t)(base + r) * D + lane] = z;
+                z = s.Y[r][lane];
+                o = z;
             }
+            zz = z * z;
+            if (f.out) { f.out[(int64_t)(base + r) * D + lane] = o; }
+            if (f.out_cm) { s.Y[r][lane] = o; } // stored chain-minor below
         }
         zz = warp_sum(zz);
         if (lane == 0) { f.logq[base + r] = -0.5f * zz - 0.91893853320467274f * D - s.logdet[r] - ls; }
+    }
+    if (f.out_cm) { // coalesced over the rows, one coordinate at a time
+        __syncthreads();
+        for (int i = threadIdx.x; i < D * FLOW_ROWS; i += blockDim.x) {
+            const int c = i / FLOW_ROWS, r = i % FLOW_ROWS;
+            if (r < rows) { f.out_cm[(int64_t)c * f.cm_stride + base + r] = s.Y[r][c]; }
+        }
     }
 }
 
@@ -910,10 +933,34 @@ extern "C" int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n)
 }
 
 // one pass over device arrays (in [n][D] float -> out, logq); tape optional
+static int flow_pass_launch(mcig_flow *f, FlowArgs &a, int64_t n, cudaStream_t st)
+{
+    const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
+    flow_pass_kernel<<<grid, FLOW_THREADS, sizeof(FlowSmem), st>>>(a);
+    FCK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+// one pass with chain-minor walkers: input in_cm (double, NULL: rows d_in) and output
+// out_cm (float, NULL: none), both with stride nstride; log q into d_logq
+int mcig_flow_pass_device_cm(mcig_flow *f, int dir, const float *d_in, const double *in_cm, int64_t nstride, int64_t n,
+                             float *out_cm, float *d_logq, cudaStream_t st)
+{
+    FlowArgs a;
+    a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = dir;
+    a.in = d_in; a.out = nullptr; a.logq = d_logq;
+    a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
+    a.perm = f->perm; a.tape = nullptr; a.wb = f->wb; a.theta = f->theta;
+    a.wstride = WB_LAYER; a.pstride = f->pstride;
+    a.in_cm = in_cm; a.out_cm = out_cm; a.cm_stride = nstride;
+    return flow_pass_launch(f, a, n, st);
+}
+
 int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, float *d_out, float *d_logq, float *d_tape,
                           cudaStream_t st)
 {
     FlowArgs a;
+    a.in_cm = nullptr; a.out_cm = nullptr; a.cm_stride = 0;
     a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = dir;
     a.in = d_in; a.out = d_out; a.logq = d_logq;
     a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;

@@ -296,17 +296,22 @@ def _timed_device_ms(tm):
 def run_c3(args):
     """4,096 uneven integrals in one batch (persistent launch per ndim bucket, CUDA graph).
 
-    Integral i: ndim ~ U{1..64}, NMC_i = 2^U(14,20) samples split over 16 chains, target a
-    product of 2-4 isotropic Gaussians on contiguous coordinate blocks (widths log-uniform on
-    [0.3, 3]), MultiStepMove of 4 single-coordinate sub-moves on the same factors, x.x per
-    block in a BlockAccumulator (16 blocks per chain).  Metric: integrals/s."""
+    Integral i: ndim ~ U{1..64}, NMC_i = 2^U(14,20) samples, target a product of 2-4
+    isotropic Gaussians on contiguous coordinate blocks (widths log-uniform on [0.3, 3]),
+    MultiStepMove of 4 single-coordinate sub-moves on the same factors, x.x per block in a
+    BlockAccumulator (16 blocks per chain).  The samples of an integral are split over
+    NMC_i / 4,096 chains (at least 4) of 4,096 steps, combined as MPIMCI combines ranks, so
+    every work unit of the persistent launch has the same length and the ~250,000 units fill
+    the GPU.  Metric: integrals/s."""
     import mcintegratorplusplus_gb300 as mcig
-    n, nch = args.integrals, 16
+    n, steps = args.integrals, 4096
     rng = np.random.default_rng(33)
     mcis, exact, nmcs = [], [], []
+    chains = []
     for i in range(n):
         ndim = int(rng.integers(1, 65))
-        nmc = int(2 ** rng.uniform(14, 20)) // nch // 16 * 16
+        nch = max(4, int(round(2 ** rng.uniform(14, 20) / steps)))
+        nmc = steps
         nb = int(min(ndim, rng.integers(2, 5)))
         cuts = np.sort(rng.choice(np.arange(1, ndim), nb - 1, replace=False)) if nb > 1 else np.array([], int)
         bounds = [0] + [int(c) for c in cuts] + [ndim]
@@ -326,6 +331,7 @@ def run_c3(args):
         mcis.append(m)
         exact.append(np.array([(bounds[k + 1] - bounds[k]) * widths[k] ** 2 for k in range(nb)]))
         nmcs.append(nmc)
+        chains.append(nch)
     b = mcig.Batch(mcis, nmcs)
     blocks = b.autotune(None)
     for _ in range(args.warmup):
@@ -340,13 +346,14 @@ def run_c3(args):
         ms.append(b.last_ms())
     ck = clocks.stop()
     z = np.concatenate([np.abs(a - x) / np.maximum(e, 1e-300) for (a, e), x in zip(res, exact)])
-    outer = float(np.sum(nmcs)) * nch
+    outer = float(np.dot(nmcs, chains))
     t = float(np.mean(ms)) * 1e-3
     return {"metric": "integrals/s (C3: 4,096 uneven integrals, ndim 1-64, MultiStepMove)", "value": n / t,
             "unit": "integrals/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": "C3 uneven batch", "integrals": n, "chains_per_integral": nch,
+            "config": {"workload": "C3 uneven batch", "integrals": n, "steps_per_chain": steps,
+                       "chains_per_integral": "NMC_i / 4096 (min 4): %d..%d, %d in all" % (min(chains), max(chains), sum(chains)),
                        "outer_steps": outer, "sub_moves": 4, "block_sizes": blocks,
                        "l2": "working set (walkers, block sums) below L2; no flush"},
             "outer_steps_per_s": outer / t,

@@ -1187,26 +1187,68 @@ static int estimate_all(mcig_mci *h, const std::vector<ObsDef> &obs, const std::
     return MCIG_OK;
 }
 
-// MPIMCI::integrate reduction (src/MPIMCI.cpp:85-92) of the per-chain estimates, one
-// thread per value summing the chains in order, so the result is the host loop's
-// (this unit is compiled with -fmad=false); scale: volume factor of the no-pdf path
-static __global__ void combine_chains_kernel(const double *__restrict__ avg, const double *__restrict__ err, int64_t nc,
-                                             int nod, int scale, double vol, double *out)
+// MPIMCI::integrate reduction (src/MPIMCI.cpp:85-92) of the per-chain estimates:
+// average = sum(avg) / n, error = sqrt(sum(err^2)) / n, with a fixed summation order
+// (COMB_T partial sums over the chains t, t + COMB_T, ..., then a pairwise tree) that
+// the device kernel and the host function below share, so a batched integral and its
+// own integrate give the same bits (this unit is compiled with -fmad=false and
+// -ffp-contract=off).
+#define COMB_T 256
+
+static void combine_host(const double *avg, const double *err, int64_t stride, int64_t n, double &a, double &e)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nod) { return; }
+    double pa[COMB_T], pe[COMB_T];
+    for (int t = 0; t < COMB_T; ++t) {
+        double sa = 0., se = 0.;
+        for (int64_t c = t; c < n; c += COMB_T) {
+            sa += avg[c * stride];
+            se += err[c * stride] * err[c * stride];
+        }
+        pa[t] = sa;
+        pe[t] = se;
+    }
+    for (int h = COMB_T / 2; h > 0; h >>= 1) {
+        for (int t = 0; t < h; ++t) {
+            pa[t] += pa[t + h];
+            pe[t] += pe[t + h];
+        }
+    }
+    a = pa[0] / (double)n;
+    e = std::sqrt(pe[0]) / (double)n;
+}
+
+// one block of COMB_T threads per value i (stride nod between chains); scale: volume
+// factor of the no-pdf path
+static __global__ void __launch_bounds__(COMB_T) combine_chains_kernel(const double *__restrict__ avg,
+                                                                      const double *__restrict__ err, int64_t nc,
+                                                                      int nod, int scale, double vol, double *out)
+{
+    __shared__ double pa[COMB_T], pe[COMB_T];
+    const int i = blockIdx.x, t = threadIdx.x;
     double sa = 0., se = 0.;
-    for (int64_t c = 0; c < nc; ++c) {
+    for (int64_t c = t; c < nc; c += COMB_T) {
         sa += avg[c * nod + i];
         se += err[c * nod + i] * err[c * nod + i];
     }
-    double a = sa / (double)nc, e = sqrt(se) / (double)nc;
-    if (scale) {
-        a *= vol;
-        e *= vol;
+    pa[t] = sa;
+    pe[t] = se;
+    __syncthreads();
+    for (int h = COMB_T / 2; h > 0; h >>= 1) {
+        if (t < h) {
+            pa[t] += pa[t + h];
+            pe[t] += pe[t + h];
+        }
+        __syncthreads();
     }
-    out[i] = a;
-    out[nod + i] = e;
+    if (t == 0) {
+        double a = pa[0] / (double)nc, e = sqrt(pe[0]) / (double)nc;
+        if (scale) {
+            a *= vol;
+            e *= vol;
+        }
+        out[i] = a;
+        out[nod + i] = e;
+    }
 }
 
 // combination of the estimates in est_avg/est_err into average/error (host arrays)
@@ -1215,8 +1257,7 @@ static int combine_on_device(mcig_mci *h, int nod, double *average, double *erro
     int rc;
     if ((rc = h->comb.alloc(2 * (size_t)std::max(nod, 1)))) { return rc; }
     if (!h->h_comb) { CK(cudaMallocHost(&h->h_comb, 2 * MCIG_MAXOBS * (2 * MCIG_MAXDIM + 8) * sizeof(double))); }
-    combine_chains_kernel<<<(nod + 127) / 128, 128, 0, h->stream>>>(h->est_avg.p, h->est_err.p, h->nchains, nod, scale, vol,
-                                                                  h->comb.p);
+    combine_chains_kernel<<<nod, COMB_T, 0, h->stream>>>(h->est_avg.p, h->est_err.p, h->nchains, nod, scale, vol, h->comb.p);
     ++h->launches;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_comb, h->comb.p, 2 * (size_t)nod * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1718,15 +1759,7 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     h->counts_on_device = h->chains_on_device = false; // the host copies above are current
     h->chain_scale = 1.;
     const int nod = nobsdim(h);
-    for (int i = 0; i < nod; ++i) {
-        double sa = 0., se = 0.;
-        for (size_t c = 0; c < nc; ++c) {
-            sa += h->chain_avg[c * nod + i];
-            se += h->chain_err[c * nod + i] * h->chain_err[c * nod + i];
-        }
-        average[i] = sa / (double)nc;
-        error[i] = std::sqrt(se) / (double)nc;
-    }
+    for (int i = 0; i < nod; ++i) { combine_host(h->chain_avg.data() + i, h->chain_err.data() + i, nod, (int64_t)nc, average[i], error[i]); }
     return MCIG_OK;
 }
 
@@ -1971,13 +2004,10 @@ extern "C" int mcig_batch_run(mcig_batch *b, double *avg, double *err)
         const int nod = nobsdim(h);
         const size_t nc = (size_t)h->nchains;
         for (int i = 0; i < nod; ++i) {
-            double sa = 0., se = 0.;
-            for (size_t c = 0; c < nc; ++c) {
-                sa += h->chain_avg[c * nod + i];
-                se += h->chain_err[c * nod + i] * h->chain_err[c * nod + i];
-            }
-            if (avg) { avg[off + i] = sa / (double)nc; }
-            if (err) { err[off + i] = std::sqrt(se) / (double)nc; }
+            double a, e;
+            combine_host(h->chain_avg.data() + i, h->chain_err.data() + i, nod, (int64_t)nc, a, e);
+            if (avg) { avg[off + i] = a; }
+            if (err) { err[off + i] = e; }
         }
         off += nod;
         h->h_nacc.resize(nc);

@@ -203,6 +203,7 @@ struct FlowSmem {
     __nv_bfloat16 W3n[2][32 * LDH_S];
     float bias[2][2 * FLOW_H + 32];       // b1, b2, b3 of the layer in weight buffer of the same index
     float logdet[FLOW_ROWS];
+    int perm[FLOW_MAXL * FLOW_MAXD];      // coordinate permutations of all layers
 };
 
 // bf16 weight copies per layer (flow_cast_kernel): offsets in elements
@@ -343,13 +344,29 @@ __device__ __forceinline__ void load_tile_async(__nv_bfloat16 *dst, int ld, cons
     }
 }
 
-// the generative-direction weights of one layer into weight buffer buf, as one copy group
-__device__ __forceinline__ void load_layer_weights_async(FlowSmem &s, const __nv_bfloat16 *wl, int buf)
+// the generative-direction weights of one layer and its biases b1, b2 (float, 16-byte
+// aligned in the parameter vector) into buffer buf, as one copy group; b3 (2d floats)
+// is copied with plain loads
+__device__ __forceinline__ void load_layer_weights_async(FlowSmem &s, const __nv_bfloat16 *wl, const float *P, int d, int buf)
 {
     load_tile_async<16>(s.W1n[buf], LDA_S, wl + WB_W1N, FLOW_H);
     load_tile_async<FLOW_H>(s.W2n[buf], LDH_S, wl + WB_W2N, FLOW_H);
     load_tile_async<FLOW_H>(s.W3n[buf], LDH_S, wl + WB_W3N, 32);
+    // a layer's floats start on a 16-byte boundary when d is even (odd d: plain loads)
+    const bool aligned = ((reinterpret_cast<uintptr_t>(P + pl_b1(d)) | reinterpret_cast<uintptr_t>(P + pl_b2(d))) & 15) == 0;
+    if (aligned) {
+        for (int i = threadIdx.x; i < FLOW_H / 4; i += blockDim.x) {
+            cp_async16(s.bias[buf] + 4 * i, P + pl_b1(d) + 4 * i);
+            cp_async16(s.bias[buf] + FLOW_H + 4 * i, P + pl_b2(d) + 4 * i);
+        }
+    } else {
+        for (int i = threadIdx.x; i < FLOW_H; i += blockDim.x) {
+            s.bias[buf][i] = P[pl_b1(d) + i];
+            s.bias[buf][FLOW_H + i] = P[pl_b2(d) + i];
+        }
+    }
     cp_async_commit();
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) { s.bias[buf][2 * FLOW_H + i] = (i < 2 * d) ? P[pl_b3(d) + i] : 0.f; }
 }
 
 // S tanh(o / S) with one exponential: tanh|u| = 1 - 2 / (e^{2|u|} + 1), sign restored
@@ -399,24 +416,19 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
         }
     }
     if (lane < 16) { s.logdet[r0 + lane] = 0.f; }
+    for (int i = threadIdx.x; i < f.L * D; i += blockDim.x) { s.perm[i] = f.perm[i]; }
     auto layer_of = [&](int step) { return (f.dir == 0) ? step : f.L - 1 - step; };
-    load_layer_weights_async(s, f.wb + (int64_t)layer_of(0) * f.wstride, 0);
+    auto params_of = [&](int step) { return f.theta + (int64_t)layer_of(step) * f.pstride; };
+    load_layer_weights_async(s, f.wb + (int64_t)layer_of(0) * f.wstride, params_of(0), d, 0);
     for (int step = 0; step < f.L; ++step) {
         const int l = layer_of(step);
         const int buf = step & 1;
-        const int *perm = f.perm + l * D;
-        const float *P = f.theta + (int64_t)l * f.pstride;
-        // biases of this layer into bias buffer buf (last read in layer step - 2)
-        for (int i = threadIdx.x; i < 2 * FLOW_H + 32; i += blockDim.x) {
-            float v = 0.f;
-            if (i < FLOW_H) { v = P[pl_b1(d) + i]; }
-            else if (i < 2 * FLOW_H) { v = P[pl_b2(d) + i - FLOW_H]; }
-            else if (i - 2 * FLOW_H < 2 * d) { v = P[pl_b3(d) + i - 2 * FLOW_H]; }
-            s.bias[buf][i] = v;
-        }
-        cp_async_wait<0>(); // this layer's weights (issued during the previous layer) have arrived
+        const int *perm = s.perm + l * D;
+        cp_async_wait<0>(); // this layer's weights and biases (issued during the previous layer) have arrived
         __syncthreads();    // ... for every thread; and every warp has left the previous layer
-        if (step + 1 < f.L) { load_layer_weights_async(s, f.wb + (int64_t)layer_of(step + 1) * f.wstride, buf ^ 1); }
+        if (step + 1 < f.L) {
+            load_layer_weights_async(s, f.wb + (int64_t)layer_of(step + 1) * f.wstride, params_of(step + 1), d, buf ^ 1);
+        }
         // a-half of the warp's rows as bf16 (columns d..15 zero)
         {
             const int pa = (lane & 15) < d ? perm[lane & 15] : 0;

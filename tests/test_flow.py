@@ -68,6 +68,26 @@ def test_flow_passes_match_oracle(mcig):
 
 
 @pytest.mark.gpu
+def test_flow_odd_half_dimension_matches_oracle(mcig):
+    """D = 6 (d = 3): layer parameter blocks that do not start on 16-byte boundaries."""
+    Dd, Ld = 6, 3
+    f = mcig.Flow(Dd, Ld, H, seed=3)
+    rng = np.random.default_rng(4)
+    th = (fo.init_params(Dd, Ld, H, 3).astype(np.float64) + rng.standard_normal(fo.nparams(Dd, Ld, H)) * 0.02)
+    f.set_params(th.astype(np.float32))
+    perms = fo.permutations(Dd, Ld, 3)
+    z = rng.standard_normal((200, Dd))
+    x, lq = f.forward(z)
+    xo, lqo = fo.forward(th.astype(np.float32).astype(np.float64), z, Dd, Ld, H, perms, bf16=True)
+    assert np.abs(x - xo).max() < 2e-2 * max(1.0, np.abs(xo).max())
+    assert np.abs(lq - lqo).max() < 5e-2
+    loss, g = f.loss_grad(xo)
+    lo, go = fo.loss_and_grad(th.astype(np.float32).astype(np.float64), xo, Dd, Ld, H, perms, bf16=True)
+    assert abs(loss - lo) < 1e-3 * abs(lo) + 1e-3
+    assert np.linalg.norm(g - go) / np.linalg.norm(go) < 2e-2
+
+
+@pytest.mark.gpu
 def test_flow_gradient_matches_oracle(mcig):
     f = mcig.Flow(D, L, H, seed=11)
     th = random_params(9)

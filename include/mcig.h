@@ -125,6 +125,15 @@ int mcig_reset_domain(mcig_mci *h);
 int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double *error, int do_find_mrt2step,
                    int do_decorrelation);
 int mcig_get_chain_results(const mcig_mci *h, double *chain_avg, double *chain_err);
+/* MCI::storeObservablesOnFile / storeWalkerPositionsOnFile / clear*File
+ * (src/MCIntegrator.cpp:495-542): during the main sampling of the next integrate
+ * calls, every freq-th step of chain 0 is written as the reference writes it
+ * ("<step> v1 v2 ... " and "<step>   x1   x2 ..."), observables as the values of
+ * each accumulator's last accumulation.  The general kernel runs while a file is set. */
+int mcig_store_observables_on_file(mcig_mci *h, const char *path, int freq);
+int mcig_clear_observable_file(mcig_mci *h);
+int mcig_store_walker_positions_on_file(mcig_mci *h, const char *path, int freq);
+int mcig_clear_walker_file(mcig_mci *h);
 /* MCI::getAcceptanceRate (:587-592) of the last sampling run, over all chains */
 int mcig_get_acceptance_rate(const mcig_mci *h, double *rate);
 /* per-chain accepted / rejected counts of the last sampling run */

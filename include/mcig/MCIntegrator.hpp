@@ -58,6 +58,8 @@ inline Observable Constval(double v = 1.3) { return {MCIG_OBS_CONST, {v}}; }
 inline Observable Polynom() { return {MCIG_OBS_POLYNOM, {}}; }
 inline Observable GaussXSquared() { return {MCIG_OBS_GAUSSX2, {}}; }
 inline Observable XI(int i) { return {MCIG_OBS_XI, {double(i)}}; }
+// log of the product of the sampling functions at the walker: an observable that depends on them
+inline Observable LogPDF() { return {MCIG_OBS_LOGPDF, {}}; }
 inline Observable X2Blocks(const std::vector<int> &bounds /* b_0 < ... < b_nb */)
 {
     Observable o{MCIG_OBS_X2BLOCK, {double(bounds.size() - 1)}};
@@ -105,6 +107,11 @@ public:
 
     // --- setters
     void setSeed(uint64_t seed) { detail::check(mcig_set_seed(_h, seed)); }
+    // file output of chain 0 during the main sampling (MCIntegrator.hpp storeObservablesOnFile et al.)
+    void storeObservablesOnFile(const std::string &path, int freq) { detail::check(mcig_store_observables_on_file(_h, path.c_str(), freq)); }
+    void clearObservableFile() { detail::check(mcig_clear_observable_file(_h)); }
+    void storeWalkerPositionsOnFile(const std::string &path, int freq) { detail::check(mcig_store_walker_positions_on_file(_h, path.c_str(), freq)); }
+    void clearWalkerFile() { detail::check(mcig_clear_walker_file(_h)); }
     void setX(int i, double val)
     {
         std::vector<double> x = getXAll();

@@ -77,7 +77,8 @@ enum mcig_pdf_kind {
  */
 enum mcig_obs_kind {
     MCIG_OBS_X2SUM = 0, MCIG_OBS_XND = 1, MCIG_OBS_X2 = 2, MCIG_OBS_X2MEAN = 3,
-    MCIG_OBS_CONST = 4, MCIG_OBS_POLYNOM = 5, MCIG_OBS_X2BLOCK = 6, MCIG_OBS_GAUSSX2 = 7, MCIG_OBS_XI = 8
+    MCIG_OBS_CONST = 4, MCIG_OBS_POLYNOM = 5, MCIG_OBS_X2BLOCK = 6, MCIG_OBS_GAUSSX2 = 7, MCIG_OBS_XI = 8,
+    MCIG_OBS_LOGPDF = 9 /* log of the product of the sampling functions at the walker (depends on them) */
 };
 
 /* arithmetic of the sampling loop on the device */

@@ -61,6 +61,10 @@ SIGNATURES = {
     "mcig_reset_domain": (c_int, [c_void_p]),
     "mcig_integrate": (c_int, [c_void_p, c_int64, P_double, P_double, c_int, c_int]),
     "mcig_get_chain_results": (c_int, [c_void_p, P_double, P_double]),
+    "mcig_store_observables_on_file": (c_int, [c_void_p, ctypes.c_char_p, c_int]),
+    "mcig_clear_observable_file": (c_int, [c_void_p]),
+    "mcig_store_walker_positions_on_file": (c_int, [c_void_p, ctypes.c_char_p, c_int]),
+    "mcig_clear_walker_file": (c_int, [c_void_p]),
     "mcig_get_acceptance_rate": (c_int, [c_void_p, P_double]),
     "mcig_get_counts": (c_int, [c_void_p, P_int64, P_int64]),
     "mcig_get_obs_data": (c_int, [c_void_p, c_int, P_double, P_int64]),

@@ -106,6 +106,11 @@ struct mcig_mci {
     std::vector<ObsDef> obs;
     int periodic = 0;
     std::vector<double> lb, ub;
+    // file output of the main sampling (MCI::storeObservablesOnFile / storeWalkerPositionsOnFile)
+    std::string obs_path, wlk_path;
+    int obs_freq = 0, wlk_freq = 0;
+    DBuf<int64_t> dump_steps;
+    DBuf<double> dump_x, dump_vals;
     double target = 0.5;
     int nfind = -50;
     int64_t ndecorr = -10000;
@@ -194,7 +199,8 @@ static int obs_nvals(int ndim, int kind, const double *params, int np, int *nv)
     case MCIG_OBS_X2SUM:
     case MCIG_OBS_X2MEAN:
     case MCIG_OBS_POLYNOM:
-    case MCIG_OBS_GAUSSX2: *nv = 1; return MCIG_OK;
+    case MCIG_OBS_GAUSSX2:
+    case MCIG_OBS_LOGPDF: *nv = 1; return MCIG_OK;
     case MCIG_OBS_CONST:
         if (np < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "CONST needs its value"); }
         *nv = 1;
@@ -292,6 +298,7 @@ extern "C" int mcig_destroy(mcig_mci *h)
     h->fblob.release(); h->tape.release(); h->est_avg.release(); h->est_err.release(); h->scratch.release();
     h->comb.release();
     h->xstage.release();
+    h->dump_steps.release(); h->dump_x.release(); h->dump_vals.release();
     if (h->h_comb) { cudaFreeHost(h->h_comb); h->h_comb = nullptr; }
     h->active.release(); h->bits.release();
     for (auto &b : h->obsdata) { b.release(); }
@@ -890,7 +897,8 @@ static int launch(mcig_mci *h, const KParams &kp)
     const int block = MCIG_FAST_BLOCK;
     const int grid = (int)((h->nchains + block - 1) / block);
     const bool small_n = kp.nsteps < ((int64_t)1 << 31); // 32-bit step counters in the register-resident kernel
-    const bool fast = h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n);
+    // file output is recorded by the general kernel
+    const bool fast = kp.ndump == 0 && (h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n));
     mcig_launch_fn fn = nullptr;
     size_t smem = (size_t)kp.fblob_len * sizeof(float);
     if (fast) {
@@ -1074,7 +1082,9 @@ extern "C" int mcig_accumulate_walk(int device, int obs_kind, const double *para
     int nv = 0;
     int rc = obs_nvals(ndim, obs_kind, params, nparams, &nv);
     if (rc) { return rc; }
-    if (obs_kind == MCIG_OBS_X2BLOCK || obs_kind == MCIG_OBS_GAUSSX2) { return set_err(MCIG_ERR_UNSUPPORTED, "observable kind not supported on a walk"); }
+    if (obs_kind == MCIG_OBS_X2BLOCK || obs_kind == MCIG_OBS_GAUSSX2 || obs_kind == MCIG_OBS_LOGPDF) {
+        return set_err(MCIG_ERR_UNSUPPORTED, "observable kind not supported on a walk");
+    }
     blocksize = std::max(0, blocksize);
     nskip = std::max(1, nskip);
     if (nsteps < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[AccumulatorInterface::allocate] Provided number of MC steps was < 1 ."); }
@@ -1377,6 +1387,105 @@ static int auto_decorrelation(mcig_mci *h, KParams kp)
     return MCIG_OK;
 }
 
+// ------------------------------------------------------------------------
+// file output (MCIntegrator.cpp:495-542): chain 0, during the main sampling
+// ------------------------------------------------------------------------
+extern "C" int mcig_store_observables_on_file(mcig_mci *h, const char *path, int freq)
+{
+    if (!path || freq < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "file output needs a path and freq >= 1"); }
+    h->obs_path = path;
+    h->obs_freq = freq;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_clear_observable_file(mcig_mci *h)
+{
+    h->obs_path.clear();
+    h->obs_freq = 0;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_store_walker_positions_on_file(mcig_mci *h, const char *path, int freq)
+{
+    if (!path || freq < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "file output needs a path and freq >= 1"); }
+    h->wlk_path = path;
+    h->wlk_freq = freq;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_clear_walker_file(mcig_mci *h)
+{
+    h->wlk_path.clear();
+    h->wlk_freq = 0;
+    return MCIG_OK;
+}
+
+// observable values (reference operation order, double) at every recorded position
+static __global__ void dump_obs_kernel(const KParams p, int64_t ndump, const double *dx, double *vals)
+{
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= ndump) { return; }
+    double v[2 * MCIG_MAXDIM + 8];
+    for (int o = 0; o < p.nobs; ++o) {
+        obs_eval<double>(p, p.obs[o], dx + k * p.ndim, v);
+        for (int j = 0; j < p.obs[o].nv; ++j) { vals[k * p.nobsdim + p.obs[o].voff + j] = v[j]; }
+    }
+}
+
+// the steps whose walker the files need: every freq-th step for the walker file, and for
+// the observable file the last accumulation step of each observable at or before every
+// freq-th step (an accumulator holds the values of its last accumulation, AccumulatorInterface.cpp:99-114)
+static std::vector<int64_t> dump_list(const mcig_mci *h, int64_t nmc)
+{
+    std::vector<int64_t> v;
+    for (int64_t r = 0; r < nmc; ++r) {
+        if (h->wlk_freq > 0 && r % h->wlk_freq == 0) { v.push_back(r); }
+        if (h->obs_freq > 0 && r % h->obs_freq == 0) {
+            for (auto &o : h->obs) { v.push_back(r - r % o.nskip); }
+        }
+    }
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    return v;
+}
+
+static int write_dump_files(mcig_mci *h, int64_t nmc, const std::vector<int64_t> &steps)
+{
+    const size_t nd = steps.size();
+    const int nod = nobsdim(h);
+    std::vector<double> xs(nd * h->ndim), vals(nd * std::max(nod, 1));
+    CK(cudaMemcpy(xs.data(), h->dump_x.p, xs.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (nod > 0) { CK(cudaMemcpy(vals.data(), h->dump_vals.p, nd * nod * sizeof(double), cudaMemcpyDeviceToHost)); }
+    auto index_of = [&](int64_t r) { return (size_t)(std::lower_bound(steps.begin(), steps.end(), r) - steps.begin()); };
+    if (h->wlk_freq > 0) { // MCI::storeWalkerPositions (:533-542)
+        FILE *f = fopen(h->wlk_path.c_str(), "w");
+        if (!f) { return set_err(MCIG_ERR_RUNTIME, "cannot open %s", h->wlk_path.c_str()); }
+        for (int64_t r = 0; r < nmc; r += h->wlk_freq) {
+            const double *x = xs.data() + index_of(r) * h->ndim;
+            fprintf(f, "%lld", (long long)r);
+            for (int j = 0; j < h->ndim; ++j) { fprintf(f, "   %g", x[j]); }
+            fprintf(f, "\n");
+        }
+        fclose(f);
+    }
+    if (h->obs_freq > 0) { // MCI::storeObservables (:509-516), ObservableContainer::printObsValues (:85-93)
+        FILE *f = fopen(h->obs_path.c_str(), "w");
+        if (!f) { return set_err(MCIG_ERR_RUNTIME, "cannot open %s", h->obs_path.c_str()); }
+        for (int64_t r = 0; r < nmc; r += h->obs_freq) {
+            fprintf(f, "%lld", (long long)r);
+            int off = 0;
+            for (auto &o : h->obs) {
+                const double *v = vals.data() + index_of(r - r % o.nskip) * nod + off;
+                for (int j = 0; j < o.nv; ++j) { fprintf(f, " %g", v[j]); }
+                off += o.nv;
+            }
+            fprintf(f, " \n");
+        }
+        fclose(f);
+    }
+    return MCIG_OK;
+}
+
 extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double *error, int do_find, int do_decorr)
 {
     if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
@@ -1395,6 +1504,15 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
     if ((rc = fill_common(h, kp))) { return rc; }
     // device buffers first, so that allocation stays outside the timed phases
     if (nmc > 0 && (rc = alloc_obs_data(h, h->obs, nmc, h->obsdata, h->obs_nstore, h->full32))) { return rc; }
+    std::vector<int64_t> dump;
+    if (nmc > 0 && (h->obs_freq > 0 || h->wlk_freq > 0)) {
+        dump = dump_list(h, nmc);
+        if ((rc = h->dump_steps.alloc(dump.size())) || (rc = h->dump_x.alloc(dump.size() * h->ndim)) ||
+            (rc = h->dump_vals.alloc(dump.size() * std::max(nobsdim(h), 1)))) {
+            return rc;
+        }
+        CK(cudaMemcpyAsync(h->dump_steps.p, dump.data(), dump.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    }
     CK(cudaEventRecord(h->ev[0], h->stream));
     // phase 1: MCI::findMRT2Step (only with a pdf; every move here has step sizes)
     if (!h->pdfs.empty() && do_find && h->nfind != 0) {
@@ -1429,7 +1547,17 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
             s.bits = h->bits.p;
             h->bits_steps = nmc;
         }
+        if (!dump.empty()) {
+            s.dump_steps = h->dump_steps.p;
+            s.ndump = (int64_t)dump.size();
+            s.dump_x = h->dump_x.p;
+        }
         if ((rc = launch(h, s))) { return rc; }
+        if (!dump.empty() && nobsdim(h) > 0) {
+            dump_obs_kernel<<<(int)((dump.size() + 127) / 128), 128, 0, h->stream>>>(s, (int64_t)dump.size(), h->dump_x.p,
+                                                                                  h->dump_vals.p);
+            ++h->launches;
+        }
     }
     CK(cudaEventRecord(h->ev[3], h->stream));
     if (nmc > 0) {
@@ -1446,6 +1574,7 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
         h->ms[k] = ms;
     }
     h->counts_on_device = true;
+    if (!dump.empty() && (rc = write_dump_files(h, nmc, dump))) { return rc; }
     if (nmc > 0) {
         // volume scaling of the no-pdf path (MCIntegrator.cpp:70-77)
         double vol = 1.;
@@ -1613,7 +1742,7 @@ __global__ void flow_accept_kernel(KParams p, const float *xprop, const float *l
     float vals[2 * MCIG_MAXDIM + 8];
     for (int o = 0; o < p.nobs; ++o) {
         const ObsDesc &od = p.obs[o];
-        obs_eval<float>(p, od, x, vals);
+        obs_eval<float>(p, od, x, vals, p.fblob);
         const size_t base = (size_t)krow * od.nv * p.nchains + c;
         for (int j = 0; j < od.nv; ++j) {
             if (od.full32) { ((float *)od.data)[base + (size_t)j * p.nchains] = vals[j]; }

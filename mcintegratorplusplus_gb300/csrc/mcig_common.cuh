@@ -95,6 +95,11 @@ struct KParams {
     uint8_t *bits;          // optional [nsteps][nchains] accept record
     int64_t acc_offset;     // Full accumulators: row of this launch's first accumulation
     const uint8_t *active;  // optional: chains with active[c] == 0 skip this launch
+    // file output (storeObservablesOnFile / storeWalkerPositionsOnFile): chain 0 records
+    // its walker after the steps dump_steps[0..ndump) (ascending) into dump_x[ndump][ndim]
+    const int64_t *dump_steps;
+    int64_t ndump;
+    double *dump_x;
     // random numbers
     uint32_t key0, key1;
     const double *tape;

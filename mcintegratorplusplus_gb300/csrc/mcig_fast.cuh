@@ -334,6 +334,11 @@ struct FastSampler {
             put<1>(od, k, flush, blk, &v, 1);
             break;
         }
+        case MCIG_OBS_LOGPDF: { // the log density the Metropolis test keeps for the walker
+            const float v = lp;
+            put<1>(od, k, flush, blk, &v, 1);
+            break;
+        }
         case MCIG_OBS_XI: {
             const int idx = (int)p.params[od.poff];
             float v = 0.f;

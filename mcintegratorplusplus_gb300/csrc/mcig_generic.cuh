@@ -188,11 +188,38 @@ static __device__ float pdf_logp_f(const KParams &p, const PdfDesc &d, const flo
 // ------------------------------------------------------------------------
 // observables (observableFunction of the test classes; oracle obs_eval)
 // ------------------------------------------------------------------------
+// log of the product of the sampling functions at x: double -sum_k (proto_k summed in
+// index order), as the oracle; float sum_k log p_k (the float path's log densities)
+static __device__ double logpdf_d(const KParams &p, const double *x)
+{
+    double s = 0.;
+    for (int k = 0; k < p.npdf; ++k) {
+        const PdfDesc &d = p.pdf[k];
+        double t = 0.;
+        if (d.kind == MCIG_PDF_GAUSS || d.kind == MCIG_PDF_EXP) {
+            for (int i = 0; i < p.ndim; ++i) { t = t + proto_i_d(d.kind, x[i]); }
+        } else {
+            t = t + pdf_proto_scalar_d(p, d, x);
+        }
+        s = s - t;
+    }
+    return s;
+}
+
 template <class R>
-__device__ void obs_eval(const KParams &p, const ObsDesc &o, const R *x, R *out)
+__device__ void obs_eval(const KParams &p, const ObsDesc &o, const R *x, R *out, const float *blob = nullptr)
 {
     const int nd = p.ndim;
     switch (o.kind) {
+    case MCIG_OBS_LOGPDF: { // a dependent observable: reads the sampling functions
+        if constexpr (std::is_same<R, double>::value) { out[0] = logpdf_d(p, x); }
+        else {
+            float s = 0.f;
+            for (int k = 0; k < p.npdf; ++k) { s += pdf_logp_f(p, p.pdf[k], x, blob ? blob : p.fblob); }
+            out[0] = s;
+        }
+        break;
+    }
     case MCIG_OBS_X2SUM: { // X2Sum (:424-430)
         R s = (R)0;
         for (int i = 0; i < nd; ++i) { s = s + x[i] * x[i]; }
@@ -546,15 +573,20 @@ struct GenericSampler {
         R vals[NV];
         for (int j = 0; j < p.nobsdim; ++j) { sums[j].zero(); }
         int64_t na = 0;
+        int64_t dpos = 0; // next entry of the dump list (chain 0)
         for (int64_t r = 0; r < n; ++r) {
             const bool a = step(movetype);
+            if (c == 0 && dpos < p.ndump && r == p.dump_steps[dpos]) {
+                for (int i = 0; i < p.ndim; ++i) { p.dump_x[dpos * p.ndim + i] = (double)x[i]; }
+                ++dpos;
+            }
             na += a ? 1 : 0;
             if (p.bits) { p.bits[(size_t)r * p.nchains + c] = a ? 1 : 0; }
             for (int o = 0; o < p.nobs; ++o) {
                 const ObsDesc &od = p.obs[o];
                 if (r % od.nskip != 0) { continue; }
                 const int64_t k = r / od.nskip; // accumulation index
-                obs_eval<R>(p, od, x, vals);
+                obs_eval<R>(p, od, x, vals, blob);
                 if (od.acc == MCIG_ACC_FULL) { // FullAccumulator::_accumulate (FullAccumulator.cpp:14-18)
                     const size_t row = (size_t)(p.acc_offset + k);
                     if (od.full32) {

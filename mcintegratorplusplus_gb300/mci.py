@@ -30,7 +30,7 @@ SRRD_UNIFORM, SRRD_GAUSSIAN, SRRD_STUDENT, SRRD_CAUCHY, SRRD_EXPONENTIAL, SRRD_G
     SRRD_LOGNORMAL, SRRD_CHISQ, SRRD_FISHER = range(10)
 EST_NOOP, EST_UNCORRELATED, EST_CORRELATED, EST_FCBLOCKER, EST_MJBLOCKER = range(5)
 PDF_GAUSS_SUM, PDF_GAUSS, PDF_EXP, PDF_GAUSS_PREC, PDF_GAUSS_BLOCK, PDF_GAUSS_MIX = range(6)
-OBS_X2SUM, OBS_XND, OBS_X2, OBS_X2MEAN, OBS_CONST, OBS_POLYNOM, OBS_X2BLOCK, OBS_GAUSSX2, OBS_XI = range(9)
+OBS_X2SUM, OBS_XND, OBS_X2, OBS_X2MEAN, OBS_CONST, OBS_POLYNOM, OBS_X2BLOCK, OBS_GAUSSX2, OBS_XI, OBS_LOGPDF = range(10)
 PREC_FP64, PREC_FP32, PREC_FP32_ACC64 = range(3)
 
 
@@ -278,6 +278,20 @@ class MCI:
         lens = np.ascontiguousarray(np.asarray(lens, dtype=np.int64))
         self._tape = (t, lens)
         _raise(self.L.mcig_set_replay(self._h, _dp(t), t.shape[1], lens.ctypes.data_as(P_int64)))
+
+    def storeObservablesOnFile(self, path, freq):
+        """MCI::storeObservablesOnFile: every freq-th main-sampling step of chain 0."""
+        _raise(self.L.mcig_store_observables_on_file(self._h, str(path).encode(), int(freq)))
+
+    def clearObservableFile(self):
+        _raise(self.L.mcig_clear_observable_file(self._h))
+
+    def storeWalkerPositionsOnFile(self, path, freq):
+        """MCI::storeWalkerPositionsOnFile: every freq-th main-sampling step of chain 0."""
+        _raise(self.L.mcig_store_walker_positions_on_file(self._h, str(path).encode(), int(freq)))
+
+    def clearWalkerFile(self):
+        _raise(self.L.mcig_clear_walker_file(self._h))
 
     def setRecordAccepts(self, on=True):
         _raise(self.L.mcig_set_record_accepts(self._h, int(bool(on))))

@@ -447,6 +447,8 @@ typedef struct {
     int nobs;
     int nparams;
     double *params;
+    const pdfdef *pdf; /* LOGPDF: the sampling functions of the MCI (NULL: none) */
+    const int *npdf;
 } obsdef;
 
 static int obs_init(obsdef *o, int kind, int ndim, const double *params, int nparams)
@@ -463,7 +465,8 @@ static int obs_init(obsdef *o, int kind, int ndim, const double *params, int npa
     case MCIG_OBS_X2SUM:
     case MCIG_OBS_X2MEAN:
     case MCIG_OBS_POLYNOM:
-    case MCIG_OBS_GAUSSX2: o->nobs = 1; break;
+    case MCIG_OBS_GAUSSX2:
+    case MCIG_OBS_LOGPDF: o->nobs = 1; break;
     case MCIG_OBS_CONST:
         if (nparams < 1) { return fail(MCIG_ERR_INVALID_ARGUMENT, "CONST needs its value"); }
         o->nobs = 1;
@@ -502,6 +505,15 @@ static void obs_eval(const obsdef *o, const double *x, double *out)
 {
     const int nd = o->ndim;
     switch (o->kind) {
+    case MCIG_OBS_LOGPDF: { /* log of the product of the sampling functions: -sum_k (sum of proto_k) */
+        double s = 0., pv[256];
+        for (int k = 0; o->pdf && k < *o->npdf; ++k) {
+            pdf_proto(&o->pdf[k], x, pv);
+            s = s - fold_sum(pv, o->pdf[k].nproto);
+        }
+        out[0] = s;
+        break;
+    }
     case MCIG_OBS_X2SUM: { /* X2Sum (:424-430) */
         double s = 0.;
         for (int i = 0; i < nd; ++i) { s = s + x[i] * x[i]; }
@@ -1182,6 +1194,8 @@ int orc_add_observable(orc_mci *h, int kind, const double *params, int nparams, 
     obsentry *e = &h->obs[h->nobs];
     int rc = obs_init(&e->def, kind, h->ndim, params, nparams);
     if (rc) { return rc; }
+    e->def.pdf = h->pdf;
+    e->def.npdf = &h->npdf;
     e->acc_type = (blocksize == 0) ? MCIG_ACC_SIMPLE : (blocksize == 1 ? MCIG_ACC_FULL : MCIG_ACC_BLOCK);
     e->blocksize = blocksize;
     e->nskip = nskip;

@@ -15,7 +15,7 @@ GOLDEN_PATH = os.path.join(HERE, "reference_golden.json")
 
 # enum values of include/mcig_types.h
 PDF_GAUSS_SUM, PDF_GAUSS, PDF_EXP = 0, 1, 2
-OBS_X2SUM, OBS_XND, OBS_X2, OBS_X2MEAN, OBS_CONST, OBS_POLYNOM, OBS_X2BLOCK, OBS_GAUSSX2, OBS_XI = range(9)
+OBS_X2SUM, OBS_XND, OBS_X2, OBS_X2MEAN, OBS_CONST, OBS_POLYNOM, OBS_X2BLOCK, OBS_GAUSSX2, OBS_XI, OBS_LOGPDF = range(10)
 MOVE_ALL, MOVE_VEC, MOVE_MULTISTEP = 0, 1, 2
 SRRD_UNIFORM, SRRD_GAUSSIAN = 0, 1
 EST_NOOP, EST_UNCORRELATED, EST_CORRELATED, EST_FCBLOCKER, EST_MJBLOCKER = range(5)

@@ -1,0 +1,61 @@
+"""Accumulators of the register-resident float kernel against its own Full samples
+(the reference's ut1 check that simple, block and full data agree,
+test/ut1/main.cpp:341-345): on one trajectory, every Block mean is the mean of the
+Full samples of its block and every Simple average the mean of all of them, for
+one-value and vector observables, nskip 1 and 3, ndim at and below the padded width."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def run(mcig, ndim, nskip, prec, kernel):
+    nc, nmc = 256, 960
+    m = mcig.MCI(ndim, nc, precision=prec)
+    m.setSeed(9)
+    m.addSamplingFunction(mcig.PDF_GAUSS)
+    m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+    m.setNdecorrelationSteps(100)
+    m.setKernel(kernel)
+    naccu = 1 + (nmc - 1) // nskip
+    bs = naccu // 8
+    # x.x through all three accumulators, x_i through Full and Block (the value slots of
+    # one integrate are limited to 2 MAXD + 8)
+    m.addObservable(mcig.OBS_X2SUM, (), 1, nskip, False, mcig.EST_UNCORRELATED)   # Full (double here)
+    m.addObservable(mcig.OBS_X2SUM, (), bs, nskip, False, mcig.EST_UNCORRELATED)  # Block
+    m.addObservable(mcig.OBS_X2SUM, (), 0, nskip, False, mcig.EST_NOOP)           # Simple
+    m.addObservable(mcig.OBS_XND, (), 1, nskip, False, mcig.EST_UNCORRELATED)
+    m.addObservable(mcig.OBS_XND, (), bs, nskip, False, mcig.EST_UNCORRELATED)
+    m.integrate(nmc, False, True)
+    out = []
+    for k, nv, has_simple in ((0, 1, True), (3, ndim, False)):
+        full = m.getObsData(k).reshape(nc, naccu, nv)
+        block = m.getObsData(k + 1).reshape(nc, 8, nv)
+        simple = m.getObsData(k + 2).reshape(nc, nv) if has_simple else None
+        out.append((full, block, simple, bs))
+    return out
+
+
+@pytest.mark.parametrize("ndim", [16, 13])
+@pytest.mark.parametrize("nskip", [1, 3])
+def test_fast_kernel_block_and_simple_equal_full_means(ndim, nskip):
+    import mcintegratorplusplus_gb300 as mcig
+    for full, block, simple, bs in run(mcig, ndim, nskip, mcig.PREC_FP32, 2):
+        means = full.reshape(full.shape[0], -1, bs, full.shape[2]).mean(axis=2)
+        # Kahan-compensated float sums against double sums of the same float samples
+        np.testing.assert_allclose(block, means, rtol=2e-6, atol=2e-6)
+        if simple is not None:
+            np.testing.assert_allclose(simple, full.mean(axis=1), rtol=2e-6, atol=2e-6)
+
+
+def test_fast_and_general_kernel_accumulate_alike():
+    """The same float configuration through both kernels: identical Philox draws, so the
+    trajectories agree up to float rounding of the log-density, and the accumulated data
+    of the two kernels agree closely on the (vast) majority of chains."""
+    import mcintegratorplusplus_gb300 as mcig
+    a = run(mcig, 16, 1, mcig.PREC_FP32, 2)
+    b = run(mcig, 16, 1, mcig.PREC_FP32, 1)
+    for (fa, ba, sa, _), (fb, bb, sb, _) in zip(a, b):
+        same = np.all(np.abs(fa - fb) < 1e-4 * (1 + np.abs(fb)), axis=(1, 2))
+        assert same.mean() > 0.9, same.mean()
+        np.testing.assert_allclose(ba[same], bb[same], rtol=1e-4, atol=1e-4)

@@ -109,6 +109,7 @@ def test_replay_obs_data_matches_oracle(mcig):
     ref = orc.OracleMCI(3, 1)
     cases.configure(ref, r, lambda mm, s: mm.set_seeds([s]))
     ref.add_observable(cases.OBS_XND, (), 1, 2)
+    ref.add_observable(cases.OBS_LOGPDF, (), 1, 1)  # depends on the sampling functions
     ref.set_record(True)
     ref.integrate(0, True, True)
     ref.integrate(4096, False, False)
@@ -116,10 +117,11 @@ def test_replay_obs_data_matches_oracle(mcig):
     g = mcig.MCI(3, 1, precision=mcig.PREC_FP64)
     cases.configure(g, r, lambda mm, s: None)
     g.add_observable(cases.OBS_XND, (), 1, 2)
+    g.add_observable(cases.OBS_LOGPDF, (), 1, 1)
     g.setReplay(tape, lens)
     g.integrate(0, True, True)
     g.integrate(4096, False, False)
-    for o in range(3):
+    for o in range(4):
         np.testing.assert_array_equal(g.getObsData(o), ref.obs_data(o))
 
 

@@ -157,3 +157,23 @@ def test_error_behaviour():
         m.add_observable(cases.OBS_X2SUM, (), 0, 1, True, cases.EST_NOOP)
     with pytest.raises(orc.OracleError, match="multiple of passed veclen"):
         m.set_trial_move(cases.MOVE_VEC, 0, 2)
+
+
+def test_oracle_logpdf_observable_is_minus_the_protos():
+    """The log-pdf observable of the oracle (a dependent observable) equals -sum of the
+    Gauss protos x_i^2 of the recorded walker, summed in index order."""
+    from oracle import oracle as orc
+    m = orc.OracleMCI(3, 1)
+    m.set_seeds([11])
+    m.add_sampling_function(1, ())          # Gauss: exp(-sum x_i^2)
+    m.add_observable(1, (), 1, 1)            # x_i, Full
+    m.add_observable(9, (), 1, 1)            # log pdf, Full
+    m.integrate(0, True, True)
+    m.integrate(64, False, False)
+    xs = m.obs_data(0).reshape(64, 3)
+    lp = m.obs_data(1).reshape(64)
+    for x, v in zip(xs, lp):
+        s = 0.
+        for xi in x:
+            s = s + xi * xi
+        assert v == 0. - s

@@ -307,74 +307,67 @@ struct FastSampler {
         }
     }
 
-    // observableFunction of the test classes (oracle obs_eval), in float, then put();
-    // the one-value observables take the one-value path
+    // observableFunction of the test classes (oracle obs_eval), in float, then put():
+    // the one-value kinds share one put<1>, the vector kinds one put<MAXD>
     __device__ __forceinline__ void observe_put(const ObsDesc &od, uint32_t k, bool flush, uint32_t blk)
     {
-        switch (od.kind) {
+        const int kind = od.kind;
+        if (kind == MCIG_OBS_XND || kind == MCIG_OBS_X2 || kind == MCIG_OBS_X2BLOCK) {
+            float v[MAXD];
+            int nv = p.ndim;
+            if (kind == MCIG_OBS_XND) {
+#pragma unroll
+                for (int i = 0; i < MAXD; ++i) { v[i] = x[i]; }
+            } else if (kind == MCIG_OBS_X2) {
+#pragma unroll
+                for (int i = 0; i < MAXD; ++i) { v[i] = x[i] * x[i]; }
+            } else { // X2BLOCK: sum of x_i^2 over each block [b_k, b_k+1)
+                const double *pp = p.params + od.poff;
+                nv = (int)pp[0];
+#pragma unroll
+                for (int kb = 0; kb < MAXD; ++kb) {
+                    float s = 0.f;
+                    if (kb < nv) {
+                        const int a = (int)pp[1 + kb], b = (int)pp[2 + kb];
+#pragma unroll
+                        for (int i = 0; i < MAXD; ++i) {
+                            if (i >= a && i < b) { s = fmaf(x[i], x[i], s); }
+                        }
+                    }
+                    v[kb] = s;
+                }
+            }
+            put<MAXD>(od, k, flush, blk, v, nv);
+            return;
+        }
+        float v;
+        switch (kind) {
         case MCIG_OBS_X2SUM:
         case MCIG_OBS_X2MEAN: {
             float s = 0.f;
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); } // padded coordinates are 0
-            const float v = od.kind == MCIG_OBS_X2SUM ? s : s / (float)p.ndim;
-            put<1>(od, k, flush, blk, &v, 1);
+            v = kind == MCIG_OBS_X2SUM ? s : s / (float)p.ndim;
             break;
         }
-        case MCIG_OBS_XND: put<MAXD>(od, k, flush, blk, x, p.ndim); break;
-        case MCIG_OBS_X2: {
-            float v[MAXD];
-#pragma unroll
-            for (int i = 0; i < MAXD; ++i) { v[i] = x[i] * x[i]; }
-            put<MAXD>(od, k, flush, blk, v, p.ndim);
-            break;
-        }
-        case MCIG_OBS_CONST: {
-            const float v = (float)p.params[od.poff];
-            put<1>(od, k, flush, blk, &v, 1);
-            break;
-        }
-        case MCIG_OBS_LOGPDF: { // the log density the Metropolis test keeps for the walker
-            const float v = lp;
-            put<1>(od, k, flush, blk, &v, 1);
-            break;
-        }
+        case MCIG_OBS_CONST: v = (float)p.params[od.poff]; break;
         case MCIG_OBS_XI: {
             const int idx = (int)p.params[od.poff];
-            float v = 0.f;
+            v = 0.f;
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) { v = (i == idx) ? x[i] : v; }
-            put<1>(od, k, flush, blk, &v, 1);
             break;
         }
         case MCIG_OBS_POLYNOM: {
-            float v = 0.f;
+            v = 0.f;
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) { v += x[i]; }
-            put<1>(od, k, flush, blk, &v, 1);
             break;
         }
-        case MCIG_OBS_X2BLOCK: {
-            const double *pp = p.params + od.poff;
-            const int nb = (int)pp[0];
-            float v[MAXD];
-#pragma unroll
-            for (int kb = 0; kb < MAXD; ++kb) {
-                float s = 0.f;
-                if (kb < nb) {
-                    const int a = (int)pp[1 + kb], b = (int)pp[2 + kb];
-#pragma unroll
-                    for (int i = 0; i < MAXD; ++i) {
-                        if (i >= a && i < b) { s = fmaf(x[i], x[i], s); }
-                    }
-                }
-                v[kb] = s;
-            }
-            put<MAXD>(od, k, flush, blk, v, nb);
-            break;
+        case MCIG_OBS_LOGPDF: v = lp; break; // the log density the Metropolis test keeps for the walker
+        default: return;
         }
-        default: break;
-        }
+        put<1>(od, k, flush, blk, &v, 1);
     }
 
     // observable od after step r: accumulation index k = r / nskip when nskip

@@ -541,21 +541,28 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
     for (int r = warp; r < FLOW_ROWS; r += NW) { // d(0.5|z|^2)/dz / B
         if (lane < D) { s.G[r][lane] = (r < rows) ? f.z[(int64_t)(base + r) * D + lane] * f.inv_batch : 0.f; }
     }
+    // weight tiles arrive by cp.async into whichever buffer has just been freed, one copy
+    // group each, in the order they are needed: W1n/W2n of the next layer, W3t -> W3n
+    // buffer, W2t -> W2n buffer, W1t -> W3n buffer
+    load_tile_async<16>(s.W1n, LDA_S, f.wb + WB_W1N, FLOW_H);
+    load_tile_async<FLOW_H>(s.W2n, LDH_S, f.wb + WB_W2N, FLOW_H);
+    cp_async_commit();
     __syncthreads();
     for (int l = 0; l < f.L; ++l) { // reverse of the density direction
         const int *perm = f.perm + l * D;
         const float *P = f.theta + (int64_t)l * f.pstride;
         float *GP = f.grad + (int64_t)l * f.pstride;
         const __nv_bfloat16 *wl = f.wb + (int64_t)l * f.wstride;
-        load_tile<16>(s.W1n, LDA_S, wl + WB_W1N, FLOW_H);
-        load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W2N, FLOW_H);
-        load_tile<FLOW_H>(s.W3n, LDH_S, wl + WB_W3N, 32);
+        const __nv_bfloat16 *wnext = (l + 1 < f.L) ? wl + f.wstride : nullptr;
+        load_tile_async<32>(s.W3n, LDO_S, wl + WB_W3T, FLOW_H); // W3t [H][32]
+        cp_async_commit();
         for (int i = threadIdx.x; i < FLOW_ROWS * 16; i += blockDim.x) {
             const int r = i / 16, c = i % 16;
             const float v = (r < rows && c < d) ? f.tape[((int64_t)l * f.n + base + r) * 4 * d + c] : 0.f;
             s.A[r * LDA_S + c] = __float2bfloat16_rn(v);
         }
         for (int i = threadIdx.x; i < 2 * FLOW_H + 32; i += blockDim.x) { s.red[i] = 0.f; }
+        cp_async_wait<1>(); // W1n and W2n of this layer (W3t may still be in flight)
         __syncthreads();
         // recompute h1, h2 (same bf16 GEMMs as the pass kernel)
         for (int i = threadIdx.x; i < FLOW_H; i += blockDim.x) {
@@ -570,6 +577,8 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
             store_act(acc, s.bias, true, s.H1, LDH_S, r0);
         }
         __syncthreads();
+        if (wnext) { load_tile_async<16>(s.W1n, LDA_S, wnext + WB_W1N, FLOW_H); } // W1n is free
+        cp_async_commit();
         {
             float acc[16][4];
             zero_acc(acc);
@@ -577,6 +586,8 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
             store_act(acc, s.bias + FLOW_H, true, s.H2, LDH_S, r0);
         }
         __syncthreads();
+        load_tile_async<FLOW_H>(s.W2n, LDH_S, wl + WB_W2T, FLOW_H); // W2t [H][H] into the free W2n buffer
+        cp_async_commit();
         // coupling backward: g_o = [g_sraw, g_t] for the b half.  Warp w takes rows w, w+8, ...;
         // lane j is output column j, so the tape reads of a row are contiguous and the b3
         // gradient of column j accumulates in lane j's register.
@@ -610,8 +621,8 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
                 s.G[r][bj] = s.G[r][bj] * __expf(-f.tape[((int64_t)l * f.n + base + r) * 4 * d + 2 * d + lane]);
             }
         }
-        // g_h2 = (g_o W3^T) * relu'(h2): W3t [H][32] into the W3n buffer with stride LDO_S
-        load_tile<32>(s.W3n, LDO_S, wl + WB_W3T, FLOW_H);
+        // g_h2 = (g_o W3^T) * relu'(h2): W3t [H][32] in the W3n buffer with stride LDO_S
+        cp_async_wait<2>(); // W3t (the next layer's W1n and this layer's W2t may still be in flight)
         __syncthreads();
         {
             float acc[16][4];
@@ -635,6 +646,8 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
             }
         }
         __syncthreads();
+        load_tile_async<FLOW_H>(s.W3n, LDH_S, wl + WB_W1T, 16); // W1t [16][H] into the free W3n buffer
+        cp_async_commit();
         // dW3 = h2^T g_o: rows h (16 per warp), 4 n-tiles over the 32 outputs
         {
             float acc[4][4];
@@ -649,9 +662,8 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
                 }
             }
         }
-        // g_h1 = (g_h2 W2^T) * relu'(h1): W2t [H][H] into the W2n buffer
-        __syncthreads();
-        load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W2T, FLOW_H);
+        // g_h1 = (g_h2 W2^T) * relu'(h1): W2t [H][H] in the W2n buffer
+        cp_async_wait<1>(); // W2t (W1t may still be in flight)
         __syncthreads();
         {
             float acc[16][4];
@@ -687,13 +699,15 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
             }
         }
         __syncthreads();
-        // g_a = g_h1 W1^T: W1t [16][H] into the W1n buffer region sized [16][LDH_S] (it fits in W2n)
-        load_tile<FLOW_H>(s.W2n, LDH_S, wl + WB_W1T, 16);
+        // g_a = g_h1 W1^T: W1t [16][H] in the W3n buffer with stride LDH_S
+        if (wnext) { load_tile_async<FLOW_H>(s.W2n, LDH_S, wnext + WB_W2N, FLOW_H); } // W2t done: next W2n
+        cp_async_commit();
+        cp_async_wait<1>(); // W1t (the next layer's W2n may still be in flight)
         __syncthreads();
         {
             float acc[2][4];
             zero_acc(acc);
-            warp_gemm<FLOW_H / 16, 2>(s.GH1, LDH_S, r0, s.W2n, LDH_S, acc);
+            warp_gemm<FLOW_H / 16, 2>(s.GH1, LDH_S, r0, s.W3n, LDH_S, acc);
 #pragma unroll
             for (int nt = 0; nt < 2; ++nt) {
                 const int c = nt * 8 + 2 * t;

@@ -2139,11 +2139,8 @@ extern "C" int mcig_batch_run(mcig_batch *b, double *avg, double *err)
             if (err) { err[off + i] = e; }
         }
         off += nod;
-        h->h_nacc.resize(nc);
-        h->h_nrej.resize(nc);
-        cudaMemcpy(h->h_nacc.data(), h->nacc.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost);
-        cudaMemcpy(h->h_nrej.data(), h->nrej.p, nc * sizeof(int64_t), cudaMemcpyDeviceToHost);
-        h->counts_on_device = h->chains_on_device = false; // the host copies above are current
+        h->counts_on_device = true;   // copied when asked for (host_results)
+        h->chains_on_device = false;  // the chain estimates were set above
         h->chain_scale = 1.;
     }
     return MCIG_OK;

@@ -185,6 +185,32 @@ static __device__ float pdf_logp_f(const KParams &p, const PdfDesc &d, const flo
     }
 }
 
+// log p(xn) - log p(w) of a separable float sampling function when xn and w differ only
+// in [lo, hi) (the float counterpart of the updatedAcceptance of Gauss / ExpNDPDF,
+// TestMCIFunctions.hpp:181-189, :246-255); returns false for the other kinds
+static __device__ bool pdf_delta_f(const PdfDesc &d, const float *w, const float *xn, int lo, int hi, float &delta)
+{
+    float s = 0.f;
+    switch (d.kind) {
+    case MCIG_PDF_GAUSS_SUM:
+    case MCIG_PDF_GAUSS:
+        for (int i = lo; i < hi; ++i) { s += xn[i] * xn[i] - w[i] * w[i]; }
+        delta = -s;
+        return true;
+    case MCIG_PDF_EXP:
+        for (int i = lo; i < hi; ++i) { s += fabsf(xn[i]) - fabsf(w[i]); }
+        delta = -s;
+        return true;
+    case MCIG_PDF_GAUSS_BLOCK: {
+        const int a = max(lo, d.b0), b = min(hi, d.b1);
+        for (int i = a; i < b; ++i) { s += xn[i] * xn[i] - w[i] * w[i]; }
+        delta = -(float)d.c * s;
+        return true;
+    }
+    default: return false;
+    }
+}
+
 // ------------------------------------------------------------------------
 // observables (observableFunction of the test classes; oracle obs_eval)
 // ------------------------------------------------------------------------
@@ -387,7 +413,8 @@ struct GenericSampler {
     }
 
     // SRRDVecMove::trialMove (SRRDVecMove.hpp:75-96) from pos into xn; returns the first index
-    __device__ int vec_move(const R *pos, int substep, int srrd, int veclen)
+    // copy_all false: xn already equals pos outside the moved vector (MultiStepMove keeps it so)
+    __device__ int vec_move(const R *pos, int substep, int srrd, int veclen, bool copy_all = true)
     {
         const int nvecs = p.ndim / veclen;
         int vidx;
@@ -400,7 +427,11 @@ struct GenericSampler {
         }
         const int lo = vidx * veclen;
         const R s = step_of_rt<R>(p, st, lo);
-        for (int i = 0; i < p.ndim; ++i) { xn[i] = pos[i]; }
+        if (copy_all) {
+            for (int i = 0; i < p.ndim; ++i) { xn[i] = pos[i]; }
+        } else {
+            for (int i = lo; i < lo + veclen; ++i) { xn[i] = pos[i]; }
+        }
         constexpr int CPB = Cpb<R>::v;
         R d[CPB];
         for (int i = lo; i < lo + veclen; ++i) {
@@ -425,7 +456,9 @@ struct GenericSampler {
     // sub-pdfs; returns oldPDF/newPDF (double) or its log (float); xn = end point.
     __device__ R multistep()
     {
-        for (int i = 0; i < p.ndim; ++i) { w[i] = x[i]; }
+        // w: the sub-chain's walker; xn equals w outside the vector a sub-step moves, so a
+        // sub-step touches only veclen coordinates
+        for (int i = 0; i < p.ndim; ++i) { w[i] = x[i]; xn[i] = x[i]; }
         R sp[MCIG_MAXPDF];
         for (int k = 0; k < p.ms_npdf; ++k) { sp[k] = pdf_state(p.ms_pdf[k], w); }
         R oldv;
@@ -437,7 +470,7 @@ struct GenericSampler {
             for (int k = 0; k < p.ms_npdf; ++k) { oldv += sp[k]; }
         }
         for (int s = 0; s < p.ms_nsteps; ++s) {
-            const int lo = vec_move(w, 1 + s, p.ms_srrd, p.ms_veclen);
+            const int lo = vec_move(w, 1 + s, p.ms_srrd, p.ms_veclen, false);
             const int hi = lo + p.ms_veclen;
             R spn[MCIG_MAXPDF];
             bool acc;
@@ -453,17 +486,23 @@ struct GenericSampler {
             } else {
                 float dl = 0.f;
                 for (int k = 0; k < p.ms_npdf; ++k) {
-                    spn[k] = pdf_logp_f(p, p.ms_pdf[k], xn, blob);
-                    dl += spn[k] - sp[k];
+                    float delta;
+                    if (!pdf_delta_f(p.ms_pdf[k], w, xn, lo, hi, delta)) {
+                        delta = pdf_logp_f(p, p.ms_pdf[k], xn, blob) - sp[k];
+                    }
+                    spn[k] = sp[k] + delta;
+                    dl += delta;
                 }
                 acc = (__log2f(accept_u(1 + s)) <= dl * 1.44269504f);
             }
             if (acc) {
                 for (int i = lo; i < hi; ++i) { w[i] = xn[i]; }
                 for (int k = 0; k < p.ms_npdf; ++k) { sp[k] = spn[k]; }
+            } else {
+                for (int i = lo; i < hi; ++i) { xn[i] = w[i]; }
             }
         }
-        for (int i = 0; i < p.ndim; ++i) { xn[i] = w[i]; }
+        // xn == w: the end point of the sub-chain
         if constexpr (EXACT) {
             double newv = 1.;
             for (int k = 0; k < p.ms_npdf; ++k) { newv *= pdf_value_d(p, p.ms_pdf[k], w, sp[k]); }
@@ -574,6 +613,17 @@ struct GenericSampler {
         for (int j = 0; j < p.nobsdim; ++j) { sums[j].zero(); }
         int64_t na = 0;
         int64_t dpos = 0; // next entry of the dump list (chain 0)
+        // per observable: steps until its next accumulation (nskip), accumulation index,
+        // accumulations left in the current block, block index - counters instead of
+        // 64-bit divisions on every step
+        int skipleft[MCIG_MAXOBS], bleft[MCIG_MAXOBS];
+        int64_t kacc[MCIG_MAXOBS], bidx[MCIG_MAXOBS];
+        for (int o = 0; o < p.nobs; ++o) {
+            skipleft[o] = 0;
+            bleft[o] = p.obs[o].bs;
+            kacc[o] = 0;
+            bidx[o] = 0;
+        }
         for (int64_t r = 0; r < n; ++r) {
             const bool a = step(movetype);
             if (c == 0 && dpos < p.ndump && r == p.dump_steps[dpos]) {
@@ -584,8 +634,9 @@ struct GenericSampler {
             if (p.bits) { p.bits[(size_t)r * p.nchains + c] = a ? 1 : 0; }
             for (int o = 0; o < p.nobs; ++o) {
                 const ObsDesc &od = p.obs[o];
-                if (r % od.nskip != 0) { continue; }
-                const int64_t k = r / od.nskip; // accumulation index
+                if (skipleft[o] > 0) { --skipleft[o]; continue; } // accumulate when nskip divides r
+                skipleft[o] = od.nskip - 1;
+                const int64_t k = kacc[o]++; // accumulation index r / nskip
                 obs_eval<R>(p, od, x, vals, blob);
                 if (od.acc == MCIG_ACC_FULL) { // FullAccumulator::_accumulate (FullAccumulator.cpp:14-18)
                     const size_t row = (size_t)(p.acc_offset + k);
@@ -598,12 +649,12 @@ struct GenericSampler {
                     }
                 } else {
                     for (int j = 0; j < od.nv; ++j) { sums[od.voff + j].add((AccV)vals[j]); }
-                    if (od.acc == MCIG_ACC_BLOCK && (k + 1) % od.bs == 0) {
+                    if (od.acc == MCIG_ACC_BLOCK && --bleft[o] == 0) { // blocksize divides k + 1
                         // block sum times 1./blocksize (BlockAccumulator.cpp:20-41)
-                        const double normf = 1. / od.bs;
-                        double *dst = (double *)od.data + (size_t)(k / od.bs) * od.nv * p.nchains + c;
+                        bleft[o] = od.bs;
+                        double *dst = (double *)od.data + (size_t)(bidx[o]++) * od.nv * p.nchains + c;
                         for (int j = 0; j < od.nv; ++j) {
-                            dst[(size_t)j * p.nchains] = sums[od.voff + j].get() * normf;
+                            dst[(size_t)j * p.nchains] = sums[od.voff + j].get() * od.inv_bs;
                             sums[od.voff + j].zero();
                         }
                     }

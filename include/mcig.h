@@ -57,6 +57,12 @@ void *mcig_get_stream(const mcig_mci *h);
  * else the general kernel), 1 general kernel, 2 register-resident kernel
  * (MCIG_ERR_UNSUPPORTED at integrate when the configuration needs the general one). */
 int mcig_set_kernel(mcig_mci *h, int policy);
+/* Phase fusion (default on): where the register-resident kernel serves calibration, a fixed
+ * burn-in and the sampling (no file output, no accept recording), integrate runs the three
+ * phases of every chain in one launch, so chains whose step calibration converges early
+ * sample while the others still calibrate.  Results are those of separate launches; the
+ * timings then report the whole launch as sampling time.  0 turns it off. */
+int mcig_set_phase_fusion(mcig_mci *h, int on);
 
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
  * from counter (step, c).  */
@@ -230,6 +236,28 @@ int mcig_batch_get_blocks(const mcig_batch *b, int *blocks);
 int mcig_batch_set_blocks(mcig_batch *b, const int *blocks);
 /* time 32/64/128/256 chains per block per bucket, keep the fastest; cache file optional */
 int mcig_batch_autotune(mcig_batch *b, const char *cache_path);
+
+/* ------------------------------------------------------------------------
+ * Plugins: user sampling functions and observables compiled for the device
+ * (include/mcig/plugin.cuh).  They replace the reference's user classes derived
+ * from SamplingFunctionInterface / ObservableFunctionInterface, passed to
+ * MCI::addSamplingFunction (MCIntegrator.hpp:174-184) and MCI::addObservable
+ * (:152-172).  A plugin is a shared library built with MCIG_PLUGIN; after
+ * mcig_set_plugin the kinds MCIG_PDF_USER + k and MCIG_OBS_USER + k name its k-th
+ * sampling function and observable (addSamplingFunction / addObservable /
+ * mcig_multistep_add_pdf, parameters handed to the functor).  Handles with plugin
+ * kinds run the plugin's general kernel in every precision; the register-resident
+ * kernel, batches, the learned proposal, observable file output and the LOGPDF
+ * observable are for built-in kinds.  A plugin stays loaded while handles use it.
+ * ------------------------------------------------------------------------ */
+typedef struct mcig_plugin mcig_plugin;
+/* dlopen the library; MCIG_ERR_INVALID_ARGUMENT when it is not a plugin of this version */
+int mcig_plugin_load(const char *path, mcig_plugin **out);
+int mcig_plugin_unload(mcig_plugin *pl);
+/* number of sampling functions and observables of the plugin */
+int mcig_plugin_counts(const mcig_plugin *pl, int *npdf, int *nobs);
+/* attach (or, with NULL, detach) the plugin whose kinds the handle may use */
+int mcig_set_plugin(mcig_mci *h, const mcig_plugin *pl);
 
 /* Philox4x32-10 block (for known-answer tests of the device generator) */
 int mcig_philox_block(int device, const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

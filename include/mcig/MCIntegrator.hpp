@@ -82,6 +82,24 @@ inline void check(int rc)
 inline const double *ptr(const std::vector<double> &v) { return v.empty() ? nullptr : v.data(); }
 } // namespace detail
 
+// user sampling functions and observables compiled for the device (mcig/plugin.cuh): the
+// loaded library; its k-th functors are pdf(k, params) and obs(k, params).  It must outlive
+// every MCI that uses it.
+class Plugin
+{
+private:
+    mcig_plugin *_p = nullptr;
+
+public:
+    explicit Plugin(const std::string &path) { detail::check(mcig_plugin_load(path.c_str(), &_p)); }
+    ~Plugin() { mcig_plugin_unload(_p); }
+    Plugin(const Plugin &) = delete;
+    Plugin &operator=(const Plugin &) = delete;
+    const mcig_plugin *handle() const { return _p; }
+    static SamplingFunction pdf(int k, std::vector<double> params = {}) { return {MCIG_PDF_USER + k, std::move(params)}; }
+    static Observable obs(int k, std::vector<double> params = {}) { return {MCIG_OBS_USER + k, std::move(params)}; }
+};
+
 class MCI
 {
 private:
@@ -106,6 +124,7 @@ public:
     mcig_mci *handle() const { return _h; }
 
     // --- setters
+    void setPlugin(const Plugin *pl) { detail::check(mcig_set_plugin(_h, pl ? pl->handle() : nullptr)); }
     void setSeed(uint64_t seed) { detail::check(mcig_set_seed(_h, seed)); }
     // file output of chain 0 during the main sampling (MCIntegrator.hpp storeObservablesOnFile et al.)
     void storeObservablesOnFile(const std::string &path, int freq) { detail::check(mcig_store_observables_on_file(_h, path.c_str(), freq)); }

@@ -61,7 +61,10 @@ enum mcig_accumulator { MCIG_ACC_SIMPLE = 0, MCIG_ACC_FULL = 1, MCIG_ACC_BLOCK =
  */
 enum mcig_pdf_kind {
     MCIG_PDF_GAUSS_SUM = 0, MCIG_PDF_GAUSS = 1, MCIG_PDF_EXP = 2,
-    MCIG_PDF_GAUSS_PREC = 3, MCIG_PDF_GAUSS_BLOCK = 4, MCIG_PDF_GAUSS_MIX = 5
+    MCIG_PDF_GAUSS_PREC = 3, MCIG_PDF_GAUSS_BLOCK = 4, MCIG_PDF_GAUSS_MIX = 5,
+    /* MCIG_PDF_USER + k: the k-th sampling function of the plugin attached to the handle
+     * (mcig_set_plugin, include/mcig/plugin.cuh), k < MCIG_MAXUSER */
+    MCIG_PDF_USER = 100
 };
 
 /* Observables.  Number of values in brackets.
@@ -78,8 +81,13 @@ enum mcig_pdf_kind {
 enum mcig_obs_kind {
     MCIG_OBS_X2SUM = 0, MCIG_OBS_XND = 1, MCIG_OBS_X2 = 2, MCIG_OBS_X2MEAN = 3,
     MCIG_OBS_CONST = 4, MCIG_OBS_POLYNOM = 5, MCIG_OBS_X2BLOCK = 6, MCIG_OBS_GAUSSX2 = 7, MCIG_OBS_XI = 8,
-    MCIG_OBS_LOGPDF = 9 /* log of the product of the sampling functions at the walker (depends on them) */
+    MCIG_OBS_LOGPDF = 9, /* log of the product of the sampling functions at the walker (depends on them) */
+    /* MCIG_OBS_USER + k: the k-th observable of the attached plugin, k < MCIG_MAXUSER */
+    MCIG_OBS_USER = 100
 };
+
+/* user functors per plugin and kind (sampling functions, observables) */
+#define MCIG_MAXUSER 16
 
 /* arithmetic of the sampling loop on the device */
 enum mcig_precision {

@@ -2,4 +2,4 @@
 MCI::integrate (Metropolis sampling, accumulators, estimators) as sm_103a CUDA
 kernels behind the C ABI of include/mcig.h (libmcigpu.so)."""
 from .mci import *  # noqa: F401,F403
-from .mci import MCI, Flow, Batch, integrate_flow, estimate, accumulate_walk, philox_block  # noqa: F401
+from .mci import MCI, Flow, Batch, Plugin, integrate_flow, estimate, accumulate_walk, philox_block  # noqa: F401

@@ -31,6 +31,7 @@ SIGNATURES = {
     "mcig_set_precision": (c_int, [c_void_p, c_int]),
     "mcig_get_stream": (c_void_p, [c_void_p]),
     "mcig_set_kernel": (c_int, [c_void_p, c_int]),
+    "mcig_set_phase_fusion": (c_int, [c_void_p, c_int]),
     "mcig_set_seed": (c_int, [c_void_p, ctypes.c_uint64]),
     "mcig_set_x": (c_int, [c_void_p, P_double, c_int64]),
     "mcig_get_x": (c_int, [c_void_p, P_double]),
@@ -95,6 +96,10 @@ SIGNATURES = {
     "mcig_integrate_flow": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_int64, c_int, c_int, c_double, P_double,
                                     P_double, c_int, c_int, P_double]),
     "mcig_mjblocker_estimate_noalloc": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "mcig_plugin_load": (c_int, [ctypes.c_char_p, ctypes.POINTER(c_void_p)]),
+    "mcig_plugin_unload": (c_int, [c_void_p]),
+    "mcig_plugin_counts": (c_int, [c_void_p, P_int, P_int]),
+    "mcig_set_plugin": (c_int, [c_void_p, c_void_p]),
 }
 
 

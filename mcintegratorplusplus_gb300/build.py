@@ -107,5 +107,43 @@ def build(force=False, verbose=False):
     return LIB
 
 
+def build_plugin(src, out, verbose=False):
+    """Compile a plugin source (one that ends with MCIG_PLUGIN, include/mcig/plugin.cuh) into the
+    shared library `out`: the double path (-DMCIG_PLUGIN_PART=1, -fmad=false: the reference's
+    operation order) and the float path (-DMCIG_PLUGIN_PART=2) as two objects, linked together.
+    Skipped when `out` is newer than the source and the integrator's headers."""
+    src, out = os.path.abspath(src), os.path.abspath(out)
+    if os.path.exists(out) and os.path.getmtime(out) > max(os.path.getmtime(src), _deps()):
+        return out
+    work = out + ".build"
+    os.makedirs(work, exist_ok=True)
+    inc = ["-I", os.path.join(os.path.dirname(HERE), "include"), "-I", CSRC]
+
+    def part(args):
+        n, flags = args
+        obj = os.path.join(work, "part%d.o" % n)
+        r = None
+        for extra in FALLBACKS:
+            cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"] + inc + flags + extra + \
+                ["-DMCIG_PLUGIN_PART=%d" % n, "-c", src, "-o", obj]
+            r = subprocess.run(cmd, capture_output=True, text=True, env=dict(os.environ, TMPDIR=work))
+            if r.returncode == 0:
+                return obj
+            if verbose:
+                print("nvcc failed for plugin part %d with %s (rc %d)" % (n, extra, r.returncode))
+        raise RuntimeError("nvcc failed for plugin %s:\n%s" % (src, r.stderr[-4000:]))
+
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        objs = list(ex.map(part, [(1, ["-fmad=false"]), (2, [])]))
+    tmp = out + ".tmp%d" % os.getpid()
+    r = subprocess.run([_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("plugin link failed:\n" + r.stderr[-4000:])
+    os.replace(tmp, out)
+    if verbose:
+        print("linked", out)
+    return out
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True)

@@ -4,6 +4,7 @@
 // Compiled with -fmad=false: the estimator kernels in this unit follow the
 // reference's double operation order.
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <chrono>
@@ -91,8 +92,18 @@ struct ObsDef {
     int nv, blocksize, nskip, flag_equil, estimator, acc;
 };
 
+// a loaded plugin (include/mcig/plugin.cuh): its user functors and its general kernel
+struct mcig_plugin {
+    void *dl = nullptr;
+    int npdf = 0, nobs = 0;
+    int (*pdf_nproto)(int, int) = nullptr;
+    int (*obs_nvals)(int, int) = nullptr;
+    mcig_plugin_launch_fn (*launcher)(int, int) = nullptr;
+};
+
 struct mcig_mci {
     int ndim;
+    const mcig_plugin *plugin = nullptr; // user functors (MCIG_PDF_USER / MCIG_OBS_USER kinds)
     int64_t nchains;
     int device;
     int prec;
@@ -116,6 +127,7 @@ struct mcig_mci {
     int64_t ndecorr = -10000;
     int full32 = 0;
     int kernel_policy = 0; // 0 auto, 1 general kernel, 2 register-resident kernel
+    int fuse_phases = 1;   // calibration, burn-in and sampling in one register-resident launch
     FastConst fc;          // constant data of the register-resident kernel
     // device chain state
     DBuf<double> x, step;
@@ -227,6 +239,65 @@ static int obs_nvals(int ndim, int kind, const double *params, int np, int *nv)
     }
 }
 
+// plugin kinds (include/mcig/plugin.cuh): the k-th functor of the attached plugin
+static bool is_user_pdf(int kind) { return kind >= MCIG_PDF_USER; }
+static bool is_user_obs(int kind) { return kind >= MCIG_OBS_USER; }
+
+static int user_pdf_nproto(const mcig_mci *h, int kind, int *nproto)
+{
+    if (!h->plugin) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "sampling function kind %d is a plugin kind and the handle has no plugin", kind); }
+    const int k = kind - MCIG_PDF_USER;
+    if (k >= h->plugin->npdf) {
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "the plugin has %d sampling functions, kind %d asks for number %d", h->plugin->npdf, kind, k);
+    }
+    const int n = h->plugin->pdf_nproto(k, h->ndim);
+    if (n < 0) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin sampling function %d: nproto(%d) is above its max_nproto", k, h->ndim); }
+    *nproto = n;
+    return MCIG_OK;
+}
+
+static int user_obs_nvals(const mcig_mci *h, int kind, int *nv)
+{
+    if (!h->plugin) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "observable kind %d is a plugin kind and the handle has no plugin", kind); }
+    const int k = kind - MCIG_OBS_USER;
+    if (k >= h->plugin->nobs) {
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "the plugin has %d observables, kind %d asks for number %d", h->plugin->nobs, kind, k);
+    }
+    const int n = h->plugin->obs_nvals(k, h->ndim);
+    if (n < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin observable %d: nobs(%d) = %d", k, h->ndim, n); }
+    *nv = n;
+    return MCIG_OK;
+}
+
+static bool uses_plugin(const mcig_mci *h)
+{
+    for (auto &d : h->pdfs) {
+        if (is_user_pdf(d.kind)) { return true; }
+    }
+    for (auto &d : h->ms_pdfs) {
+        if (is_user_pdf(d.kind)) { return true; }
+    }
+    for (auto &o : h->obs) {
+        if (is_user_obs(o.kind)) { return true; }
+    }
+    return false;
+}
+
+// what the plugin kernel does not serve
+static int check_plugin_use(const mcig_mci *h)
+{
+    if (!uses_plugin(h)) { return MCIG_OK; }
+    if (!h->plugin) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin kinds are in use and the handle has no plugin"); }
+    bool upd = false, uob = false;
+    for (auto &d : h->pdfs) { upd = upd || is_user_pdf(d.kind); }
+    for (auto &o : h->obs) { uob = uob || is_user_obs(o.kind); }
+    for (auto &o : h->obs) {
+        if (upd && o.kind == MCIG_OBS_LOGPDF) { return set_err(MCIG_ERR_UNSUPPORTED, "the LOGPDF observable reads built-in sampling functions only"); }
+    }
+    if (uob && h->obs_freq > 0) { return set_err(MCIG_ERR_UNSUPPORTED, "observable file output is not served for plugin observables"); }
+    return MCIG_OK;
+}
+
 // ------------------------------------------------------------------------
 // creation / state
 // ------------------------------------------------------------------------
@@ -285,6 +356,73 @@ extern "C" int mcig_create(int ndim, int64_t nchains, int device, int precision,
         return rc;
     }
     *out = h;
+    return MCIG_OK;
+}
+
+// ------------------------------------------------------------------------
+// plugins (include/mcig/plugin.cuh)
+// ------------------------------------------------------------------------
+extern "C" int mcig_plugin_load(const char *path, mcig_plugin **out)
+{
+    if (!path || !out) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "path or out is NULL"); }
+    *out = nullptr;
+    void *dl = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+    if (!dl) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin %s: %s", path, dlerror()); }
+    auto sym = [&](const char *name) { return dlsym(dl, name); };
+    auto abi = (int (*)(void))sym("mcig_plugin_abi");
+    auto kps = (int (*)(void))sym("mcig_plugin_kparams_size");
+    auto npdf = (int (*)(void))sym("mcig_plugin_npdf");
+    auto nobs = (int (*)(void))sym("mcig_plugin_nobs");
+    auto pl = new mcig_plugin;
+    pl->pdf_nproto = (int (*)(int, int))sym("mcig_plugin_pdf_nproto");
+    pl->obs_nvals = (int (*)(int, int))sym("mcig_plugin_obs_nvals");
+    pl->launcher = (mcig_plugin_launch_fn(*)(int, int))sym("mcig_plugin_launcher");
+    if (!abi || !kps || !npdf || !nobs || !pl->pdf_nproto || !pl->obs_nvals || !pl->launcher) {
+        delete pl;
+        dlclose(dl);
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin %s does not export the plugin entry points (MCIG_PLUGIN)", path);
+    }
+    if (abi() != MCIG_PLUGIN_ABI || kps() != (int)sizeof(KParams)) {
+        delete pl;
+        dlclose(dl);
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin %s was built against another version of the integrator", path);
+    }
+    pl->npdf = npdf();
+    pl->nobs = nobs();
+    if (pl->npdf > MCIG_MAXUSER || pl->nobs > MCIG_MAXUSER) {
+        delete pl;
+        dlclose(dl);
+        return set_err(MCIG_ERR_UNSUPPORTED, "plugin %s: at most %d sampling functions and %d observables", path, MCIG_MAXUSER, MCIG_MAXUSER);
+    }
+    pl->dl = dl;
+    *out = pl;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_plugin_unload(mcig_plugin *pl)
+{
+    if (!pl) { return MCIG_OK; }
+    if (pl->dl) { dlclose(pl->dl); }
+    delete pl;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_plugin_counts(const mcig_plugin *pl, int *npdf, int *nobs)
+{
+    if (!pl) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin is NULL"); }
+    if (npdf) { *npdf = pl->npdf; }
+    if (nobs) { *nobs = pl->nobs; }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_plugin(mcig_mci *h, const mcig_plugin *pl)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    if (!pl && uses_plugin(h)) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "the handle holds plugin kinds: remove them before detaching the plugin"); }
+    if (pl && h->plugin && pl != h->plugin && uses_plugin(h)) {
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "the handle holds kinds of another plugin: remove them first");
+    }
+    h->plugin = pl;
     return MCIG_OK;
 }
 
@@ -492,7 +630,8 @@ extern "C" int mcig_multistep_add_pdf(mcig_mci *h, int kind, const double *param
 {
     if (h->movetype != MCIG_MOVE_MULTISTEP) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "no multi-step move is set"); }
     if ((int)h->ms_pdfs.size() >= MCIG_MAXPDF) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d sub-sampling functions", MCIG_MAXPDF); }
-    int rc = check_pdf(h->ndim, kind, params, nparams);
+    int np_ = 0;
+    int rc = is_user_pdf(kind) ? user_pdf_nproto(h, kind, &np_) : check_pdf(h->ndim, kind, params, nparams);
     if (rc) { return rc; }
     h->ms_pdfs.push_back(PdfDef{kind, std::vector<double>(params, params + std::max(nparams, 0))});
     return MCIG_OK;
@@ -501,7 +640,8 @@ extern "C" int mcig_multistep_add_pdf(mcig_mci *h, int kind, const double *param
 extern "C" int mcig_add_sampling_function(mcig_mci *h, int kind, const double *params, int nparams)
 {
     if ((int)h->pdfs.size() >= MCIG_MAXPDF) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d sampling functions", MCIG_MAXPDF); }
-    int rc = check_pdf(h->ndim, kind, params, nparams);
+    int np_ = 0;
+    int rc = is_user_pdf(kind) ? user_pdf_nproto(h, kind, &np_) : check_pdf(h->ndim, kind, params, nparams);
     if (rc) { return rc; }
     h->pdfs.push_back(PdfDef{kind, std::vector<double>(params, params + std::max(nparams, 0))});
     return MCIG_OK;
@@ -532,7 +672,7 @@ extern "C" int mcig_add_observable(mcig_mci *h, int kind, const double *params, 
     }
     if (estimator < MCIG_EST_NOOP || estimator > MCIG_EST_MJBLOCKER) { return set_err(MCIG_ERR_DOMAIN, "[createEstimator] Unhandled estimator enumerator."); }
     int nv = 0;
-    int rc = obs_nvals(h->ndim, kind, params, nparams, &nv);
+    int rc = is_user_obs(kind) ? user_obs_nvals(h, kind, &nv) : obs_nvals(h->ndim, kind, params, nparams, &nv);
     if (rc) { return rc; }
     int maxnv = 2 * maxd_bucket(h->ndim) + 8;
     if (nobsdim(h) + nv > maxnv) { return set_err(MCIG_ERR_UNSUPPORTED, "at most %d observable values for ndim %d", maxnv, h->ndim); }
@@ -682,6 +822,7 @@ static int build_pdf_desc(mcig_mci *h, const PdfDef &d, std::vector<double> &P, 
     out.poff = (int)P.size();
     out.np = (int)d.params.size();
     P.insert(P.end(), d.params.begin(), d.params.end());
+    if (is_user_pdf(d.kind)) { return user_pdf_nproto(h, d.kind, &out.nproto); }
     if (d.kind == MCIG_PDF_GAUSS_BLOCK) {
         out.b0 = (int)d.params[0];
         out.b1 = (int)d.params[1];
@@ -771,6 +912,7 @@ static void fill_fast_const(const mcig_mci *h, FastConst &kp)
 static int fill_common(mcig_mci *h, KParams &kp)
 {
     memset(&kp, 0, sizeof(kp));
+    if (int rc0 = check_plugin_use(h)) { return rc0; }
     kp.ndim = h->ndim;
     kp.nchains = (int)h->nchains;
     kp.srrd = h->srrd;
@@ -873,6 +1015,7 @@ static int fill_common(mcig_mci *h, KParams &kp)
 // with a sampling function and observables it evaluates without exp()
 static bool fast_eligible(const mcig_mci *h)
 {
+    if (uses_plugin(h)) { return false; }
     if (h->prec == MCIG_PREC_FP64 || h->replay || h->ndim > 32 || h->pdfs.empty()) { return false; }
     if (h->srrd != MCIG_SRRD_UNIFORM && h->srrd != MCIG_SRRD_GAUSSIAN) { return false; }
     if (h->movetype != MCIG_MOVE_ALL && h->movetype != MCIG_MOVE_VEC) { return false; }
@@ -910,6 +1053,13 @@ static int launch(mcig_mci *h, const KParams &kp)
         }
         fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk);
         smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
+    } else if (uses_plugin(h)) { // the plugin's general kernel over its functors
+        mcig_plugin_launch_fn pf = h->plugin ? h->plugin->launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX) : nullptr;
+        if (!pf) { return set_err(MCIG_ERR_UNSUPPORTED, "the plugin has no kernel for this precision"); }
+        const int e = pf(kp, h->movetype, grid, block, smem, h->stream);
+        if (e != 0) { return set_err(MCIG_ERR_CUDA, "plugin kernel launch: %s", cudaGetErrorString((cudaError_t)e)); }
+        ++h->launches;
+        return MCIG_OK;
     } else {
         fn = mcig_generic_launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX);
     }
@@ -917,6 +1067,13 @@ static int launch(mcig_mci *h, const KParams &kp)
     fn(kp, &h->fc, h->movetype, grid, block, smem, h->stream);
     ++h->launches;
     CK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_phase_fusion(mcig_mci *h, int on)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    h->fuse_phases = on ? 1 : 0;
     return MCIG_OK;
 }
 
@@ -1514,16 +1671,38 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
         CK(cudaMemcpyAsync(h->dump_steps.p, dump.data(), dump.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
     }
     CK(cudaEventRecord(h->ev[0], h->stream));
+    // the three phases in one launch of the register-resident kernel, where that kernel
+    // serves each of them (fixed burn-in, no file output): every chain runs
+    // findMRT2Step, initialDecorrelation and sample one after the other on its own
+    const bool calib = !h->pdfs.empty() && do_find && h->nfind != 0;
+    const bool burnin = !h->pdfs.empty() && do_decorr && h->ndecorr > 0;
+    const int64_t lim = (int64_t)1 << 31;
+    const bool fuse = h->fuse_phases && nmc > 0 && nmc < lim && h->ndecorr < lim && dump.empty() && !h->record &&
+                      !(do_decorr && h->ndecorr < 0) && h->kernel_policy != 1 && fast_eligible(h);
+    if (fuse) {
+        KParams s = kp;
+        s.mode = KMODE_FUSED;
+        s.nsteps = nmc;
+        s.fuse_calib = calib ? min_stat(h->ndim) : 0;
+        s.fuse_burnin = burnin ? h->ndecorr : 0;
+        for (size_t o = 0; o < h->obs.size(); ++o) {
+            s.obs[o].data = h->obsdata[o].p;
+            s.obs[o].nstore = h->obs_nstore[o];
+        }
+        CK(cudaEventRecord(h->ev[1], h->stream)); // the phases' time is reported as sampling time
+        CK(cudaEventRecord(h->ev[2], h->stream));
+        if ((rc = launch(h, s))) { return rc; }
+    }
     // phase 1: MCI::findMRT2Step (only with a pdf; every move here has step sizes)
-    if (!h->pdfs.empty() && do_find && h->nfind != 0) {
+    if (!fuse && calib) {
         KParams c = kp;
         c.mode = KMODE_CALIB;
         c.nsteps = min_stat(h->ndim);
         if ((rc = launch(h, c))) { return rc; }
     }
-    CK(cudaEventRecord(h->ev[1], h->stream));
+    if (!fuse) { CK(cudaEventRecord(h->ev[1], h->stream)); }
     // phase 2: MCI::initialDecorrelation
-    if (!h->pdfs.empty() && do_decorr) {
+    if (!fuse && !h->pdfs.empty() && do_decorr) {
         if (h->ndecorr > 0) {
             KParams d = kp;
             d.mode = KMODE_STEPS;
@@ -1533,8 +1712,8 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
             if ((rc = auto_decorrelation(h, kp))) { return rc; }
         }
     }
-    CK(cudaEventRecord(h->ev[2], h->stream));
-    if (nmc > 0) {
+    if (!fuse) { CK(cudaEventRecord(h->ev[2], h->stream)); }
+    if (nmc > 0 && !fuse) {
         KParams s = kp;
         s.mode = KMODE_SAMPLE;
         s.nsteps = nmc;
@@ -1759,6 +1938,7 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     if (mcig_flow_dim(f) != h->ndim) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "flow dimension differs from the integrator's"); }
     if (h->prec == MCIG_PREC_FP64 || h->replay) { return set_err(MCIG_ERR_UNSUPPORTED, "the learned proposal runs in the float precision modes"); }
     if (h->pdfs.empty()) { return set_err(MCIG_ERR_DOMAIN, "the learned proposal needs a sampling function"); }
+    if (uses_plugin(h)) { return set_err(MCIG_ERR_UNSUPPORTED, "the learned proposal evaluates built-in sampling functions only"); }
     if (period < 1 || nmc < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "period and nmc must be >= 1"); }
     for (auto &o : h->obs) {
         if (o.acc != MCIG_ACC_FULL || o.nskip != 1) {
@@ -2006,6 +2186,7 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
         if (!h || h->device != dev) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: every handle must exist on the same device"); }
         if (h->prec != MCIG_PREC_FP32 || h->replay) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: handles must use MCIG_PREC_FP32 and Philox"); }
         if (h->pdfs.empty()) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: every integral needs a sampling function"); }
+        if (uses_plugin(h)) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: plugin kinds are integrated one handle at a time"); }
         if (nmc[i] < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: nmc must be >= 1"); }
         if (do_decorr && h->ndecorr < 0) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: automatic decorrelation is not batched (use N > 0)"); }
         for (auto &o : h->obs) {

@@ -35,7 +35,9 @@
 #define MCIG_FCONST 2080 // floats of sampling-function data in the parameter block (register-resident kernel)
 
 enum { RNG_PHILOX = 0, RNG_TAPE = 1 };
-enum { KMODE_STEPS = 0, KMODE_SAMPLE = 1, KMODE_CALIB = 2 };
+// KMODE_FUSED (register-resident kernel): calibration (MIN_STAT fuse_calib, none if 0), burn-in
+// (fuse_burnin steps) and sampling (nsteps) of each chain in one launch
+enum { KMODE_STEPS = 0, KMODE_SAMPLE = 1, KMODE_CALIB = 2, KMODE_FUSED = 3 };
 
 struct PdfDesc {
     int kind;
@@ -45,6 +47,7 @@ struct PdfDesc {
     double c;     // GAUSS_BLOCK: 1/(2 w^2)
     int foff;     // float path: offset of this pdf's data in the shared-memory blob
     int fstride;  // float path: coordinate stride of that data (>= ndim, zero-padded)
+    int nproto;   // plugin kinds: proto values of this sampling function
 };
 
 struct ObsDesc {
@@ -66,8 +69,9 @@ struct ObsDesc {
 struct KParams {
     int ndim;
     int nchains;
-    int64_t nsteps;     // steps of this launch (KMODE_STEPS / KMODE_SAMPLE), MIN_STAT (KMODE_CALIB)
+    int64_t nsteps;     // steps of this launch (KMODE_STEPS / KMODE_SAMPLE / KMODE_FUSED), MIN_STAT (KMODE_CALIB)
     int mode;
+    int64_t fuse_calib, fuse_burnin; // KMODE_FUSED: MIN_STAT of the calibration (0: none), burn-in steps
     // trial move
     int srrd, veclen, ntypes;
     int typeEnds[MCIG_MAXTYPES];

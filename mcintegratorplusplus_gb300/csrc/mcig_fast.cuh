@@ -421,9 +421,8 @@ struct FastSampler {
     }
 
     // MCI::findMRT2Step (MCIntegrator.cpp:87-168) for this chain alone
-    __device__ void calibrate()
+    __device__ void calibrate(int64_t MIN_STAT)
     {
-        const int64_t MIN_STAT = p.nsteps;
         int cons = 0, counter = 0;
         int64_t na = 0;
         while ((p.nfind < 0 && cons < 5) || counter < p.nfind) {
@@ -482,8 +481,16 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
     FastSampler<MAXD, MOVE, KAHAN, PK> s(p, fc, c, slots);
-    if (p.mode == KMODE_CALIB) { s.calibrate(); }
-    else { s.run(p.nsteps, p.mode == KMODE_SAMPLE); }
+    if (p.mode == KMODE_CALIB) { s.calibrate(p.nsteps); }
+    else if (p.mode == KMODE_FUSED) {
+        // MCI::integrate's phases for this chain alone: a chain whose calibration converges
+        // early goes on sampling while the others still calibrate
+        if (p.fuse_calib > 0) { s.calibrate(p.fuse_calib); }
+        if (p.fuse_burnin > 0) { s.run(p.fuse_burnin, false); }
+        s.run(p.nsteps, true);
+    } else {
+        s.run(p.nsteps, p.mode == KMODE_SAMPLE);
+    }
     s.store_state();
 }
 

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "mcig_common.cuh"
+#include "mcig_plugin.cuh"
 
 template <class R>
 __device__ __forceinline__ R step_of_rt(const KParams &p, const R *st, int i)
@@ -318,11 +319,25 @@ template <> struct AccSlot<true> {
 // ------------------------------------------------------------------------
 // the sampler
 // ------------------------------------------------------------------------
-template <class R, int RNG, bool KAHAN>
-struct GenericSampler {
+// proto values of plugin sampling functions: protoold / protonew of the main chain's (upo,
+// upn) and of MultiStepMove's sub-pdfs (mpo, mpn), the k-th at k * max_nproto; an empty base
+// of the built-in kernels
+template <class R, int CAP, bool ON> struct UserProtoStore {
+    R upo[CAP], upn[CAP], mpo[CAP], mpn[CAP];
+};
+template <class R, int CAP> struct UserProtoStore<R, CAP, false> {
+    static constexpr R *upo = nullptr, *upn = nullptr, *mpo = nullptr, *mpn = nullptr;
+};
+
+// U: the plugin's functor lists (mcig_plugin.cuh); mcig::NoPlugin for the built-in kernels
+template <class R, int RNG, bool KAHAN, class U = mcig::NoPlugin>
+struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, (U::npdf > 0)> {
     static constexpr bool EXACT = std::is_same<R, double>::value;
     static constexpr int NV = 2 * MCIG_MAXDIM + 8;
     using AccV = typename std::conditional<KAHAN, float, double>::type;
+    static constexpr bool USER_PDF = U::npdf > 0;
+    static constexpr bool USER_OBS = U::nobs > 0;
+    static constexpr int MP = U::max_nproto; // proto values per plugin pdf
 
     const KParams &p;
     const int c;
@@ -383,10 +398,50 @@ struct GenericSampler {
         else { return pdf_logp_f(p, d, pos, blob); }
     }
 
+    __device__ __forceinline__ bool user_pdf(const PdfDesc &d) const
+    {
+        if constexpr (USER_PDF) { return d.kind >= MCIG_PDF_USER; }
+        else { return false; }
+    }
+    __device__ __forceinline__ bool user_obs(const ObsDesc &o) const
+    {
+        if constexpr (USER_OBS) { return o.kind >= MCIG_OBS_USER; }
+        else { return false; }
+    }
+    __device__ __forceinline__ mcig::UserArgs uargs(int poff, int np) const { return mcig::UserArgs{p.ndim, p.params + poff, np}; }
+
+    // ProtoFunctionInterface::initializeProtoValues of a plugin sampling function (protonew = protoold)
+    __device__ void user_init(const PdfDesc &d, const R *pos, R *po, R *pn)
+    {
+        U::proto(d.kind - MCIG_PDF_USER, uargs(d.poff, d.np), pos, po);
+        for (int j = 0; j < d.nproto; ++j) { pn[j] = po[j]; }
+    }
+    // SamplingFunctionInterface::computeAcceptance of a plugin sampling function: updates pn
+    __device__ R user_accept(const PdfDesc &d, const R *xo, const R *xnew, bool partial, int lo, int hi, const R *po, R *pn)
+    {
+        const mcig::UserWalker<R> w{xo, xnew, hi - lo, lo};
+        return U::accept(d.kind - MCIG_PDF_USER, uargs(d.poff, d.np), w, partial, po, pn);
+    }
+    // newToOld (src, dst) = (pn, po) on acceptance, oldToNew = (po, pn) on rejection
+    __device__ __forceinline__ static void copy_protos(const R *src, R *dst, int n)
+    {
+        for (int j = 0; j < n; ++j) { dst[j] = src[j]; }
+    }
+    // samplingFunction of a plugin pdf at its protos: the value (double) or its log (float)
+    __device__ __forceinline__ R user_value(const PdfDesc &d, const R *pv)
+    {
+        const R v = U::sampling(d.kind - MCIG_PDF_USER, uargs(d.poff, d.np), pv);
+        if constexpr (EXACT) { return v; }
+        else { return logf(v); }
+    }
+
     // ProtoFunctionInterface::initializeProtoValues (ProtoFunctionInterface.cpp:40-44)
     __device__ void init_protos()
     {
-        for (int k = 0; k < p.npdf; ++k) { lp[k] = pdf_state(p.pdf[k], x); }
+        for (int k = 0; k < p.npdf; ++k) {
+            if (user_pdf(p.pdf[k])) { user_init(p.pdf[k], x, this->upo + k * MP, this->upn + k * MP); }
+            else { lp[k] = pdf_state(p.pdf[k], x); }
+        }
     }
 
     // draw j of the move group (substep, TAG_MOVE): coordinate-indexed for Philox
@@ -460,11 +515,20 @@ struct GenericSampler {
         // sub-step touches only veclen coordinates
         for (int i = 0; i < p.ndim; ++i) { w[i] = x[i]; xn[i] = x[i]; }
         R sp[MCIG_MAXPDF];
-        for (int k = 0; k < p.ms_npdf; ++k) { sp[k] = pdf_state(p.ms_pdf[k], w); }
+        for (int k = 0; k < p.ms_npdf; ++k) {
+            if (user_pdf(p.ms_pdf[k])) {
+                user_init(p.ms_pdf[k], w, this->mpo + k * MP, this->mpn + k * MP);
+                sp[k] = user_value(p.ms_pdf[k], this->mpo + k * MP);
+            } else {
+                sp[k] = pdf_state(p.ms_pdf[k], w);
+            }
+        }
         R oldv;
         if constexpr (EXACT) {
             oldv = 1.;
-            for (int k = 0; k < p.ms_npdf; ++k) { oldv *= pdf_value_d(p, p.ms_pdf[k], w, sp[k]); }
+            for (int k = 0; k < p.ms_npdf; ++k) {
+                oldv *= user_pdf(p.ms_pdf[k]) ? sp[k] : pdf_value_d(p, p.ms_pdf[k], w, sp[k]);
+            }
         } else {
             oldv = 0.f;
             for (int k = 0; k < p.ms_npdf; ++k) { oldv += sp[k]; }
@@ -478,6 +542,11 @@ struct GenericSampler {
                 double a = 1.;
                 const bool partial = p.ms_veclen < p.ndim;
                 for (int k = 0; k < p.ms_npdf; ++k) {
+                    if (user_pdf(p.ms_pdf[k])) {
+                        a *= user_accept(p.ms_pdf[k], w, xn, partial, lo, hi, this->mpo + k * MP, this->mpn + k * MP);
+                        spn[k] = sp[k];
+                        continue;
+                    }
                     double pn = 0.;
                     a *= pdf_accept_d(p, p.ms_pdf[k], w, xn, partial, lo, hi, sp[k], pn);
                     spn[k] = pn;
@@ -485,9 +554,12 @@ struct GenericSampler {
                 acc = (accept_u(1 + s) <= a * 1.);
             } else {
                 float dl = 0.f;
+                const bool partial = p.ms_veclen < p.ndim;
                 for (int k = 0; k < p.ms_npdf; ++k) {
                     float delta;
-                    if (!pdf_delta_f(p.ms_pdf[k], w, xn, lo, hi, delta)) {
+                    if (user_pdf(p.ms_pdf[k])) {
+                        delta = logf(user_accept(p.ms_pdf[k], w, xn, partial, lo, hi, this->mpo + k * MP, this->mpn + k * MP));
+                    } else if (!pdf_delta_f(p.ms_pdf[k], w, xn, lo, hi, delta)) {
                         delta = pdf_logp_f(p, p.ms_pdf[k], xn, blob) - sp[k];
                     }
                     spn[k] = sp[k] + delta;
@@ -501,15 +573,27 @@ struct GenericSampler {
             } else {
                 for (int i = lo; i < hi; ++i) { xn[i] = w[i]; }
             }
+            if constexpr (USER_PDF) {
+                for (int k = 0; k < p.ms_npdf; ++k) {
+                    if (!user_pdf(p.ms_pdf[k])) { continue; }
+                    if (acc) { copy_protos(this->mpn + k * MP, this->mpo + k * MP, p.ms_pdf[k].nproto); }
+                    else { copy_protos(this->mpo + k * MP, this->mpn + k * MP, p.ms_pdf[k].nproto); }
+                }
+            }
         }
         // xn == w: the end point of the sub-chain
         if constexpr (EXACT) {
             double newv = 1.;
-            for (int k = 0; k < p.ms_npdf; ++k) { newv *= pdf_value_d(p, p.ms_pdf[k], w, sp[k]); }
+            for (int k = 0; k < p.ms_npdf; ++k) {
+                newv *= user_pdf(p.ms_pdf[k]) ? user_value(p.ms_pdf[k], this->mpo + k * MP)
+                                              : pdf_value_d(p, p.ms_pdf[k], w, sp[k]);
+            }
             return oldv / newv;
         } else {
             float newv = 0.f;
-            for (int k = 0; k < p.ms_npdf; ++k) { newv += sp[k]; }
+            for (int k = 0; k < p.ms_npdf; ++k) {
+                newv += user_pdf(p.ms_pdf[k]) ? user_value(p.ms_pdf[k], this->mpo + k * MP) : sp[k];
+            }
             return oldv - newv;
         }
     }
@@ -539,13 +623,19 @@ struct GenericSampler {
             double a = 1.;
             for (int k = 0; k < p.npdf; ++k) {
                 double pn = lp[k];
-                a *= pdf_accept_d(p, p.pdf[k], x, xn, partial, lo, hi, lp[k], pn);
+                if (user_pdf(p.pdf[k])) { a *= user_accept(p.pdf[k], x, xn, partial, lo, hi, this->upo + k * MP, this->upn + k * MP); }
+                else { a *= pdf_accept_d(p, p.pdf[k], x, xn, partial, lo, hi, lp[k], pn); }
                 lpn[k] = pn;
             }
             acc = (accept_u(0) <= a * moveAcc);
         } else {
             float dl = moveAcc;
             for (int k = 0; k < p.npdf; ++k) {
+                if (user_pdf(p.pdf[k])) {
+                    lpn[k] = lp[k];
+                    dl += logf(user_accept(p.pdf[k], x, xn, partial, lo, hi, this->upo + k * MP, this->upn + k * MP));
+                    continue;
+                }
                 lpn[k] = pdf_logp_f(p, p.pdf[k], xn, blob);
                 dl += lpn[k] - lp[k];
             }
@@ -554,6 +644,13 @@ struct GenericSampler {
         if (acc) {
             for (int i = lo; i < hi; ++i) { x[i] = xn[i]; }
             for (int k = 0; k < p.npdf; ++k) { lp[k] = lpn[k]; }
+        }
+        if constexpr (USER_PDF) { // newToOld / oldToNew (ProtoFunctionInterface.cpp:46-56)
+            for (int k = 0; k < p.npdf; ++k) {
+                if (!user_pdf(p.pdf[k])) { continue; }
+                if (acc) { copy_protos(this->upn + k * MP, this->upo + k * MP, p.pdf[k].nproto); }
+                else { copy_protos(this->upo + k * MP, this->upn + k * MP, p.pdf[k].nproto); }
+            }
         }
         end_step();
         return acc;
@@ -637,7 +734,8 @@ struct GenericSampler {
                 if (skipleft[o] > 0) { --skipleft[o]; continue; } // accumulate when nskip divides r
                 skipleft[o] = od.nskip - 1;
                 const int64_t k = kacc[o]++; // accumulation index r / nskip
-                obs_eval<R>(p, od, x, vals, blob);
+                if (user_obs(od)) { U::observe(od.kind - MCIG_OBS_USER, uargs(od.poff, od.np), (const R *)x, vals); }
+                else { obs_eval<R>(p, od, x, vals, blob); }
                 if (od.acc == MCIG_ACC_FULL) { // FullAccumulator::_accumulate (FullAccumulator.cpp:14-18)
                     const size_t row = (size_t)(p.acc_offset + k);
                     if (od.full32) {
@@ -709,7 +807,7 @@ struct GenericSampler {
     }
 };
 
-template <class R, int RNG, bool KAHAN>
+template <class R, int RNG, bool KAHAN, class U = mcig::NoPlugin>
 __global__ void __launch_bounds__(128) mcig_generic_kernel(const KParams p, int movetype)
 {
     extern __shared__ float smem_blob[];
@@ -718,7 +816,7 @@ __global__ void __launch_bounds__(128) mcig_generic_kernel(const KParams p, int 
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    GenericSampler<R, RNG, KAHAN> s(p, c, smem_blob);
+    GenericSampler<R, RNG, KAHAN, U> s(p, c, smem_blob);
     if (p.mode == KMODE_CALIB) { s.run_calibration(movetype, p.nsteps); }
     else if (p.mode == KMODE_SAMPLE) { s.run_sample(movetype, p.nsteps); }
     else { s.run_steps(movetype, p.nsteps); }

@@ -14,3 +14,10 @@ mcig_launch_fn mcig_generic_launcher(int precision, int rng);
 // maxd 4, 8, 16 or 32, pdf set pk (PK_ANY, or PK_GAUSS / PK_PREC / PK_MIX for a single
 // sampling function of that kind); NULL otherwise
 mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk);
+
+// general kernel of a plugin (include/mcig/plugin.cuh) over its user functors: launches and
+// returns the launch's cudaError_t of the plugin's own CUDA runtime
+typedef int (*mcig_plugin_launch_fn)(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st);
+
+// interface version of plugins against this library (with sizeof(KParams))
+#define MCIG_PLUGIN_ABI 1

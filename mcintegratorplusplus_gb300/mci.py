@@ -11,7 +11,8 @@ Differences from the reference, by design of the device path:
   * one object holds `nchains` independent chains (one per GPU thread);
     integrate() combines them with the MPIMCI formula (src/MPIMCI.cpp:85-92);
   * sampling functions and observables are device functors chosen by kind
-    (include/mcig_types.h) instead of virtual C++ objects;
+    (include/mcig_types.h) instead of virtual C++ objects; user functors are
+    structs compiled into a plugin (include/mcig/plugin.cuh, Plugin below);
   * the seed keys a Philox4x32-10 stream instead of std::mt19937_64 (replay
     mode consumes the reference's recorded draws instead).
 """
@@ -32,6 +33,7 @@ EST_NOOP, EST_UNCORRELATED, EST_CORRELATED, EST_FCBLOCKER, EST_MJBLOCKER = range
 PDF_GAUSS_SUM, PDF_GAUSS, PDF_EXP, PDF_GAUSS_PREC, PDF_GAUSS_BLOCK, PDF_GAUSS_MIX = range(6)
 OBS_X2SUM, OBS_XND, OBS_X2, OBS_X2MEAN, OBS_CONST, OBS_POLYNOM, OBS_X2BLOCK, OBS_GAUSSX2, OBS_XI, OBS_LOGPDF = range(10)
 PREC_FP64, PREC_FP32, PREC_FP32_ACC64 = range(3)
+PDF_USER, OBS_USER = 100, 100  # + k: the k-th sampling function / observable of the handle's plugin
 
 
 class DomainError(ValueError):
@@ -94,6 +96,11 @@ class MCI:
         except Exception:
             pass
 
+    def setPlugin(self, plugin):
+        """Attach a Plugin whose kinds PDF_USER + k / OBS_USER + k this MCI may use (None detaches)."""
+        _raise(self.L.mcig_set_plugin(self._h, plugin._h if plugin is not None else None))
+        self._plugin = plugin  # kept alive while the handle may use it
+
     # --- setters (MCIntegrator.hpp:96-123)
     def setSeed(self, seed):
         _raise(self.L.mcig_set_seed(self._h, ctypes.c_uint64(int(seed) & ((1 << 64) - 1))))
@@ -101,6 +108,10 @@ class MCI:
     def setKernel(self, policy):
         """0 automatic, 1 general kernel, 2 register-resident float kernel."""
         _raise(self.L.mcig_set_kernel(self._h, int(policy)))
+
+    def setPhaseFusion(self, on=True):
+        """Calibration, burn-in and sampling in one register-resident launch where it applies (default on)."""
+        _raise(self.L.mcig_set_phase_fusion(self._h, int(bool(on))))
 
     def setPrecision(self, precision):
         _raise(self.L.mcig_set_precision(self._h, int(precision)))
@@ -406,6 +417,29 @@ def integrate_flow(m, flow, nmc, period=5, refresh=0, train_steps=400, batch=204
                                    float(lr), _dp(avg), _dp(err), int(bool(doFindMRT2step)), int(bool(doDecorrelation)),
                                    ctypes.byref(acc)))
     return avg[:m.getNObsDim()], err[:m.getNObsDim()], acc.value
+
+
+class Plugin:
+    """User sampling functions and observables compiled for the device: a shared library
+    built from a source that ends with MCIG_PLUGIN (include/mcig/plugin.cuh), e.g. with
+    mcintegratorplusplus_gb300.build.build_plugin."""
+
+    def __init__(self, path):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        _raise(self.L.mcig_plugin_load(str(path).encode(), ctypes.byref(h)))
+        self._h = h
+        npdf, nobs = ctypes.c_int(), ctypes.c_int()
+        _raise(self.L.mcig_plugin_counts(self._h, ctypes.byref(npdf), ctypes.byref(nobs)))
+        self.npdf, self.nobs = npdf.value, nobs.value
+
+    def pdf(self, k):
+        """kind of the k-th sampling function"""
+        return PDF_USER + int(k)
+
+    def obs(self, k):
+        """kind of the k-th observable"""
+        return OBS_USER + int(k)
 
 
 class Batch:

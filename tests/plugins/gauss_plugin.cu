@@ -1,0 +1,108 @@
+// Test plugin: user functors written the way a user of the reference writes
+// SamplingFunctionInterface / ObservableFunctionInterface classes, with the arithmetic of the
+// reference's test classes (test/common/TestMCIFunctions.hpp), so that integrals with them equal
+// integrals with the built-in kinds bit for bit.
+#include <mcig/plugin.cuh>
+
+// exp(-sum_i x_i^2) with one proto value per index (Gauss, TestMCIFunctions.hpp:151-190)
+struct IndexGauss {
+    static constexpr int max_nproto = 64;
+    static int nproto(int ndim) { return ndim; }
+    template <class R> __device__ static void protoFunction(const mcig::UserArgs &a, const R *in, R *pv)
+    {
+        for (int i = 0; i < a.ndim; ++i) { pv[i] = in[i] * in[i]; }
+    }
+    template <class R> __device__ static R samplingFunction(const mcig::UserArgs &a, const R *pv)
+    {
+        R s = (R)0;
+        for (int i = 0; i < a.ndim; ++i) { s = s + pv[i]; }
+        return exp(-s);
+    }
+    template <class R> __device__ static R acceptanceFunction(const mcig::UserArgs &a, const R *po, const R *pn)
+    {
+        R e = (R)0;
+        for (int i = 0; i < a.ndim; ++i) { e = e + po[i]; }
+        R f = (R)0;
+        for (int i = 0; i < a.ndim; ++i) { f = f + pn[i]; }
+        e = e - f;
+        return exp(e);
+    }
+    template <class R>
+    __device__ static R updatedAcceptance(const mcig::UserArgs &, const mcig::UserWalker<R> &w, const R *po, R *pn)
+    {
+        R e = (R)0;
+        for (int i = w.lo; i < w.lo + w.nchanged; ++i) {
+            pn[i] = w.xnew[i] * w.xnew[i];
+            e = e + (pn[i] - po[i]);
+        }
+        return exp(-e);
+    }
+};
+
+// exp(-sum_i x_i^2) with a single proto value (ThreeDimGaussianPDF, :123-148, any ndim);
+// no updatedAcceptance: partial moves recompute the proto value
+struct SumGauss {
+    static constexpr int max_nproto = 1;
+    static int nproto(int) { return 1; }
+    template <class R> __device__ static void protoFunction(const mcig::UserArgs &a, const R *in, R *pv)
+    {
+        R s = in[0] * in[0];
+        for (int i = 1; i < a.ndim; ++i) { s = s + in[i] * in[i]; }
+        pv[0] = s;
+    }
+    template <class R> __device__ static R samplingFunction(const mcig::UserArgs &, const R *pv) { return exp(-pv[0]); }
+    template <class R> __device__ static R acceptanceFunction(const mcig::UserArgs &, const R *po, const R *pn)
+    {
+        return exp(-pn[0] + po[0]);
+    }
+};
+
+// exp(-c sum_{b0<=i<b1} x_i^2), parameters [b0, b1, c]
+struct ScaledBlockGauss {
+    static constexpr int max_nproto = 1;
+    static int nproto(int) { return 1; }
+    template <class R> __device__ static void protoFunction(const mcig::UserArgs &a, const R *in, R *pv)
+    {
+        R s = (R)0;
+        for (int i = (int)a.params[0]; i < (int)a.params[1]; ++i) { s = s + in[i] * in[i]; }
+        pv[0] = s * (R)a.params[2];
+    }
+    template <class R> __device__ static R samplingFunction(const mcig::UserArgs &, const R *pv) { return exp(-pv[0]); }
+    template <class R> __device__ static R acceptanceFunction(const mcig::UserArgs &, const R *po, const R *pn)
+    {
+        return exp(-pn[0] + po[0]);
+    }
+};
+
+// sum_i x_i^2 (X2Sum, :415-433)
+struct SquaredNorm {
+    static int nobs(int) { return 1; }
+    template <class R> __device__ static void observableFunction(const mcig::UserArgs &a, const R *in, R *out)
+    {
+        R s = (R)0;
+        for (int i = 0; i < a.ndim; ++i) { s = s + in[i] * in[i]; }
+        out[0] = s;
+    }
+};
+
+// x_i (XND, :335-350)
+struct Position {
+    static int nobs(int ndim) { return ndim; }
+    template <class R> __device__ static void observableFunction(const mcig::UserArgs &a, const R *in, R *out)
+    {
+        for (int i = 0; i < a.ndim; ++i) { out[i] = in[i]; }
+    }
+};
+
+// x_i + params[0]: an observable with a parameter
+struct ShiftedPosition {
+    static int nobs(int ndim) { return ndim; }
+    template <class R> __device__ static void observableFunction(const mcig::UserArgs &a, const R *in, R *out)
+    {
+        for (int i = 0; i < a.ndim; ++i) { out[i] = in[i] + (R)a.params[0]; }
+    }
+};
+
+using TestPdfs = mcig::PdfList<IndexGauss, SumGauss, ScaledBlockGauss>;
+using TestObss = mcig::ObsList<SquaredNorm, Position, ShiftedPosition>;
+MCIG_PLUGIN(TestPdfs, TestObss)

@@ -59,3 +59,34 @@ def test_fast_and_general_kernel_accumulate_alike():
         same = np.all(np.abs(fa - fb) < 1e-4 * (1 + np.abs(fb)), axis=(1, 2))
         assert same.mean() > 0.9, same.mean()
         np.testing.assert_allclose(ba[same], bb[same], rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.parametrize("prec", ["PREC_FP32", "PREC_FP32_ACC64"])
+def test_phase_fusion_equals_separate_launches(prec):
+    """Calibration, burn-in and sampling of every chain in one launch give the results of the
+    three launches: estimates, step sizes, walkers, counts and the accumulated data."""
+    import mcintegratorplusplus_gb300 as mcig
+    rng = np.random.default_rng(4)
+    q, _ = np.linalg.qr(rng.normal(size=(16, 16)))
+    P = q @ np.diag(10.0 ** rng.uniform(-1, 1, 16)) @ q.T
+
+    def go(fuse):
+        m = mcig.MCI(16, 2048, precision=getattr(mcig, prec))
+        m.setSeed(21)
+        m.setPhaseFusion(fuse)
+        m.addSamplingFunction(mcig.PDF_GAUSS_PREC, P.ravel())
+        m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+        m.setNdecorrelationSteps(300)
+        m.addObservable(mcig.OBS_X2SUM, (), 16, 1, True, mcig.EST_UNCORRELATED)
+        m.addObservable(mcig.OBS_XND, (), 1, 1, False, mcig.EST_MJBLOCKER)
+        avg, err = m.integrate(2048)
+        ms = m.getLastTimings()
+        return dict(avg=avg, err=err, steps=m.getMRT2Steps(), x=m.getX(), counts=m.getCounts(),
+                    d0=m.getObsData(0), d1=m.getObsData(1), ms=ms)
+
+    a, b = go(True), go(False)
+    for k in ("avg", "err", "steps", "x", "d0", "d1"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    for u, v in zip(a["counts"], b["counts"]):
+        np.testing.assert_array_equal(u, v)
+    assert a["ms"]["launches"] < b["ms"]["launches"] and a["ms"]["calibration_ms"] < 0.05

@@ -1,0 +1,227 @@
+"""User functors compiled as a plugin (include/mcig/plugin.cuh, tests/plugins/gauss_plugin.cu):
+the plugin builds and loads; integrals with its functors equal integrals with the built-in kinds
+of the same arithmetic bit for bit (double path), reproduce the oracle's run under replay, and
+agree statistically on the float paths; what the plugin kernel does not serve is an error."""
+import ctypes
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+import cases
+from oracle import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "plugins", "gauss_plugin.cu")
+OUT = os.path.join(HERE, "plugins", "_build", "gauss_plugin.so")
+
+# kinds of the test plugin
+IDX_GAUSS, SUM_GAUSS, BLOCK_GAUSS = 0, 1, 2
+SQNORM, POSITION, SHIFTED = 0, 1, 2
+
+
+@pytest.fixture(scope="module")
+def plugin_path():
+    if not shutil.which("nvcc") and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("nvcc is not available")
+    from mcintegratorplusplus_gb300 import build
+    return build.build_plugin(SRC, OUT)
+
+
+def test_plugin_exports_and_loads(plugin_path):
+    """The plugin's entry points answer without a GPU; the library accepts it and refuses a
+    library that is not a plugin."""
+    P = ctypes.CDLL(plugin_path)
+    assert P.mcig_plugin_abi() == 1
+    assert P.mcig_plugin_npdf() == 3 and P.mcig_plugin_nobs() == 3
+    assert P.mcig_plugin_pdf_nproto(IDX_GAUSS, 5) == 5
+    assert P.mcig_plugin_pdf_nproto(IDX_GAUSS, 65) == -1  # above max_nproto
+    assert P.mcig_plugin_pdf_nproto(SUM_GAUSS, 40) == 1
+    assert P.mcig_plugin_obs_nvals(POSITION, 7) == 7 and P.mcig_plugin_obs_nvals(SQNORM, 7) == 1
+    import mcintegratorplusplus_gb300 as mcig
+    pl = mcig.Plugin(plugin_path)
+    assert (pl.npdf, pl.nobs) == (3, 3)
+    assert pl.pdf(2) == mcig.PDF_USER + 2 and pl.obs(1) == mcig.OBS_USER + 1
+    from mcintegratorplusplus_gb300 import _lib
+    with pytest.raises(ValueError, match="plugin"):
+        mcig.Plugin(_lib.lib_path())
+
+
+@pytest.fixture(scope="module")
+def mcig():
+    import mcintegratorplusplus_gb300 as m
+    return m
+
+
+@pytest.fixture(scope="module")
+def plugin(mcig, plugin_path):
+    return mcig.Plugin(plugin_path)
+
+
+def _run(mcig, plugin, ndim, nchains, prec, move, pdfs, obs, ms=None, seed=77, nmc=4096, ndecorr=200):
+    m = mcig.MCI(ndim, nchains, precision=prec)
+    m.setPlugin(plugin)
+    m.setSeed(seed)
+    m.setTrialMove(*move)
+    for kind, par in pdfs:
+        m.addSamplingFunction(kind, par)
+    if ms is not None:
+        nsub, subpdfs = ms
+        m.setMultiStepMove(nsub, mcig.SRRD_UNIFORM, 1, 0.6)
+        for kind, par in subpdfs:
+            m.addMultiStepSamplingFunction(kind, par)
+    for kind, par, bs, nskip, est in obs:
+        m.addObservable(kind, par, bs, nskip, bs > 0, est)
+    m.setNdecorrelationSteps(ndecorr)
+    avg, err = m.integrate(nmc)
+    data = [m.getObsData(o) for o in range(len(obs))]
+    return dict(avg=avg, err=err, acc=m.getAcceptanceRate(), data=data, steps=m.getMRT2Steps(),
+                chains=m.getChainResults(), x=m.getX())
+
+
+def _assert_same(a, b):
+    np.testing.assert_array_equal(a["avg"], b["avg"])
+    np.testing.assert_array_equal(a["err"], b["err"])
+    np.testing.assert_array_equal(a["steps"], b["steps"])
+    np.testing.assert_array_equal(a["x"], b["x"])
+    assert a["acc"] == b["acc"]
+    for u, v in zip(a["data"], b["data"]):
+        np.testing.assert_array_equal(u, v)
+
+
+@pytest.mark.gpu
+def test_vec_move_updated_acceptance_equals_builtin_gauss(mcig, plugin):
+    """One proto value per index with updatedAcceptance under single-coordinate moves (the
+    partial path) against the built-in Gauss kind; Block and Full (nskip 2) accumulators."""
+    move = (mcig.MOVE_VEC, mcig.SRRD_UNIFORM, 1)
+    E = mcig.EST_UNCORRELATED, mcig.EST_CORRELATED
+    u = _run(mcig, plugin, 5, 64, mcig.PREC_FP64, move, [(plugin.pdf(IDX_GAUSS), ())],
+             [(plugin.obs(SQNORM), (), 16, 1, E[0]), (plugin.obs(POSITION), (), 1, 2, E[1])])
+    b = _run(mcig, plugin, 5, 64, mcig.PREC_FP64, move, [(mcig.PDF_GAUSS, ())],
+             [(mcig.OBS_X2SUM, (), 16, 1, E[0]), (mcig.OBS_XND, (), 1, 2, E[1])])
+    _assert_same(u, b)
+    assert 0.3 < u["acc"] < 0.7
+
+
+@pytest.mark.gpu
+def test_all_move_two_pdfs_with_parameters_equal_builtin(mcig, plugin):
+    """A product of two user sampling functions, one with parameters, under all-moves; a user
+    observable with a parameter against its built-in counterpart plus the shift."""
+    move = (mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+    u = _run(mcig, plugin, 4, 128, mcig.PREC_FP64, move,
+             [(plugin.pdf(SUM_GAUSS), ()), (plugin.pdf(BLOCK_GAUSS), (0, 2, 0.5))],
+             [(plugin.obs(SQNORM), (), 32, 1, mcig.EST_MJBLOCKER), (plugin.obs(SHIFTED), (0.25,), 0, 1, mcig.EST_NOOP)])
+    b = _run(mcig, plugin, 4, 128, mcig.PREC_FP64, move,
+             [(mcig.PDF_GAUSS_SUM, ()), (mcig.PDF_GAUSS_BLOCK, (0, 2, 1.0))],  # 0.5 / 1.0^2 = 0.5
+             [(mcig.OBS_X2SUM, (), 32, 1, mcig.EST_MJBLOCKER), (mcig.OBS_XND, (), 0, 1, mcig.EST_NOOP)])
+    np.testing.assert_array_equal(u["avg"][:1], b["avg"][:1])
+    np.testing.assert_array_equal(u["err"][:1], b["err"][:1])
+    np.testing.assert_array_equal(u["steps"], b["steps"])
+    np.testing.assert_array_equal(u["x"], b["x"])
+    np.testing.assert_allclose(u["avg"][1:], b["avg"][1:] + 0.25, rtol=0, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_multistep_move_with_user_sub_pdfs_equals_builtin(mcig, plugin):
+    """MultiStepMove whose sub-chain runs on user sampling functions (protos kept across the
+    sub-steps, newToOld / oldToNew) inside a chain on a user sampling function."""
+    move = (mcig.MOVE_ALL, mcig.SRRD_UNIFORM)
+    obs = [(mcig.OBS_X2SUM, (), 16, 1, mcig.EST_UNCORRELATED)]
+    u = _run(mcig, plugin, 5, 64, mcig.PREC_FP64, move, [(plugin.pdf(IDX_GAUSS), ())], obs,
+             ms=(4, [(plugin.pdf(BLOCK_GAUSS), (0, 2, 0.5)), (plugin.pdf(BLOCK_GAUSS), (2, 5, 0.5))]), nmc=2048)
+    b = _run(mcig, plugin, 5, 64, mcig.PREC_FP64, move, [(mcig.PDF_GAUSS, ())], obs,
+             ms=(4, [(mcig.PDF_GAUSS_BLOCK, (0, 2, 1.0)), (mcig.PDF_GAUSS_BLOCK, (2, 5, 1.0))]), nmc=2048)
+    _assert_same(u, b)
+
+
+@pytest.mark.gpu
+def test_replay_with_user_functors_reproduces_oracle(mcig, plugin):
+    """Replaying the oracle's recorded draws, the user Gauss and observable reproduce the
+    oracle's run of the reference's Gauss and X2Sum."""
+    seeds = [3, 5]
+    m = orc.OracleMCI(3, len(seeds))
+    m.set_seeds(seeds)
+    m.set_trial_move(cases.MOVE_VEC, cases.SRRD_UNIFORM, 1)
+    m.add_sampling_function(cases.PDF_GAUSS)
+    m.add_observable(cases.OBS_X2SUM, (), 8, 1, True, cases.EST_UNCORRELATED)
+    m.set_ndecorrelation_steps(100)
+    m.set_record(True)
+    m.integrate(0, True, True)
+    avg, err, ca, ce = m.integrate(4096, False, False, per_chain=True)
+    tape, lens = m.get_tapes()
+    g = mcig.MCI(3, len(seeds), precision=mcig.PREC_FP64)
+    g.setPlugin(plugin)
+    g.setTrialMove(mcig.MOVE_VEC, mcig.SRRD_UNIFORM, 1)
+    g.addSamplingFunction(plugin.pdf(IDX_GAUSS))
+    g.addObservable(plugin.obs(SQNORM), (), 8, 1, True, mcig.EST_UNCORRELATED)
+    g.setNdecorrelationSteps(100)
+    g.setReplay(tape, lens)
+    g.integrate(0, True, True)
+    gavg, gerr = g.integrate(4096, False, False)
+    gca, gce = g.getChainResults()
+    np.testing.assert_allclose(gca, ca, rtol=1e-12)
+    np.testing.assert_allclose(gce, ce, rtol=1e-12)
+    np.testing.assert_allclose(gavg, avg, rtol=1e-12)
+    np.testing.assert_allclose(gerr, err, rtol=1e-12)
+    a, _ = g.getCounts()
+    oa, _ = m.counts()
+    np.testing.assert_array_equal(a, oa)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["PREC_FP32", "PREC_FP32_ACC64"])
+def test_float_paths_agree_with_builtin_and_analytic(mcig, plugin, prec):
+    """Float walker: the log of the user acceptance ratio in the Metropolis test.  <sum x^2> of
+    exp(-sum x^2) is ndim / 2."""
+    p = getattr(mcig, prec)
+    move = (mcig.MOVE_VEC, mcig.SRRD_UNIFORM, 2)
+    ndim = 8
+    u = _run(mcig, plugin, ndim, 2048, p, move, [(plugin.pdf(IDX_GAUSS), ())],
+             [(plugin.obs(SQNORM), (), 32, 1, mcig.EST_UNCORRELATED)], nmc=4096, ndecorr=500)
+    b = _run(mcig, plugin, ndim, 2048, p, move, [(mcig.PDF_GAUSS, ())],
+             [(mcig.OBS_X2SUM, (), 32, 1, mcig.EST_UNCORRELATED)], nmc=4096, ndecorr=500, seed=78)
+    for r in (u, b):
+        assert abs(r["avg"][0] - ndim / 2) < 5 * r["err"][0], (r["avg"], r["err"])
+    assert abs(u["avg"][0] - b["avg"][0]) < 5 * np.hypot(u["err"][0], b["err"][0])
+    assert abs(u["acc"] - b["acc"]) < 0.01
+
+
+@pytest.mark.gpu
+def test_plugin_errors(mcig, plugin):
+    m = mcig.MCI(3, 4, precision=mcig.PREC_FP64)
+    with pytest.raises(ValueError, match="no plugin"):
+        m.addSamplingFunction(mcig.PDF_USER)
+    with pytest.raises(ValueError, match="no plugin"):
+        m.addObservable(mcig.OBS_USER, (), 1, 1, False, mcig.EST_CORRELATED)
+    m.setPlugin(plugin)
+    with pytest.raises(ValueError, match="sampling functions"):
+        m.addSamplingFunction(plugin.pdf(3))
+    with pytest.raises(ValueError, match="observables"):
+        m.addObservable(plugin.obs(7), (), 1, 1, False, mcig.EST_CORRELATED)
+    m64 = mcig.MCI(64, 1)  # nproto(64) is at max_nproto: accepted
+    m64.setPlugin(plugin)
+    m64.addSamplingFunction(plugin.pdf(IDX_GAUSS))
+    m.addSamplingFunction(plugin.pdf(IDX_GAUSS))
+    m.addObservable(mcig.OBS_LOGPDF, (), 0, 1, False, mcig.EST_NOOP)
+    with pytest.raises(NotImplementedError, match="LOGPDF"):
+        m.integrate(64)
+    m.popObservable()
+    m.addObservable(plugin.obs(SQNORM), (), 0, 1, False, mcig.EST_NOOP)
+    with pytest.raises(ValueError, match="plugin kinds"):
+        m.setPlugin(None)
+    m.setKernel(2)
+    with pytest.raises(NotImplementedError):
+        m.integrate(64)
+    m.setKernel(0)
+    m.integrate(64)
+    f = mcig.MCI(4, 4, precision=mcig.PREC_FP32)
+    f.setPlugin(plugin)
+    f.addSamplingFunction(plugin.pdf(SUM_GAUSS))
+    f.addObservable(mcig.OBS_X2SUM, (), 16, 1, True, mcig.EST_UNCORRELATED)
+    f.setNdecorrelationSteps(10)
+    with pytest.raises(NotImplementedError, match="batch"):
+        mcig.Batch([f], 256)
+    fl = mcig.Flow(4, nlayers=2)
+    with pytest.raises(NotImplementedError, match="built-in"):
+        mcig.integrate_flow(f, fl, 64)

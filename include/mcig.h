@@ -57,12 +57,23 @@ void *mcig_get_stream(const mcig_mci *h);
  * else the general kernel), 1 general kernel, 2 register-resident kernel
  * (MCIG_ERR_UNSUPPORTED at integrate when the configuration needs the general one). */
 int mcig_set_kernel(mcig_mci *h, int policy);
-/* Phase fusion (default on): where the register-resident kernel serves calibration, a fixed
+/* Phase fusion (default off): where the register-resident kernel serves calibration, a fixed
  * burn-in and the sampling (no file output, no accept recording), integrate runs the three
  * phases of every chain in one launch, so chains whose step calibration converges early
  * sample while the others still calibrate.  Results are those of separate launches; the
- * timings then report the whole launch as sampling time.  0 turns it off. */
+ * timings then report the whole launch as sampling time.  Off by default: when a few chains
+ * calibrate for many iterations, their calibration competes with the other chains' sampling
+ * for instruction issue and then their own sampling ends the launch late (65,536 chains of a
+ * 16-D correlated Gaussian: 66.3 ms fused against 58.5 ms for the three launches). */
 int mcig_set_phase_fusion(mcig_mci *h, int on);
+/* Split calibration tail (default on): where the register-resident kernel calibrates an
+ * all-coordinate move with one step-size type, no periodic domain, ndim 9..16 and one exp(-x.x)
+ * or precision-matrix sampling function, the chains still calibrating when at most 8 of
+ * their warp's 32 remain continue on 4 lanes each (4 coordinates per lane, the proposal
+ * exchanged by warp shuffles).  Step sizes, walkers and counts are identical to the one-lane
+ * calibration; only the time changes.  0 turns it off.  No counterpart in the reference,
+ * whose MCI::findMRT2Step (src/MCIntegrator.cpp:87-168) calibrates one chain. */
+int mcig_set_calibration_split(mcig_mci *h, int on);
 
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
  * from counter (step, c).  */

@@ -32,6 +32,7 @@ SIGNATURES = {
     "mcig_get_stream": (c_void_p, [c_void_p]),
     "mcig_set_kernel": (c_int, [c_void_p, c_int]),
     "mcig_set_phase_fusion": (c_int, [c_void_p, c_int]),
+    "mcig_set_calibration_split": (c_int, [c_void_p, c_int]),
     "mcig_set_seed": (c_int, [c_void_p, ctypes.c_uint64]),
     "mcig_set_x": (c_int, [c_void_p, P_double, c_int64]),
     "mcig_get_x": (c_int, [c_void_p, P_double]),

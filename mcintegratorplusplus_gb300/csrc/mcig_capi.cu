@@ -127,7 +127,8 @@ struct mcig_mci {
     int64_t ndecorr = -10000;
     int full32 = 0;
     int kernel_policy = 0; // 0 auto, 1 general kernel, 2 register-resident kernel
-    int fuse_phases = 1;   // calibration, burn-in and sampling in one register-resident launch
+    int fuse_phases = 0;   // 1: calibration, burn-in and sampling in one register-resident launch
+    int calib_split = 1;   // calibration's tail split over lanes where mcig_calib.cuh serves it
     FastConst fc;          // constant data of the register-resident kernel
     // device chain state
     DBuf<double> x, step;
@@ -1053,6 +1054,11 @@ static int launch(mcig_mci *h, const KParams &kp)
         }
         fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk);
         smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
+        if (kp.mode == KMODE_CALIB && h->calib_split && h->movetype == MCIG_MOVE_ALL && maxd_bucket(h->ndim) == 16 &&
+            h->ntypes == 1 && !h->periodic && (pk == 1 || pk == 2)) { // PK_GAUSS, PK_PREC
+            fn = mcig_calib_launcher_pk16(pk); // same results, the tail's chains on four lanes each
+            smem = 0;
+        }
     } else if (uses_plugin(h)) { // the plugin's general kernel over its functors
         mcig_plugin_launch_fn pf = h->plugin ? h->plugin->launcher(h->prec, h->replay ? RNG_TAPE : RNG_PHILOX) : nullptr;
         if (!pf) { return set_err(MCIG_ERR_UNSUPPORTED, "the plugin has no kernel for this precision"); }
@@ -1074,6 +1080,13 @@ extern "C" int mcig_set_phase_fusion(mcig_mci *h, int on)
 {
     if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
     h->fuse_phases = on ? 1 : 0;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_calibration_split(mcig_mci *h, int on)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    h->calib_split = on ? 1 : 0;
     return MCIG_OK;
 }
 

@@ -33,6 +33,16 @@
 // issue all of them)
 enum { PK_ANY = 0, PK_GAUSS = 1, PK_PREC = 2, PK_MIX = 3 };
 
+// The last operations of the precision-matrix log density and of the Metropolis test in
+// round-to-nearest intrinsics, which the compiler never contracts into an FMA: the split
+// calibration (mcig_calib.cuh) evaluates them from the same operands in another context
+// and must round them alike.
+__device__ __forceinline__ float fast_lp_of_q(float q) { return __fmul_rn(-0.5f, q); }
+__device__ __forceinline__ bool fast_accept(float u, float lpn, float lp)
+{ // log2(u) <= (log p(x') - log p(x)) log2(e)
+    return __log2f(u) <= __fmul_rn(__fsub_rn(lpn, lp), 1.44269504f);
+}
+
 template <int MAXD>
 __device__ __forceinline__ float fast_logp_prec(const FastConst &fc, const float *x)
 { // -|U x|^2 / 2, U upper triangular at fconst[0], row stride MAXD
@@ -44,7 +54,7 @@ __device__ __forceinline__ float fast_logp_prec(const FastConst &fc, const float
         for (int j = i; j < MAXD; ++j) { t = fmaf(fc.fconst[i * MAXD + j], x[j], t); }
         q = fmaf(t, t, q);
     }
-    return -0.5f * q;
+    return fast_lp_of_q(q);
 }
 
 template <int MAXD>
@@ -239,7 +249,7 @@ struct FastSampler {
         }
         const float lpn = fast_logp<MAXD, PK>(p, fc, xn);
         const float u = u01_f(block(TAG_ACCEPT, 0).a);
-        const bool acc = __log2f(u) <= (lpn - lp) * 1.44269504f;
+        const bool acc = fast_accept(u, lpn, lp);
         if (acc) {
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) { x[i] = xn[i]; }

@@ -15,6 +15,11 @@ mcig_launch_fn mcig_generic_launcher(int precision, int rng);
 // sampling function of that kind); NULL otherwise
 mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk);
 
+// step-size calibration (KMODE_CALIB) with the calibration's tail split over lanes
+// (mcig_calib.cuh): all-coordinate move, one step type, no periodic domain, ndim 9..16,
+// one sampling function of kind pk (PK_GAUSS or PK_PREC); NULL otherwise
+mcig_launch_fn mcig_calib_launcher_pk16(int pk);
+
 // general kernel of a plugin (include/mcig/plugin.cuh) over its user functors: launches and
 // returns the launch's cudaError_t of the plugin's own CUDA runtime
 typedef int (*mcig_plugin_launch_fn)(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st);

@@ -1,7 +1,7 @@
 // Register-resident float sampling kernels for one-pdf configurations, all-coordinate
 // move, up to 16 dimensions: the log density is straight-line code for its kind
 // (mcig_fast.cuh, PK_*), with Kahan float or double block sums.
-#include "mcig_fast.cuh"
+#include "mcig_calib.cuh"
 #include "mcig_launchers.h"
 
 mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk)
@@ -10,6 +10,17 @@ mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk)
     case PK_GAUSS: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_GAUSS> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_GAUSS>;
     case PK_PREC: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_PREC> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_PREC>;
     case PK_MIX: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_MIX> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_MIX>;
+    default: return nullptr;
+    }
+}
+
+// calibration with the split tail (mcig_calib.cuh) for one exp(-x.x) or precision-matrix
+// sampling function; NULL for other kinds
+mcig_launch_fn mcig_calib_launcher_pk16(int pk)
+{
+    switch (pk) {
+    case PK_GAUSS: return mcig_calib_launch<16, PK_GAUSS>;
+    case PK_PREC: return mcig_calib_launch<16, PK_PREC>;
     default: return nullptr;
     }
 }

@@ -110,8 +110,12 @@ class MCI:
         _raise(self.L.mcig_set_kernel(self._h, int(policy)))
 
     def setPhaseFusion(self, on=True):
-        """Calibration, burn-in and sampling in one register-resident launch where it applies (default on)."""
+        """Calibration, burn-in and sampling in one register-resident launch where it applies (default off: slower when a few chains calibrate long)."""
         _raise(self.L.mcig_set_phase_fusion(self._h, int(bool(on))))
+
+    def setCalibrationSplit(self, on=True):
+        """Calibration's tail on 4 lanes per chain where it applies (default on; same results)."""
+        _raise(self.L.mcig_set_calibration_split(self._h, int(bool(on))))
 
     def setPrecision(self, precision):
         _raise(self.L.mcig_set_precision(self._h, int(precision)))

@@ -90,3 +90,33 @@ def test_phase_fusion_equals_separate_launches(prec):
     for u, v in zip(a["counts"], b["counts"]):
         np.testing.assert_array_equal(u, v)
     assert a["ms"]["launches"] < b["ms"]["launches"] and a["ms"]["calibration_ms"] < 0.05
+
+
+@pytest.mark.parametrize("ndim,pdf", [(16, "PDF_GAUSS_PREC"), (13, "PDF_GAUSS_PREC"), (16, "PDF_GAUSS")])
+def test_split_calibration_equals_one_lane(ndim, pdf):
+    """The calibration whose tail runs on four lanes per chain gives every chain the step size,
+    walker, Philox position and last-iteration counts of the one-lane calibration, bit for bit
+    (a last warp with lanes beyond the chains, padded coordinates at ndim 13)."""
+    import mcintegratorplusplus_gb300 as mcig
+    rng = np.random.default_rng(11)
+    q, _ = np.linalg.qr(rng.normal(size=(ndim, ndim)))
+    P = q @ np.diag(10.0 ** rng.uniform(-1, 1, ndim)) @ q.T
+
+    def go(split):
+        m = mcig.MCI(ndim, 4091, precision=mcig.PREC_FP32)
+        m.setSeed(5)
+        m.setCalibrationSplit(split)
+        if pdf == "PDF_GAUSS":
+            m.addSamplingFunction(mcig.PDF_GAUSS)
+        else:
+            m.addSamplingFunction(mcig.PDF_GAUSS_PREC, P.ravel())
+        m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+        m.setNfindMRT2Iterations(-50)
+        m.integrate(0, True, False)
+        return dict(steps=m.getMRT2Steps(), x=m.getX(), counts=m.getCounts())
+
+    a, b = go(True), go(False)
+    np.testing.assert_array_equal(a["steps"], b["steps"])
+    np.testing.assert_array_equal(a["x"], b["x"])
+    for u, v in zip(a["counts"], b["counts"]):
+        np.testing.assert_array_equal(u, v)

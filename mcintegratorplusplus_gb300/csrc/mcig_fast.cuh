@@ -33,14 +33,14 @@
 // issue all of them)
 enum { PK_ANY = 0, PK_GAUSS = 1, PK_PREC = 2, PK_MIX = 3 };
 
-// The last operations of the precision-matrix log density and of the Metropolis test in
-// round-to-nearest intrinsics, which the compiler never contracts into an FMA: the split
-// calibration (mcig_calib.cuh) evaluates them from the same operands in another context
-// and must round them alike.
-__device__ __forceinline__ float fast_lp_of_q(float q) { return __fmul_rn(-0.5f, q); }
+// The last operations of the precision-matrix log density and of the Metropolis test,
+// shared with the split calibration (mcig_calib.cuh), which evaluates them from the same
+// operands in the same expression shape (the compiler's FMA contraction of -q/2 - lp
+// is then decided alike; tests/test_fast_accumulators.py checks the bit-identity).
+__device__ __forceinline__ float fast_lp_of_q(float q) { return -0.5f * q; }
 __device__ __forceinline__ bool fast_accept(float u, float lpn, float lp)
 { // log2(u) <= (log p(x') - log p(x)) log2(e)
-    return __log2f(u) <= __fmul_rn(__fsub_rn(lpn, lp), 1.44269504f);
+    return __log2f(u) <= (lpn - lp) * 1.44269504f;
 }
 
 template <int MAXD>

@@ -10,7 +10,8 @@
 //   base affine x = mu + exp(logsig) y;  log q = log N(z) - sum s - sum logsig.
 // Sizes: D <= 32 even, d = D/2 <= 16, hidden H = 128, L <= 16 layers.
 //
-// Kernels (one CTA = 128 samples, 8 warps; warp w owns rows 16w..16w+15):
+// Kernels (one CTA = 128 samples; in the pass kernel warps w and w + 8 own rows
+// 16w..16w+15, in the backward kernel warp w alone):
 //   flow_pass_kernel     the L layers in one launch, generative or density
 //                        direction; GEMMs with mma.sync.m16n8k16 bf16 -> f32,
 //                        activations and weights staged in shared memory with
@@ -41,6 +42,7 @@ int mcig_set_last_error(int code, const char *msg); // mcig_capi.cu
 #define FLOW_MAXL 16
 #define FLOW_ROWS 128   // samples per CTA
 #define FLOW_THREADS 256
+#define FLOW_PASS_THREADS 512 // pass kernel: two warps per 16 rows, each forms half of every GEMM's columns
 #define FLOW_SMAX 3.0f
 
 // shared-memory strides (in bf16 elements), padded so that a fragment load of
@@ -286,41 +288,48 @@ __device__ __forceinline__ float sum_over_g(float v)
 // paired float atomic add (address 8-byte aligned)
 __device__ __forceinline__ void atomic_add2(float *a, float x, float y) { atomicAdd((float2 *)a, make_float2(x, y)); }
 
-// The MLP of one layer for the 16 rows r0.. of one warp: a-half in s.A -> s.H1, s.H2
-// (bf16) -> s.O (float).  Every tile row belongs to one warp, so the stages need only
-// warp synchronisation; the weights and biases of buffer buf are read-only.
-__device__ __forceinline__ void warp_layer_mlp(FlowSmem &s, int r0, int buf)
+// barrier of the two warps that share 16 rows in the pass kernel (named barrier 1 + pair)
+__device__ __forceinline__ void pair_sync(int pair)
+{
+    asm volatile("bar.sync %0, 64;\n" ::"r"(1 + pair) : "memory");
+}
+
+// The MLP of one layer for the 16 rows r0.. shared by the warps of pair `pair`: warp
+// `half` forms the columns [64 half, 64 half + 64) of h1 and h2 and [16 half, 16 half + 16)
+// of o.  Each GEMM reads the whole row of its input, so the pair meets after each stage;
+// every (row, column) is one warp's dot product over the whole row, k ascending.
+__device__ __forceinline__ void pair_layer_mlp(FlowSmem &s, int r0, int pair, int half, int buf)
 {
     const float *bias = s.bias[buf];
     {
-        float acc[16][4];
+        float acc[8][4];
         zero_acc(acc);
-        warp_gemm<1, 16>(s.A, LDA_S, r0, s.W1n[buf], LDA_S, acc);
-        store_act(acc, bias, true, s.H1, LDH_S, r0);
+        warp_gemm<1, 8>(s.A, LDA_S, r0, s.W1n[buf] + half * 64 * LDA_S, LDA_S, acc);
+        store_act(acc, bias + half * 64, true, s.H1 + half * 64, LDH_S, r0);
     }
-    __syncwarp();
+    pair_sync(pair);
     {
-        float acc[16][4];
+        float acc[8][4];
         zero_acc(acc);
-        warp_gemm<FLOW_H / 16, 16>(s.H1, LDH_S, r0, s.W2n[buf], LDH_S, acc);
-        store_act(acc, bias + FLOW_H, true, s.H2, LDH_S, r0);
+        warp_gemm<FLOW_H / 16, 8>(s.H1, LDH_S, r0, s.W2n[buf] + half * 64 * LDH_S, LDH_S, acc);
+        store_act(acc, bias + FLOW_H + half * 64, true, s.H2 + half * 64, LDH_S, r0);
     }
-    __syncwarp();
+    pair_sync(pair);
     {
-        float acc[4][4];
+        float acc[2][4];
         zero_acc(acc);
-        warp_gemm<FLOW_H / 16, 4>(s.H2, LDH_S, r0, s.W3n[buf], LDH_S, acc);
+        warp_gemm<FLOW_H / 16, 2>(s.H2, LDH_S, r0, s.W3n[buf] + half * 16 * LDH_S, LDH_S, acc);
         const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const int c = nt * 8 + 2 * t;
+        for (int nt = 0; nt < 2; ++nt) {
+            const int c = half * 16 + nt * 8 + 2 * t;
             s.O[r0 + g][c] = acc[nt][0] + bias[2 * FLOW_H + c];
             s.O[r0 + g][c + 1] = acc[nt][1] + bias[2 * FLOW_H + c + 1];
             s.O[r0 + g + 8][c] = acc[nt][2] + bias[2 * FLOW_H + c];
             s.O[r0 + g + 8][c + 1] = acc[nt][3] + bias[2 * FLOW_H + c + 1];
         }
     }
-    __syncwarp();
+    pair_sync(pair);
 }
 
 // 16-byte asynchronous global -> shared copies (cp.async, completion per thread)
@@ -385,18 +394,21 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
-// Each warp owns 16 rows of the tile through all layers (load, MLP, coupling, output),
-// so within a layer it only synchronises with itself; one block barrier per layer
-// publishes the layer's weights (prefetched with cp.async during the previous layer)
-// and frees the other weight buffer for the next prefetch.
-__global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
+// Each pair of warps (w, w + 8) owns 16 rows of the tile through all layers (load, MLP,
+// coupling, output): the two warps form half of each GEMM's columns and split the
+// element-wise work, so within a layer a pair synchronises only with itself (named
+// barriers); one block barrier per layer publishes the layer's weights (prefetched with
+// cp.async during the previous layer) and frees the other weight buffer for the next
+// prefetch.  Sixteen warps per SM hide the latency of the dependent GEMM chain that eight
+// warps left exposed.
+__global__ void __launch_bounds__(FLOW_PASS_THREADS, 1) flow_pass_kernel(FlowArgs f)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FlowSmem &s = *(FlowSmem *)smem_raw;
     const int base = blockIdx.x * FLOW_ROWS;
     const int D = f.D, d = f.d;
     const int rows = min(FLOW_ROWS, f.n - base);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, r0 = warp * 16;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, pair = warp & 7, half = warp >> 3, r0 = pair * 16;
     const float invd = 1.f / (float)d;
     if (f.in_cm) { // chain-minor walkers: coalesced over the rows, one coordinate at a time
         for (int i = threadIdx.x; i < D * FLOW_ROWS; i += blockDim.x) {
@@ -406,8 +418,8 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
             s.Y[r][c] = v;
         }
         __syncthreads();
-    } else { // the warp's rows of the tile (rows beyond n are zero)
-        for (int r = r0; r < r0 + 16; ++r) {
+    } else { // the pair's rows of the tile (rows beyond n are zero), eight per warp
+        for (int r = r0 + 8 * half; r < r0 + 8 * half + 8; ++r) {
             if (lane < D) {
                 float v = (r < rows) ? f.in[(int64_t)(base + r) * D + lane] : 0.f;
                 if (f.dir == 1) { v = (v - f.mu[lane]) * __expf(-f.logsig[lane]); } // density: undo the base affine first
@@ -415,7 +427,7 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
             }
         }
     }
-    if (lane < 16) { s.logdet[r0 + lane] = 0.f; }
+    if (half == 0 && lane < 16) { s.logdet[r0 + lane] = 0.f; }
     for (int i = threadIdx.x; i < f.L * D; i += blockDim.x) { s.perm[i] = f.perm[i]; }
     auto layer_of = [&](int step) { return (f.dir == 0) ? step : f.L - 1 - step; };
     auto params_of = [&](int step) { return f.theta + (int64_t)layer_of(step) * f.pstride; };
@@ -429,18 +441,18 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
         if (step + 1 < f.L) {
             load_layer_weights_async(s, f.wb + (int64_t)layer_of(step + 1) * f.wstride, params_of(step + 1), d, buf ^ 1);
         }
-        // a-half of the warp's rows as bf16 (columns d..15 zero)
+        // a-half of the pair's rows as bf16 (columns d..15 zero), eight rows per warp
         {
             const int pa = (lane & 15) < d ? perm[lane & 15] : 0;
-            for (int r = r0 + (lane >> 4); r < r0 + 16; r += 2) {
+            for (int r = r0 + 8 * half + (lane >> 4); r < r0 + 8 * half + 8; r += 2) {
                 const int c = lane & 15;
                 s.A[r * LDA_S + c] = __float2bfloat16_rn(c < d ? s.Y[r][pa] : 0.f);
             }
         }
-        __syncwarp();
-        warp_layer_mlp(s, r0, buf);
-        // coupling of the warp's 16 rows x d columns, (row, column) pairs spread over the lanes
-        for (int i = lane; i < 16 * d; i += 32) {
+        pair_sync(pair);
+        pair_layer_mlp(s, r0, pair, half, buf);
+        // coupling of the pair's 16 rows x d columns, (row, column) pairs spread over its 64 lanes
+        for (int i = lane + 32 * half; i < 16 * d; i += 64) {
             const int q = (int)(((float)i + 0.5f) * invd);
             const int r = r0 + q, j = i - q * d;
             const float sj = soft_clamp(s.O[r][j]);
@@ -458,18 +470,18 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_pass_kernel(FlowArgs f)
             s.Y[r][pb] = bout;
             s.O[r][j] = sj; // kept for the row's log-determinant below
         }
-        __syncwarp();
-        if (lane < 16) {
+        pair_sync(pair);
+        if (half == 0 && lane < 16) {
             float ld = 0.f;
             for (int j = 0; j < d; ++j) { ld += s.O[r0 + lane][j]; }
             s.logdet[r0 + lane] += ld;
         }
-        __syncwarp();
     }
+    pair_sync(pair); // the pair's log-determinants are complete
     // output and log q of the warp's rows
     float ls = 0.f;
     for (int c = 0; c < D; ++c) { ls += f.logsig[c]; }
-    for (int r = r0; r < min(r0 + 16, rows); ++r) {
+    for (int r = r0 + half; r < min(r0 + 16, rows); r += 2) {
         float zz = 0.f;
         if (lane < D) {
             float z, o;
@@ -962,7 +974,7 @@ extern "C" int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n)
 static int flow_pass_launch(mcig_flow *f, FlowArgs &a, int64_t n, cudaStream_t st)
 {
     const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
-    flow_pass_kernel<<<grid, FLOW_THREADS, sizeof(FlowSmem), st>>>(a);
+    flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
     FCK(cudaGetLastError());
     return MCIG_OK;
 }
@@ -993,7 +1005,7 @@ int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, f
     a.perm = f->perm; a.tape = d_tape; a.wb = f->wb; a.theta = f->theta;
     a.wstride = WB_LAYER; a.pstride = f->pstride;
     const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
-    flow_pass_kernel<<<grid, FLOW_THREADS, sizeof(FlowSmem), st>>>(a);
+    flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
     FCK(cudaGetLastError());
     return MCIG_OK;
 }

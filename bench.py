@@ -44,8 +44,8 @@ NBLOCKS = 100
 METRIC = "effective samples/s on 1 GB300 at matched std-error: learned/batched vs plain MH"
 # ncu figures of the sampling launch (65,536 chains, 600 steps, 6 blocks of 100, four
 # accumulators): DRAM bytes read + written, and warp instructions per warp-step
-CAPTURE_DRAM_BYTES = 9.58e6 + 2.6767e9
-INST_PER_WARP_STEP = 1168.0
+CAPTURE_DRAM_BYTES = 9.62e6 + 2.6769e9
+INST_PER_WARP_STEP = 1188.0
 
 
 def target(seed=2024):

@@ -67,8 +67,7 @@ static __global__ void est_uncorr_f32_kernel(EstArgs a)
     const float *d = (const float *)a.data + s;
     const int64_t stride = (int64_t)a.nv * a.nchains;
     float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
-    for (int64_t i = 0; i < a.n; ++i) {
-        const float x = d[i * stride];
+    auto add = [&](float x) {
         float y = x - c1, t = s1 + y;
         c1 = (t - s1) - y;
         s1 = t;
@@ -76,7 +75,18 @@ static __global__ void est_uncorr_f32_kernel(EstArgs a)
         t = s2 + y;
         c2 = (t - s2) - y;
         s2 = t;
+    };
+    // 32 loads in flight per thread, then the sums in sample order: with one value per
+    // series (65,536 series) one load at a time kept too few bytes in flight for HBM
+    int64_t i = 0;
+    for (; i + 32 <= a.n; i += 32) {
+        float x[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) { x[k] = d[(i + k) * stride]; }
+#pragma unroll
+        for (int k = 0; k < 32; ++k) { add(x[k]); }
     }
+    for (; i < a.n; ++i) { add(d[i * stride]); }
     const double SMALLEST_ERROR = 1.e-300;
     const double norm = 1. / a.n;
     const double average = ((double)s1 - (double)c1) * norm;

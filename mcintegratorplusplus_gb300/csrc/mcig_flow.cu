@@ -10,8 +10,8 @@
 //   base affine x = mu + exp(logsig) y;  log q = log N(z) - sum s - sum logsig.
 // Sizes: D <= 32 even, d = D/2 <= 16, hidden H = 128, L <= 16 layers.
 //
-// Kernels (one CTA = 128 samples; in the pass kernel warps w and w + 8 own rows
-// 16w..16w+15, in the backward kernel warp w alone):
+// Kernels (one CTA = 112 samples in the pass kernel, warps w and w + 7 owning rows
+// 16w..16w+15; 128 samples in the backward kernel, warp w alone owning rows 16w..16w+15):
 //   flow_pass_kernel     the L layers in one launch, generative or density
 //                        direction; GEMMs with mma.sync.m16n8k16 bf16 -> f32,
 //                        activations and weights staged in shared memory with
@@ -42,7 +42,12 @@ int mcig_set_last_error(int code, const char *msg); // mcig_capi.cu
 #define FLOW_MAXL 16
 #define FLOW_ROWS 128   // samples per CTA
 #define FLOW_THREADS 256
-#define FLOW_PASS_THREADS 512 // pass kernel: two warps per 16 rows, each forms half of every GEMM's columns
+// pass kernel: 112 samples per CTA (147 CTAs cover 16,384 samples on the 152 SMs in one
+// wave, where 128-sample CTAs left 24 SMs idle), two warps per 16 rows, each forming half of
+// every GEMM's columns
+#define FLOW_PASS_ROWS 112
+#define FLOW_PASS_PAIRS (FLOW_PASS_ROWS / 16)
+#define FLOW_PASS_THREADS (64 * FLOW_PASS_PAIRS)
 #define FLOW_SMAX 3.0f
 
 // shared-memory strides (in bf16 elements), padded so that a fragment load of
@@ -394,25 +399,25 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
-// Each pair of warps (w, w + 8) owns 16 rows of the tile through all layers (load, MLP,
+// Each pair of warps (w, w + 7) owns 16 rows of the tile through all layers (load, MLP,
 // coupling, output): the two warps form half of each GEMM's columns and split the
 // element-wise work, so within a layer a pair synchronises only with itself (named
 // barriers); one block barrier per layer publishes the layer's weights (prefetched with
 // cp.async during the previous layer) and frees the other weight buffer for the next
-// prefetch.  Sixteen warps per SM hide the latency of the dependent GEMM chain that eight
-// warps left exposed.
+// prefetch.  Two warps per 16 rows (14 per SM) hide the latency of the dependent GEMM
+// chain that one warp per 16 rows left exposed.
 __global__ void __launch_bounds__(FLOW_PASS_THREADS, 1) flow_pass_kernel(FlowArgs f)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FlowSmem &s = *(FlowSmem *)smem_raw;
-    const int base = blockIdx.x * FLOW_ROWS;
+    const int base = blockIdx.x * FLOW_PASS_ROWS;
     const int D = f.D, d = f.d;
-    const int rows = min(FLOW_ROWS, f.n - base);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, pair = warp & 7, half = warp >> 3, r0 = pair * 16;
+    const int rows = min(FLOW_PASS_ROWS, f.n - base);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, pair = warp % FLOW_PASS_PAIRS, half = warp / FLOW_PASS_PAIRS, r0 = pair * 16;
     const float invd = 1.f / (float)d;
     if (f.in_cm) { // chain-minor walkers: coalesced over the rows, one coordinate at a time
-        for (int i = threadIdx.x; i < D * FLOW_ROWS; i += blockDim.x) {
-            const int c = i / FLOW_ROWS, r = i % FLOW_ROWS;
+        for (int i = threadIdx.x; i < D * FLOW_PASS_ROWS; i += blockDim.x) {
+            const int c = i / FLOW_PASS_ROWS, r = i % FLOW_PASS_ROWS;
             float v = (r < rows) ? (float)f.in_cm[(int64_t)c * f.cm_stride + base + r] : 0.f;
             if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); }
             s.Y[r][c] = v;
@@ -501,8 +506,8 @@ __global__ void __launch_bounds__(FLOW_PASS_THREADS, 1) flow_pass_kernel(FlowArg
     }
     if (f.out_cm) { // coalesced over the rows, one coordinate at a time
         __syncthreads();
-        for (int i = threadIdx.x; i < D * FLOW_ROWS; i += blockDim.x) {
-            const int c = i / FLOW_ROWS, r = i % FLOW_ROWS;
+        for (int i = threadIdx.x; i < D * FLOW_PASS_ROWS; i += blockDim.x) {
+            const int c = i / FLOW_PASS_ROWS, r = i % FLOW_PASS_ROWS;
             if (r < rows) { f.out_cm[(int64_t)c * f.cm_stride + base + r] = s.Y[r][c]; }
         }
     }
@@ -973,7 +978,7 @@ extern "C" int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n)
 // one pass over device arrays (in [n][D] float -> out, logq); tape optional
 static int flow_pass_launch(mcig_flow *f, FlowArgs &a, int64_t n, cudaStream_t st)
 {
-    const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
+    const int grid = (int)((n + FLOW_PASS_ROWS - 1) / FLOW_PASS_ROWS);
     flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
     FCK(cudaGetLastError());
     return MCIG_OK;
@@ -1004,7 +1009,7 @@ int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, f
     a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
     a.perm = f->perm; a.tape = d_tape; a.wb = f->wb; a.theta = f->theta;
     a.wstride = WB_LAYER; a.pstride = f->pstride;
-    const int grid = (int)((n + FLOW_ROWS - 1) / FLOW_ROWS);
+    const int grid = (int)((n + FLOW_PASS_ROWS - 1) / FLOW_PASS_ROWS);
     flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
     FCK(cudaGetLastError());
     return MCIG_OK;

@@ -555,6 +555,7 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
     const int warp = threadIdx.x >> 5, r0 = warp * 16;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     constexpr int NW = FLOW_THREADS / 32;
+    static_assert(FLOW_H == 16 * NW, "dW1 gives each warp 16 of the hidden columns");
     for (int r = warp; r < FLOW_ROWS; r += NW) { // d(0.5|z|^2)/dz / B
         if (lane < D) { s.G[r][lane] = (r < rows) ? f.z[(int64_t)(base + r) * D + lane] * f.inv_batch : 0.f; }
     }
@@ -739,14 +740,15 @@ __global__ void __launch_bounds__(FLOW_THREADS) flow_backward_kernel(FlowBwdArgs
                 }
             }
         }
-        // dW1 = a^T g_h1: only warp rows 0..15 (the padded a-half)
-        if (warp == 0) {
-            float acc[16][4];
+        // dW1 = a^T g_h1: the 16 rows of the padded a-half, the 128 outputs split over the
+        // warps (16 each), so no warp forms the whole 16 x 128 product while the others wait
+        {
+            float acc[2][4];
             zero_acc(acc);
-            warp_gemm_tn<16>(s.A, LDA_S, 0, s.GH1, LDH_S, acc);
+            warp_gemm_tn<2>(s.A, LDA_S, 0, s.GH1 + 16 * warp, LDH_S, acc);
 #pragma unroll
-            for (int nt = 0; nt < 16; ++nt) {
-                const int c = nt * 8 + 2 * t;
+            for (int nt = 0; nt < 2; ++nt) {
+                const int c = 16 * warp + nt * 8 + 2 * t;
                 if (g < d) { atomic_add2(&GP[pl_W1(d) + (int64_t)g * FLOW_H + c], acc[nt][0], acc[nt][1]); }
                 if (g + 8 < d) { atomic_add2(&GP[pl_W1(d) + (int64_t)(g + 8) * FLOW_H + c], acc[nt][2], acc[nt][3]); }
             }

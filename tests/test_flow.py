@@ -53,7 +53,7 @@ def test_flow_passes_match_oracle(mcig):
     f.set_params(th)
     perms = fo.permutations(D, L, 11)
     rng = np.random.default_rng(1)
-    z = rng.standard_normal((300, D))  # not a multiple of the 128-row tile
+    z = rng.standard_normal((300, D))  # not a multiple of the 112-row pass tile nor the 128-row backward tile
     x, lq = f.forward(z)
     xo, lqo = fo.forward(th.astype(np.float64), z, D, L, H, perms, bf16=True)
     assert np.abs(x - xo).max() < 2e-2 * max(1.0, np.abs(xo).max())

@@ -92,11 +92,13 @@ def test_phase_fusion_equals_separate_launches(prec):
     assert a["ms"]["launches"] < b["ms"]["launches"] and a["ms"]["calibration_ms"] < 0.05
 
 
-@pytest.mark.parametrize("ndim,pdf", [(16, "PDF_GAUSS_PREC"), (13, "PDF_GAUSS_PREC"), (16, "PDF_GAUSS")])
-def test_split_calibration_equals_one_lane(ndim, pdf):
+@pytest.mark.parametrize("ndim,pdf,nfind", [(16, "PDF_GAUSS_PREC", -50), (13, "PDF_GAUSS_PREC", -50),
+                                            (16, "PDF_GAUSS", -50), (16, "PDF_GAUSS_PREC", 7)])
+def test_split_calibration_equals_one_lane(ndim, pdf, nfind):
     """The calibration whose tail runs on four lanes per chain gives every chain the step size,
     walker, Philox position and last-iteration counts of the one-lane calibration, bit for bit
-    (a last warp with lanes beyond the chains, padded coordinates at ndim 13)."""
+    (a last warp with lanes beyond the chains, padded coordinates at ndim 13, a fixed number
+    of iterations)."""
     import mcintegratorplusplus_gb300 as mcig
     rng = np.random.default_rng(11)
     q, _ = np.linalg.qr(rng.normal(size=(ndim, ndim)))
@@ -111,7 +113,7 @@ def test_split_calibration_equals_one_lane(ndim, pdf):
         else:
             m.addSamplingFunction(mcig.PDF_GAUSS_PREC, P.ravel())
         m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
-        m.setNfindMRT2Iterations(-50)
+        m.setNfindMRT2Iterations(nfind)
         m.integrate(0, True, False)
         return dict(steps=m.getMRT2Steps(), x=m.getX(), counts=m.getCounts())
 

@@ -152,6 +152,12 @@ public:
     void setNfindMRT2Iterations(int n) { _nfind = n; detail::check(mcig_set_nfind_mrt2_iterations(_h, n)); }
     void setNdecorrelationSteps(int64_t n) { _ndecorr = n; detail::check(mcig_set_ndecorrelation_steps(_h, n)); }
     void setPrecision(Precision p) { detail::check(mcig_set_precision(_h, static_cast<int>(p))); }
+    // device tuning without a counterpart in mci::MCI (results unchanged, include/mcig.h):
+    // kernel choice 0 automatic / 1 general / 2 register-resident, the calibration's tail on
+    // four lanes per chain (default on), the three phases in one launch (default off)
+    void setKernel(int policy) { detail::check(mcig_set_kernel(_h, policy)); }
+    void setCalibrationSplit(bool on) { detail::check(mcig_set_calibration_split(_h, on ? 1 : 0)); }
+    void setPhaseFusion(bool on) { detail::check(mcig_set_phase_fusion(_h, on ? 1 : 0)); }
 
     // --- domain
     void setIRange(double lb, double ub)

@@ -11,12 +11,18 @@ Workload (one "step" = one full MCI::integrate over every chain):
   float walker arithmetic, Kahan-compensated float block sums.
 
 Metric: effective samples/s of <x.x>, ESS = Var(x.x) / err^2 where
-Var(x.x) = 2 tr(Sigma^2) is the target variance and err the integrator's
-combined standard error from the 100-block accumulator (the reference's
-Uncorrelated estimator on block means, combined over chains with the MPIMCI
-formula).  `value` times the device work with inputs resident; `e2e` times the
-same integrate through the C ABI with the initial walkers copied from pinned
-host memory and the averages / errors read back every step.
+Var(x.x) = 2 tr(Sigma^2) is the target variance and err the standard error of the
+combined estimate measured from the spread of the chain means (the chains are
+independent: err^2 = var(chain means) / nchains), so ESS = nchains * NMC / (2 tau_int).
+Two estimates of the integrated autocorrelation time tau_int of x.x check it, from the
+Full samples of 256 chains: the reference's MJBlocker (src/MJBlocker.cpp:127-154) on
+the last 8,192 samples of every chain, and Sokal's self-consistent window (c = 5) on
+the chain-averaged autocorrelation.  The 100-block error that the integrator reports
+(Uncorrelated estimator on block means) is kept as a labelled diagnostic: with tau_int
+above the 100-step block length it underestimates the error.  `value` times the device
+work with inputs resident; `e2e` times the same integrate through the C ABI with the
+initial walkers copied from pinned host memory and the averages / errors read back
+every step.
 
 --impl reference times the CPU path on the host cores: the oracle's
 restatement of the reference (one reference MCI per chain, std::mt19937_64
@@ -69,6 +75,50 @@ def configure(m, P, nmc, nblocks=NBLOCKS):
     m.add_observable(1, (), bs, 1, False, 1)  # x_i, Block, Uncorrelated
     m.add_observable(0, (), 1, 1, False, 1)   # x.x, Full
     m.add_observable(1, (), 1, 1, False, 1)   # x_i, Full
+
+
+def sokal_tau(series, c=5.0):
+    """Integrated autocorrelation time of series[nchains][n] (steps): chain-averaged
+    autocorrelation, tau(M) = 1/2 + sum_{t=1..M} rho(t), smallest M >= c tau(M)."""
+    x = np.asarray(series, dtype=np.float64)
+    x = x - x.mean(axis=1, keepdims=True)
+    n = x.shape[1]
+    f = np.fft.rfft(x, 2 * n, axis=1)
+    acf = np.fft.irfft(f * np.conj(f), axis=1)[:, :n].mean(axis=0) / np.arange(n, 0, -1)
+    rho = acf / acf[0]
+    tau = 0.5 + np.cumsum(rho[1:])
+    for M in range(1, n - 1):
+        if M >= c * tau[M - 1]:
+            return float(tau[M - 1])
+    return float(tau[-1])
+
+
+def ess_report(chain_means, var, nchains, nmc, series=None, mj=None, block_err=None):
+    """Effective sample size of the combined mean from the spread of the chain means, with
+    tau_int cross-checks on a few chains' full series (mj: MJBlocker estimator function
+    taking x[n][ndim] and returning (avg[ndim], err[ndim]))."""
+    cm = np.asarray(chain_means, dtype=np.float64)
+    err_bc = float(cm.std(ddof=1) / np.sqrt(len(cm)))
+    ess = var / err_bc ** 2 * (nchains / len(cm))
+    out = {"ess": ess, "err_between_chains": err_bc, "tau_int_between_chains": nchains * nmc / (2.0 * ess),
+           "definition": "ESS = Var / err^2, Var the target variance of the observable, err = std(chain means) / sqrt(chains)"}
+    if series is not None:
+        s = np.asarray(series, dtype=np.float64)
+        out["tau_int_sokal"] = sokal_tau(s)
+        out["tau_series"] = "Full x.x of %d chains x %d samples" % s.shape
+        if mj is not None:
+            n2 = 1 << int(np.floor(np.log2(s.shape[1])))
+            tail = np.ascontiguousarray(s[:, -n2:].T)  # [n2][chains]: one MJBlocker series per chain
+            _, e = mj(tail)
+            v = tail.var(axis=0, ddof=1)
+            out["tau_int_mjblocker"] = float(np.mean(n2 * np.asarray(e) ** 2 / (2.0 * v)))
+            out["mjblocker_samples"] = n2
+        taus = [out[k] for k in ("tau_int_sokal", "tau_int_mjblocker") if k in out]
+        out["ess_over_ess_from_tau"] = [float(nchains * nmc / (2.0 * t) / ess) for t in taus]
+    if block_err is not None:
+        out["block100_err_over_between_chain_err"] = float(block_err / err_bc)
+        out["ess_block100_diagnostic"] = float(var / block_err ** 2)
+    return out
 
 
 class Clocks:
@@ -174,7 +224,11 @@ def run_gpu(args):
     ck = clocks.stop()
 
     xx, exx = float(avg_np[0]), float(err_np[0])
-    ess = var_xx / (exx * exx)
+    ca, _ = m.getChainResults()
+    ntau = min(256, nchains)
+    rep = ess_report(ca[:, 0], var_xx, nchains, args.nmc, series=m.getObsDataChains(2, 0, ntau),
+                     mj=lambda x: mcig.estimate(mcig.EST_MJBLOCKER, x), block_err=exx)
+    ess = rep["ess"]
     ms_dev = float(np.mean(dev_ms))
     ms_e2e = float(np.mean(wall)) * 1e3
     steps_total = nchains * (args.nmc)
@@ -202,8 +256,11 @@ def run_gpu(args):
                    "accumulation": "f32+Kahan", "calibration": "auto per chain (target 0.5)",
                    "l2": "flushed (256 MB write) before each step; Full output > L2"},
         "walker_steps_per_s": steps_total / (ms_dev * 1e-3),
-        "estimate": {"x.x": xx, "err": exx, "tr_sigma": float(np.trace(Sigma)),
-                     "z": (xx - float(np.trace(Sigma))) / exx, "acceptance": m.getAcceptanceRate()},
+        "estimate": {"x.x": xx, "err_block100": exx, "err_between_chains": rep["err_between_chains"],
+                     "tr_sigma": float(np.trace(Sigma)),
+                     "z": (xx - float(np.trace(Sigma))) / rep["err_between_chains"],
+                     "acceptance": m.getAcceptanceRate()},
+        "ess": rep,
         "phases_ms": {k: float(v) for k, v in tm.items() if k.endswith("_ms")},
         "e2e": {"value": ess / (ms_e2e * 1e-3), "unit": "effective samples/s",
                 "h2d_bytes_per_step": int(x0.numel() * 8), "d2h_bytes_per_step": int(2 * nod * 8),
@@ -248,21 +305,25 @@ def cpu_baseline(args, target_s=10.0):
         m.set_seeds(np.arange(1, nch + 1, dtype=np.uint64) * 7919)
         configure(m, P, args.nmc, args.blocks)
         t0 = time.perf_counter()
-        avg, err = m.integrate(args.nmc, True, True, nthreads=nthreads)
-        return avg, err, time.perf_counter() - t0
+        avg, err, ca, _ = m.integrate(args.nmc, True, True, nthreads=nthreads, per_chain=True)
+        return m, avg, err, ca, time.perf_counter() - t0
 
     nch = max(2 * nthreads, args.cpu_chains)
-    avg, err, dt = sample(nch)
+    m, avg, err, ca, dt = sample(nch)
     if dt < 0.5 * target_s:
         nch = int(min(NCHAINS, max(nch, nch * target_s / max(dt, 1e-3)) // nthreads * nthreads))
-        avg, err, dt = sample(nch)
+        del m
+        m, avg, err, ca, dt = sample(nch)
     # ESS is proportional to the number of chains, so ESS/s of the sample is that of the full workload
-    ess_sample = var_xx / float(err[0]) ** 2
-    return {"value": ess_sample / dt, "unit": "effective samples/s", "cores": nthreads, "kind": "port",
+    ntau = min(256, nch)
+    series = m.obs_data(2)[:ntau]
+    rep = ess_report(ca[:, 0], var_xx, nch, args.nmc, series=series,
+                     mj=lambda x: orc.estimate(4, x), block_err=float(err[0]))
+    return {"value": rep["ess"] / dt, "unit": "effective samples/s", "cores": nthreads, "kind": "port",
             "sample": "%d of the %d chains, full length (calibration, %d burn-in, %d steps), %.1f s" %
                       (nch, NCHAINS, BURNIN, args.nmc, dt),
-            "walker_steps_per_s": nch * args.nmc / dt, "x.x": float(avg[0]), "err": float(err[0]),
-            "chains": nch}
+            "walker_steps_per_s": nch * args.nmc / dt, "x.x": float(avg[0]), "err_block100": float(err[0]),
+            "chains": nch, "ess": rep}
 
 
 def run_reference(args):
@@ -445,7 +506,8 @@ def run_c5(args):
     """Learned proposal: 24-D mixture of 4 unit Gaussians at +-3 u1, +-3 u2, 16,384 chains,
     affine-coupling flow (8 layers, hidden 128, bf16 tensor cores) proposing every 5th step,
     against plain Gaussian Metropolis on the same chains.  ESS of <x_1> from the spread of the
-    chain means (ESS = Var(x_1) * chains / var(chain means)).  Metric: ESS/s with the flow."""
+    chain means (ESS = Var(x_1) * chains / var(chain means), the C2 definition), with tau_int of
+    x_1 from MJBlocker and Sokal's window on 256 chains' series.  Metric: ESS/s with the flow."""
     import mcintegratorplusplus_gb300 as mcig
     D, nch, nmc = 24, args.chains5, args.nmc5
     params, means, var_x1 = c5_target()
@@ -472,10 +534,12 @@ def run_c5(args):
                 tm = m.getLastTimings()
                 ms.append(_timed_device_ms(tm))
                 ca, _ = m.getChainResults()
-                ess.append(var_x1 * nch / float(np.var(ca[:, 0])))
+                rep = ess_report(ca[:, 0], var_x1, nch, nmc, series=m.getObsDataChains(0, 0, min(256, nch)),
+                                 mj=lambda x: mcig.estimate(mcig.EST_MJBLOCKER, x))
+                ess.append(rep["ess"])
         t = float(np.mean(ms)) * 1e-3
         res[use_flow] = (float(np.mean(ess)) / t, t, float(np.mean(ess)), float(np.mean(accs)) if accs else None,
-                         {k: float(v) for k, v in tm.items()})
+                         {k: float(v) for k, v in tm.items()}, rep)
     ratio = res[True][0] / res[False][0]
     return {"metric": "effective samples/s of <x_1> (C5: 24-D 4-mode mixture, learned flow proposal)",
             "value": res[True][0], "unit": "effective samples/s", "n_gpus": 1, "steps": args.steps,
@@ -486,8 +550,9 @@ def run_c5(args):
                        "hidden": 128, "period": 5, "adaptation_cycles": C5_ADAPT, "adam_batch": nch,
                        "adam_lr": 3e-3, "refresh": 4096},
             "plain_mh": {"value": res[False][0], "ms_per_step": res[False][1] * 1e3, "ess": res[False][2],
-                         "phases": res[False][4]},
-            "flow": {"ess": res[True][2], "acceptance": res[True][3], "phases": res[True][4]},
+                         "phases": res[False][4], "ess_detail": res[False][5]},
+            "flow": {"ess": res[True][2], "acceptance": res[True][3], "phases": res[True][4],
+                     "ess_detail": res[True][5]},
             "ess_per_s_ratio_flow_over_plain": ratio}
 
 

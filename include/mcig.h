@@ -161,6 +161,15 @@ int mcig_get_counts(const mcig_mci *h, int64_t *acc, int64_t *rej);
  * AccumulatorInterface.hpp:81).  n receives the element count when data is NULL. */
 int mcig_get_obs_data(const mcig_mci *h, int o, double *data, int64_t *n);
 
+/* The same data for the chains [c0, c0 + nc) only, [nc][nstore][nobs] (n receives the
+ * element count): a few chains' FullAccumulator series without copying every chain's. */
+int mcig_get_obs_data_chains(const mcig_mci *h, int o, int64_t c0, int64_t nc, double *data, int64_t *n);
+/* Philox step counter of every chain ([nchains]): the steps (calibration, burn-in and
+ * sampling) the chain has drawn since mcig_set_seed.  Step t of chain c draws from Philox
+ * counter (t lo, t hi, c, substep << 16 | tag << 12 | block) with key (seed lo, seed hi).
+ * No counterpart in the reference, whose chains share one sequential engine. */
+int mcig_get_step_counters(const mcig_mci *h, uint64_t *ctr);
+
 /* Replay mode (tests): consume recorded distribution outputs instead of
  * Philox draws.  tape is [nchains][stride] in the order the reference draws
  * them; lens the per-chain lengths.  Requires MCIG_PREC_FP64.  NULL switches

@@ -70,6 +70,8 @@ SIGNATURES = {
     "mcig_get_acceptance_rate": (c_int, [c_void_p, P_double]),
     "mcig_get_counts": (c_int, [c_void_p, P_int64, P_int64]),
     "mcig_get_obs_data": (c_int, [c_void_p, c_int, P_double, P_int64]),
+    "mcig_get_obs_data_chains": (c_int, [c_void_p, c_int, c_int64, c_int64, P_double, P_int64]),
+    "mcig_get_step_counters": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "mcig_set_replay": (c_int, [c_void_p, P_double, c_int64, P_int64]),
     "mcig_set_record_accepts": (c_int, [c_void_p, c_int]),
     "mcig_get_accept_bits": (c_int, [c_void_p, P_uint8, P_int64]),

@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 8) mcig_calib_kernel(const KP
             for (int k = 0; k < 4; ++k) { xn[k] = fmaf(sc[k], d[k], xo[k]); }
             CS::gather(xn, xf, base);
             const float lpn = CS::logp(U, xf, base);
-            if (fast_accept(u01_f(qa.a), lpn, lp)) {
+            if (fast_accept(accept_draw<float>(qa), lpn, lp)) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) { xo[k] = xn[k]; }
                 lp = lpn;

@@ -1839,6 +1839,39 @@ extern "C" int mcig_get_obs_data(const mcig_mci *h, int o, double *data, int64_t
     return MCIG_OK;
 }
 
+extern "C" int mcig_get_obs_data_chains(const mcig_mci *h, int o, int64_t c0, int64_t nc, double *data, int64_t *n)
+{
+    if (o < 0 || o >= (int)h->obsdata.size() || o >= (int)h->obs.size()) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "no data for observable %d", o); }
+    if (c0 < 0 || nc < 0 || c0 + nc > h->nchains) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "chains [%lld, %lld) outside [0, %lld)", (long long)c0, (long long)(c0 + nc), (long long)h->nchains); }
+    const ObsDef &d = h->obs[o];
+    const int64_t ns = h->obs_nstore[o];
+    *n = ns * d.nv * nc;
+    if (!data || nc == 0) { return MCIG_OK; }
+    cudaSetDevice(h->device);
+    const bool f32 = (d.acc == MCIG_ACC_FULL && h->full32);
+    const size_t esz = f32 ? sizeof(float) : sizeof(double);
+    const size_t rows = (size_t)ns * d.nv; // each row [nchains] holds one value of every chain
+    std::vector<char> t(rows * (size_t)nc * esz);
+    // one strided copy: nc chains of every (sample, value) row
+    CK(cudaMemcpy2D(t.data(), (size_t)nc * esz, h->obsdata[o].p + (size_t)c0 * esz, (size_t)h->nchains * esz,
+                    (size_t)nc * esz, rows, cudaMemcpyDeviceToHost));
+    for (int64_t c = 0; c < nc; ++c) {
+        for (size_t r = 0; r < rows; ++r) {
+            const size_t k = r * (size_t)nc + (size_t)c;
+            data[(size_t)c * rows + r] = f32 ? (double)((const float *)t.data())[k] : ((const double *)t.data())[k];
+        }
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_step_counters(const mcig_mci *h, uint64_t *ctr)
+{
+    if (!h || !ctr) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle or ctr is NULL"); }
+    cudaSetDevice(h->device);
+    CK(cudaMemcpy(ctr, h->ctr.p, (size_t)h->nchains * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    return MCIG_OK;
+}
+
 extern "C" int mcig_get_last_timings(const mcig_mci *h, double *ms4, int64_t *nlaunches)
 {
     for (int k = 0; k < 4; ++k) { ms4[k] = h->ms[k]; }
@@ -1922,7 +1955,7 @@ __global__ void flow_accept_kernel(KParams p, const float *xprop, const float *l
     for (int k = 0; k < p.npdf; ++k) { dl += pdf_logp_f(p, p.pdf[k], xp, p.fblob) - pdf_logp_f(p, p.pdf[k], x, p.fblob); }
     const P4 q = philox4x32_10((uint32_t)cycle, (uint32_t)(cycle >> 32), (uint32_t)c, TAG_FLOW_ACCEPT << 12,
                                p.key0 ^ 0x6A09E667u, p.key1 ^ 0xBB67AE85u);
-    const bool acc = isfinite(dl) && (__log2f(u01_f(q.a)) <= dl * 1.44269504f);
+    const bool acc = isfinite(dl) && (__log2f(accept_draw<float>(q)) <= dl * 1.44269504f);
     if (acc) {
         for (int i = 0; i < p.ndim; ++i) {
             x[i] = xp[i];

@@ -335,8 +335,10 @@ __device__ __forceinline__ void move_draws_srrd<double>(P4 q, int srrd, double *
 
 template <class R>
 __device__ __forceinline__ R accept_draw(P4 q);
+// float: on (0, 1], so the log-space test log2(u) <= ... never sees log2(0) = -inf (a
+// forced acceptance); double: on [0, 1) with 53 bits, the reference's generate_canonical range
 template <>
-__device__ __forceinline__ float accept_draw<float>(P4 q) { return u01_f(q.a); }
+__device__ __forceinline__ float accept_draw<float>(P4 q) { return u01_open0_f(q.a); }
 template <>
 __device__ __forceinline__ double accept_draw<double>(P4 q) { return u01_d(q.a, q.b); }
 

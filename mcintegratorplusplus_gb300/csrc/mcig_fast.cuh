@@ -248,7 +248,7 @@ struct FastSampler {
             }
         }
         const float lpn = fast_logp<MAXD, PK>(p, fc, xn);
-        const float u = u01_f(block(TAG_ACCEPT, 0).a);
+        const float u = accept_draw<float>(block(TAG_ACCEPT, 0));
         const bool acc = fast_accept(u, lpn, lp);
         if (acc) {
 #pragma unroll

@@ -280,6 +280,20 @@ class MCI:
         _raise(self.L.mcig_get_obs_data(self._h, int(o), _dp(out), ctypes.byref(n)))
         return out.reshape(self.nchains, -1)
 
+    def getObsDataChains(self, o, c0, nc):
+        """Accumulator data of observable o for the chains [c0, c0 + nc), [nc][nstore*nobs]."""
+        n = ctypes.c_int64()
+        _raise(self.L.mcig_get_obs_data_chains(self._h, int(o), int(c0), int(nc), None, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        _raise(self.L.mcig_get_obs_data_chains(self._h, int(o), int(c0), int(nc), _dp(out), ctypes.byref(n)))
+        return out.reshape(int(nc), -1)
+
+    def getStepCounters(self):
+        """Philox step counter of every chain (steps drawn since setSeed)."""
+        out = np.zeros(self.nchains, dtype=np.uint64)
+        _raise(self.L.mcig_get_step_counters(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+        return out
+
     def setReplay(self, tape, lens=None):
         if tape is None:
             _raise(self.L.mcig_set_replay(self._h, None, 0, None))

@@ -185,7 +185,102 @@ typedef struct {
     double *rec;
     int64_t rec_len, rec_cap;
     int exhausted;
+    /* Philox source (orc_set_philox): the draws of the device kernels' counter layout,
+     * one step's draws generated at its first draw, in the order this oracle consumes them */
+    int philox;              /* 0 off, ORC_PHILOX_FLOAT or ORC_PHILOX_DOUBLE */
+    uint32_t pkey[2], pchain;
+    uint64_t pctr;           /* step counter of the chain (the device's ctr) */
+    int pmove, psrrd, pveclen, pndim;
+    double *pbuf;            /* [pndim + 2] */
+    int pbuf_n, pbuf_pos;
 } drawsrc;
+
+/* one Philox4x32-10 block of the device kernels' counter layout:
+ * (step lo, step hi, chain, substep << 16 | tag << 12 | block) */
+static void philox_block(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const uint32_t key[2], uint32_t out[4])
+{
+    const uint32_t ctr[4] = {c0, c1, c2, c3};
+    orc_philox4x32_10(ctr, key, out);
+}
+
+#define ORC_TAG_MOVE 0u
+#define ORC_TAG_ACCEPT 1u
+#define ORC_TAG_INDEX 2u
+
+/* Box-Muller of the float kernels' draw layout (mcig_common.cuh box_muller_f), in double:
+ * u = ((w0 >> 8) + 1/2) 2^-24 in (0, 1), angle 2 pi ((w1 >> 8) 2^-24 - 1/2) */
+static void orc_bm_float(uint32_t w0, uint32_t w1, double *z0, double *z1)
+{
+    const double u = ((double)(w0 >> 8) + 0.5) * 0x1p-24;
+    const double r = sqrt(-2.0 * log(u));
+    const double th = 6.283185307179586 * ((double)(w1 >> 8) * 0x1p-24 - 0.5);
+    *z0 = r * cos(th);
+    *z1 = r * sin(th);
+}
+
+static double orc_u01_d(uint32_t hi, uint32_t lo)
+{
+    return (double)((((uint64_t)hi) << 21) | (uint64_t)(lo >> 11)) * 0x1p-53;
+}
+
+/* the move draws of Philox block b (float layout: 4 coordinates, double layout: 2) */
+static void philox_move_block(const drawsrc *d, uint32_t b, double *v)
+{
+    uint32_t q[4];
+    philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, (ORC_TAG_MOVE << 12) | b, d->pkey, q);
+    const int gauss = d->psrrd == MCIG_SRRD_GAUSSIAN;
+    if (d->philox == 1) {
+        if (gauss) {
+            orc_bm_float(q[0], q[1], &v[0], &v[1]);
+            orc_bm_float(q[2], q[3], &v[2], &v[3]);
+        } else {
+            for (int k = 0; k < 4; ++k) { v[k] = (double)(q[k] >> 8) * 0x1p-24 * 2.0 - 1.0; }
+        }
+    } else if (gauss) { /* box_muller_d: u = 1 - u01(a, b) in (0, 1], angle 2 pi u01(c, d) */
+        const double u = 1.0 - orc_u01_d(q[0], q[1]);
+        const double r = sqrt(-2.0 * log(u));
+        const double a = 6.283185307179586 * orc_u01_d(q[2], q[3]);
+        v[0] = r * cos(a);
+        v[1] = r * sin(a);
+    } else {
+        v[0] = orc_u01_d(q[0], q[1]) * 2.0 - 1.0;
+        v[1] = orc_u01_d(q[2], q[3]) * 2.0 - 1.0;
+    }
+}
+
+/* the draws of one step in this oracle's consumption order: [vector index,] the moved
+ * coordinates' draws (ascending), the acceptance uniform */
+static void philox_fill(drawsrc *d)
+{
+    const int cpb = (d->philox == 1) ? 4 : 2;
+    uint32_t q[4];
+    int n = 0, lo = 0, hi = d->pndim;
+    if (d->pmove == MCIG_MOVE_VEC) { /* index: 32-bit multiply-shift of word a of the index block */
+        const uint32_t nvecs = (uint32_t)(d->pndim / d->pveclen);
+        philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, ORC_TAG_INDEX << 12, d->pkey, q);
+        const int vidx = (int)(((uint64_t)q[0] * nvecs) >> 32);
+        d->pbuf[n++] = (double)vidx;
+        lo = vidx * d->pveclen;
+        hi = lo + d->pveclen;
+    }
+    double v[4];
+    for (int i = lo; i < hi; ++i) {
+        if (i == lo || i % cpb == 0) { philox_move_block(d, (uint32_t)(i / cpb), v); }
+        d->pbuf[n++] = v[i % cpb];
+    }
+    philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, ORC_TAG_ACCEPT << 12, d->pkey, q);
+    d->pbuf[n++] = (d->philox == 1) ? (double)((q[0] >> 8) + 1u) * 0x1p-24 /* (0, 1] */ : orc_u01_d(q[0], q[1]);
+    d->pbuf_n = n;
+    d->pbuf_pos = 0;
+}
+
+static double philox_next(drawsrc *d)
+{
+    if (d->pbuf_pos >= d->pbuf_n) { philox_fill(d); }
+    const double v = d->pbuf[d->pbuf_pos++];
+    if (d->pbuf_pos >= d->pbuf_n) { ++d->pctr; } /* the step's acceptance draw: next step */
+    return v;
+}
 
 static void rec_push(drawsrc *d, double v)
 {
@@ -212,6 +307,7 @@ static int tape_next(drawsrc *d, double *v)
 static double draw_u01(drawsrc *d)
 {
     double v;
+    if (d->philox) { return philox_next(d); }
     if (d->tape) { tape_next(d, &v); return v; }
     v = canonical(&d->mt);
     rec_push(d, v);
@@ -222,6 +318,7 @@ static double draw_u01(drawsrc *d)
 static double draw_upm1(drawsrc *d)
 {
     double v;
+    if (d->philox) { return philox_next(d); }
     if (d->tape) { tape_next(d, &v); return v; }
     v = canonical(&d->mt) * 2.0 + -1.0;
     rec_push(d, v);
@@ -232,6 +329,7 @@ static double draw_upm1(drawsrc *d)
 static double draw_normal(drawsrc *d, normstate *st)
 {
     double v;
+    if (d->philox) { return philox_next(d); }
     if (d->tape) { tape_next(d, &v); return v; }
     v = polar_normal(&d->mt, st);
     rec_push(d, v);
@@ -242,6 +340,7 @@ static double draw_normal(drawsrc *d, normstate *st)
 static int draw_index(drawsrc *d, int n)
 {
     double v;
+    if (d->philox) { return (int)philox_next(d); }
     if (d->tape) {
         tape_next(d, &v);
         int i = (int)v;
@@ -910,6 +1009,7 @@ typedef struct {
     double *po[MAXPDF], *pn[MAXPDF];
     double *spo[MAXPDF], *spn[MAXPDF];
     uint8_t *bits;
+    double *marg;  /* recorded with the bits: log(u) - log(acceptance), accepted iff <= 0 */
     int64_t nbits, capbits, main_start;
     int err;
     /* results of the last integrate */
@@ -1011,7 +1111,7 @@ void orc_destroy(orc_mci *h)
     for (int c = 0; c < h->nchains; ++c) {
         chainst *s = &h->ch[c];
         free(s->x); free(s->xn); free(s->orig); free(s->cidx); free(s->step);
-        free(s->ds.rec); free(s->bits);
+        free(s->ds.rec); free(s->bits); free(s->marg); free(s->ds.pbuf);
         for (int k = 0; k < MAXPDF; ++k) { free(s->po[k]); free(s->pn[k]); free(s->spo[k]); free(s->spn[k]); }
         chain_free_results(h, s);
     }
@@ -1284,14 +1384,76 @@ int orc_set_replay(orc_mci *h, const double *tape, int64_t stride, const int64_t
     return MCIG_OK;
 }
 
-static void push_bit(chainst *c, int b)
+/* Draws from the device kernels' Philox streams instead of the engine: chain c of this
+ * oracle is device chain chain0 + c, key (seed lo, seed hi), step counter ctr0[c] (NULL:
+ * 0).  layout 1: the float kernels' draws (mcig_common.cuh move_draws<float>, accept
+ * on (0, 1]) evaluated in double from the same Philox words; layout 2: the double
+ * kernels' draws (move_draws<double>, accept_draw<double>).  All-coordinate and vector
+ * moves with uniform or Gaussian draws; layout 0 returns to the engine. */
+int orc_set_philox(orc_mci *h, uint64_t seed, int64_t chain0, const uint64_t *ctr0, int layout)
+{
+    if (layout < 0 || layout > 2) { return fail(MCIG_ERR_INVALID_ARGUMENT, "layout must be 0, 1 or 2"); }
+    if (layout && (h->movetype == MCIG_MOVE_MULTISTEP || (h->srrd != MCIG_SRRD_UNIFORM && h->srrd != MCIG_SRRD_GAUSSIAN))) {
+        return fail(MCIG_ERR_UNSUPPORTED, "Philox draws: all-coordinate or vector moves with uniform or Gaussian draws");
+    }
+    for (int c = 0; c < h->nchains; ++c) {
+        drawsrc *d = &h->ch[c].ds;
+        d->philox = layout;
+        d->pkey[0] = (uint32_t)seed;
+        d->pkey[1] = (uint32_t)(seed >> 32);
+        d->pchain = (uint32_t)(chain0 + c);
+        d->pctr = ctr0 ? ctr0[c] : 0;
+        d->pmove = h->movetype;
+        d->psrrd = h->srrd;
+        d->pveclen = h->veclen;
+        d->pndim = h->ndim;
+        free(d->pbuf);
+        d->pbuf = layout ? (double *)calloc((size_t)h->ndim + 2, sizeof(double)) : NULL;
+        d->pbuf_n = d->pbuf_pos = 0;
+    }
+    return MCIG_OK;
+}
+
+/* the chains' Philox step counters (steps taken since orc_set_philox set them) */
+int orc_get_philox_counters(orc_mci *h, uint64_t *ctr)
+{
+    for (int c = 0; c < h->nchains; ++c) { ctr[c] = h->ch[c].ds.pctr; }
+    return MCIG_OK;
+}
+
+/* per-chain step sizes steps[nchains][ntypes] (a chain restarted at another's state) */
+int orc_set_chain_steps(orc_mci *h, const double *steps)
+{
+    for (int c = 0; c < h->nchains; ++c) {
+        for (int t = 0; t < nstepsizes(h); ++t) { h->ch[c].step[t] = steps[(size_t)c * nstepsizes(h) + t]; }
+    }
+    return MCIG_OK;
+}
+
+/* the recorded steps' margins log(u) - log(acceptance) (accepted iff <= 0), in the order of
+ * orc_get_accept_bits */
+int64_t orc_get_margins(orc_mci *h, int chain, double *out, int64_t maxn)
+{
+    const chainst *c = &h->ch[chain];
+    if (out) {
+        const int64_t n = c->nbits < maxn ? c->nbits : maxn;
+        memcpy(out, c->marg, (size_t)n * sizeof(double));
+    }
+    return c->nbits;
+}
+
+static void push_bit_margin(chainst *c, int b, double m)
 {
     if (c->nbits == c->capbits) {
         c->capbits = c->capbits ? 2 * c->capbits : 4096;
         c->bits = (uint8_t *)realloc(c->bits, (size_t)c->capbits);
+        c->marg = (double *)realloc(c->marg, (size_t)c->capbits * sizeof(double));
     }
+    c->marg[c->nbits] = m;
     c->bits[c->nbits++] = (uint8_t)b;
 }
+
+static void push_bit(chainst *c, int b) { push_bit_margin(c, b, b ? -INFINITY : INFINITY); }
 
 /* step size of x-index i (TypedMoveInterface::getStepSizeIndex, TypedMoveInterface.hpp:40-48) */
 static int type_of(const orc_mci *h, int i)
@@ -1392,9 +1554,10 @@ static void step_mrt2(const orc_mci *h, chainst *c)
     if (c->nchanged < nd) { domain_apply_sel(h, c->xn, c->nchanged, c->cidx); }
     else { domain_apply_all(h, c->xn); }
     const double pdfAcc = pdfcont_accept(h->npdf, h->pdf, c, c->po, c->pn);
-    c->accepted = (draw_u01(&c->ds) <= pdfAcc * moveAcc);
+    const double u = draw_u01(&c->ds);
+    c->accepted = (u <= pdfAcc * moveAcc);
     if (c->accepted) { ++c->acc; } else { ++c->rej; }
-    if (h->recording) { push_bit(c, c->accepted); }
+    if (h->recording) { push_bit_margin(c, c->accepted, log(u) - log(pdfAcc * moveAcc)); }
     if (c->accepted) {
         pdfcont_copy(h->npdf, h->pdf, c->po, c->pn);
         memcpy(c->x, c->xn, (size_t)nd * sizeof(double));

@@ -71,6 +71,13 @@ int orc_set_record(orc_mci *h, int on);                   /* record tape + accep
 int64_t orc_get_tape(orc_mci *h, int chain, double *out, int64_t maxn); /* returns length */
 int64_t orc_get_accept_bits(orc_mci *h, int chain, uint8_t *out, int64_t maxn, int64_t *main_start);
 int orc_set_replay(orc_mci *h, const double *tape, int64_t stride, const int64_t *lens);
+/* draws of the device kernels' Philox streams (layout 1: float kernels, 2: double kernels,
+ * 0: the engine again); chain c is device chain chain0 + c at step counter ctr0[c] */
+int orc_set_philox(orc_mci *h, uint64_t seed, int64_t chain0, const uint64_t *ctr0, int layout);
+int orc_get_philox_counters(orc_mci *h, uint64_t *ctr);
+int orc_set_chain_steps(orc_mci *h, const double *steps); /* [nchains][ntypes] */
+/* log(u) - log(acceptance) of every recorded step (accepted iff <= 0) */
+int64_t orc_get_margins(orc_mci *h, int chain, double *out, int64_t maxn);
 
 /* integrate: avg/err combined over chains with the MPIMCI formula
  * (mean of averages, sqrt(sum err^2)/nchains); chain_avg/chain_err

@@ -49,9 +49,12 @@ def lib():
         L.orc_last_error.restype = ctypes.c_char_p
         L.orc_get_acceptance_rate.restype = ctypes.c_double
         L.orc_get_acceptance_rate.argtypes = [ctypes.c_void_p]
-        for name in ("orc_get_tape", "orc_get_accept_bits", "orc_get_obs_data", "orc_accumulate_walk"):
+        for name in ("orc_get_tape", "orc_get_accept_bits", "orc_get_obs_data", "orc_accumulate_walk",
+                     "orc_get_margins"):
             getattr(L, name).restype = ctypes.c_int64
         L.orc_set_ndecorrelation_steps.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+        L.orc_set_philox.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int]
+        L.orc_get_margins.argtypes = [ctypes.c_void_p, ctypes.c_int, _c_double_p, ctypes.c_int64]
         L.orc_set_mrt2step.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.orc_set_mrt2step_i.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
         L.orc_set_target_acceptance_rate.argtypes = [ctypes.c_void_p, ctypes.c_double]
@@ -194,6 +197,31 @@ class OracleMCI:
         self._lens = np.ascontiguousarray(lens, dtype=np.int64)
         _check(self.L.orc_set_replay(self._hv(), _dp(self._tape), self._tape.shape[1],
                                      self._lens.ctypes.data_as(_c_int64_p)))
+
+    def set_philox(self, seed, chain0=0, ctr0=None, layout=1):
+        """Draw from the device kernels' Philox streams (layout 1: float kernels, 2: double
+        kernels, 0: back to std::mt19937_64): chain c is device chain chain0 + c."""
+        self._ctr0 = None if ctr0 is None else np.ascontiguousarray(np.asarray(ctr0, dtype=np.uint64))
+        _check(self.L.orc_set_philox(self._hv(), ctypes.c_uint64(int(seed)), ctypes.c_int64(int(chain0)),
+                                     None if self._ctr0 is None else self._ctr0.ctypes.data_as(ctypes.c_void_p),
+                                     int(layout)))
+
+    def philox_counters(self):
+        out = np.zeros(self.nchains, dtype=np.uint64)
+        _check(self.L.orc_get_philox_counters(self._hv(), out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def set_chain_steps(self, steps):
+        """Per-chain step sizes, [nchains][ntypes]."""
+        st = np.ascontiguousarray(np.asarray(steps, dtype=np.float64).reshape(self.nchains, -1))
+        _check(self.L.orc_set_chain_steps(self._hv(), _dp(st)))
+
+    def get_margins(self, chain=0):
+        """log(u) - log(acceptance) of every recorded step (accepted iff <= 0), aligned with get_accept_bits."""
+        n = self.L.orc_get_margins(self._hv(), chain, None, 0)
+        out = np.zeros(n)
+        self.L.orc_get_margins(self._hv(), chain, _dp(out), n)
+        return out
 
     def integrate(self, nmc, do_find=True, do_decorr=True, nthreads=1, per_chain=False):
         nod = max(self.nobsdim(), 1)

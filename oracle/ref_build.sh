@@ -3,7 +3,8 @@
 # sources, where they lie, into oracle/_ref/, and link the golden-vector
 # recorder (oracle/ref_recorder.cpp) against it.  Test infrastructure only.
 #
-# Usage: oracle/ref_build.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/ref_build.sh REFERENCE_ROOT
+#    or: MCIG_REFERENCE_ROOT=... oracle/ref_build.sh
 #
 # The reference's own build system (cmake) is not used: its few sources are
 # compiled directly with g++.  Flags: baseline target (no -march=native, hence
@@ -11,7 +12,11 @@
 # headers the sources use without including them (src/AccumulatorInterface.cpp
 # needs <stdexcept>, others <cmath>, <limits>, <fstream>, <cstdint>).
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${MCIG_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ] || [ ! -d "$REF/src" ]; then
+  echo "usage: $0 REFERENCE_ROOT (or set MCIG_REFERENCE_ROOT to the reference checkout)" >&2
+  exit 2
+fi
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

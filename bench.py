@@ -440,17 +440,25 @@ def c4_target(seed=404):
 
 def run_c4(args):
     """Precision study: 32-D mixture of 8 anisotropic Gaussians, 16,384 chains x 65,536 steps,
-    observables x.x, x_i, x_i^2 in 64-block BlockAccumulators; float walker with Kahan float
-    block sums against the same walker with double block sums (identical trajectories).
-    Metric: walker steps/s of the Kahan-float run."""
+    observables x.x, x_i, x_i^2 in 64-block BlockAccumulators.  Float walker on 8 lanes per
+    chain (mcig_lanes.cuh) with the Metropolis decision certified in double near the float
+    threshold; Kahan float block sums against double block sums (identical trajectories),
+    and the one-lane kernel for comparison.  The FP64 oracle (reference formula, double
+    walker) runs 64 of the chains from the device's burnt-in state on the same Philox draws:
+    the error of the float result against FP64, and the CPU leg (oracle steps/s on the host
+    threads).  Metric: walker steps/s of the Kahan-float run."""
     import mcintegratorplusplus_gb300 as mcig
     params, w, means, widths, m1, m2 = c4_target()
     nch, nmc = args.chains4, args.nmc4
     rng = np.random.default_rng(1)
     comp = rng.choice(C4_NCOMP, nch, p=w)
     x0 = means[comp] + widths[comp] * rng.standard_normal((nch, C4_NDIM))
+    exact = np.concatenate([[m2.sum()], m1, m2])
     out = {}
-    for name, prec in (("f32_kahan", mcig.PREC_FP32), ("f64_sums", mcig.PREC_FP32_ACC64)):
+    runs = (("f32_kahan", mcig.PREC_FP32, 8), ("f64_sums", mcig.PREC_FP32_ACC64, 8), ("one_lane_kahan", mcig.PREC_FP32, 0))
+    clocks = Clocks()
+    clocks.start()
+    for name, prec, lanes in runs:
         m = mcig.MCI(C4_NDIM, nch, precision=prec)
         m.setSeed(31)
         m.addSamplingFunction(mcig.PDF_GAUSS_MIX, params)
@@ -459,35 +467,84 @@ def run_c4(args):
         bs = nmc // 64
         for kind in (mcig.OBS_X2SUM, mcig.OBS_XND, mcig.OBS_X2):
             m.addObservable(kind, (), bs, 1, False, mcig.EST_UNCORRELATED)
-        ms = []
+        if lanes:
+            m.setLanes(lanes)
+            m.setFP64Decision(1)
+        ms, phases = [], {}
         for it in range(args.warmup + args.steps):
             m.setX(x0)
-            avg, err = m.integrate(nmc)
+            m.integrate(0, True, True)  # calibration and burn-in
+            t0 = m.getLastTimings()
+            state = (m.getX(), m.getMRT2Steps(), m.getStepCounters())
+            avg, err = m.integrate(nmc, False, False)
+            t1 = m.getLastTimings()
             if it >= args.warmup:
-                ms.append(_timed_device_ms(m.getLastTimings()))
+                ms.append(_timed_device_ms(t0) + _timed_device_ms(t1))
+                phases = {"calibration_ms": t0["calibration_ms"], "burnin_ms": t0["burnin_ms"],
+                          "sampling_ms": t1["sampling_ms"], "estimation_ms": t1["estimation_ms"]}
         data = np.concatenate([m.getObsData(o) for o in range(3)], axis=1)
         ca, _ = m.getChainResults()
-        out[name] = (float(np.mean(ms)), avg, err, data, ca, m.getLastTimings())
-    t_k = out["f32_kahan"][0] * 1e-3
-    dk, dd = out["f32_kahan"][3], out["f64_sums"][3]
+        stats = m.getDecisionStats() if lanes else None
+        out[name] = {"ms": float(np.mean(ms)), "avg": avg, "err": err, "data": data, "ca": ca, "phases": phases,
+                     "state": state, "stats": stats}
+    ck = clocks.stop()
+    t_k = out["f32_kahan"]["ms"] * 1e-3
+    dk, dd = out["f32_kahan"]["data"], out["f64_sums"]["data"]
     rel = np.abs(dk - dd) / np.maximum(np.abs(dd), 1e-3)
-    exact = np.concatenate([[m2.sum()], m1, m2])
     zs = {}
     for name in out:
-        _, avg, err, _, ca, _ = out[name]
-        sem = ca.std(0) / np.sqrt(nch)
-        zs[name] = float(np.max(np.abs(avg - exact) / sem))
-    return {"metric": "walker steps/s (C4: 16,384 chains x 32-D mixture of 8, float walker, Kahan float sums)",
+        ca = out[name]["ca"]
+        sem = ca.std(0, ddof=1) / np.sqrt(nch)
+        zs[name] = float(np.max(np.abs(ca.mean(0) - exact) / sem))
+    line = {"metric": "walker steps/s (C4: 16,384 chains x 32-D mixture of 8, float walker, Kahan float sums)",
             "value": nch * nmc / t_k, "unit": "walker steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_k * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mixture, chains start in exact samples)",
+            "vs_baseline": None, "dtype": "f32 (Metropolis decision certified in f64 near the threshold)",
+            "data": "synthetic (seeded mixture, chains start in exact samples)",
             "config": {"workload": "C4 precision study", "chains": nch, "ndim": C4_NDIM, "components": C4_NCOMP,
-                       "nmc": nmc, "blocks": 64, "observables": "x.x, x_i, x_i^2",
+                       "nmc": nmc, "blocks": 64, "observables": "x.x, x_i, x_i^2", "lanes_per_chain": 8,
                        "l2": "block output below L2; no flush"},
-            "f64_sums_steps_per_s": nch * nmc / (out["f64_sums"][0] * 1e-3),
-            "phases_ms": {k: {p: float(v) for p, v in out[k][5].items() if p.endswith("_ms")} for k in out},
+            "f64_sums_steps_per_s": nch * nmc / (out["f64_sums"]["ms"] * 1e-3),
+            "one_lane_steps_per_s": nch * nmc / (out["one_lane_kahan"]["ms"] * 1e-3),
+            "phases_ms": {k: out[k]["phases"] for k in out},
+            "fp64_decision": {"steps_tested_in_f64": out["f32_kahan"]["stats"][0],
+                              "float_decisions_reversed": out["f32_kahan"]["stats"][1],
+                              "steps": int(out["f32_kahan"]["state"][2].sum()) + nch * nmc},
             "kahan_vs_double_block_means_max_rel": float(rel.max()),
-            "max_z_vs_analytic": zs}
+            "max_z_vs_analytic": zs, "clocks": ck}
+    if args.cpu_baseline:
+        line["cpu_baseline"], line["error_vs_fp64_oracle"] = c4_oracle_leg(args, out["f32_kahan"], params, nmc)
+    return line
+
+
+def c4_oracle_leg(args, run, params, nmc, K=64):
+    """The FP64 oracle on K chains from the device's burnt-in state, on the device chains' Philox
+    draws: per-chain estimates of the float run against FP64, and the oracle's walker steps/s."""
+    from oracle import oracle as orc
+    x, steps, ctr = run["state"]
+    o = orc.OracleMCI(C4_NDIM, K)
+    o.add_sampling_function(5, params)
+    o.set_trial_move(0, 1, 0)
+    bs = nmc // 64
+    for kind in (0, 1, 2):
+        o.add_observable(kind, (), bs, 1, False, 1)
+    o.set_x(x[:K])
+    o.set_chain_steps(steps[:K])
+    o.set_philox(31, 0, ctr[:K], layout=1)
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    _, _, oca, oce = o.integrate(nmc, False, False, nthreads=nthreads, per_chain=True)
+    dt = time.perf_counter() - t0
+    ca = run["ca"][:K]
+    d = ca - oca
+    sem = oca.std(0, ddof=1) / np.sqrt(K)
+    cpu = {"value": K * nmc / dt, "unit": "walker steps/s", "cores": nthreads, "kind": "port",
+           "sample": "%d chains x %d steps of the workload from the device's burnt-in state, %.1f s" % (K, nmc, dt)}
+    err = {"chains": K, "same_draws": "Philox counters of the device chains (float draws evaluated in double)",
+           "max_abs_diff_per_chain": float(np.abs(d).max()),
+           "median_rel_diff_per_chain": float(np.median(np.abs(d) / np.maximum(np.abs(oca), 1.0))),
+           "combined_max_abs_diff_over_sem": float(np.max(np.abs(d.mean(0)) / sem))}
+    return cpu, err
 
 
 C5_ADAPT = 200  # adaptation cycles (period - 1 local steps + one Adam step on all chain positions)

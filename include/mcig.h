@@ -55,7 +55,8 @@ void *mcig_get_stream(const mcig_mci *h);
 
 /* Kernel choice: 0 automatic (register-resident float kernel where it applies,
  * else the general kernel), 1 general kernel, 2 register-resident kernel
- * (MCIG_ERR_UNSUPPORTED at integrate when the configuration needs the general one). */
+ * (MCIG_ERR_UNSUPPORTED at integrate when the configuration needs the general one),
+ * 3 multi-lane mixture kernel (mcig_set_lanes; MCIG_ERR_UNSUPPORTED where it does not apply). */
 int mcig_set_kernel(mcig_mci *h, int policy);
 /* Phase fusion (default off): where the register-resident kernel serves calibration, a fixed
  * burn-in and the sampling (no file output, no accept recording), integrate runs the three
@@ -74,6 +75,26 @@ int mcig_set_phase_fusion(mcig_mci *h, int on);
  * calibration; only the time changes.  0 turns it off.  No counterpart in the reference,
  * whose MCI::findMRT2Step (src/MCIntegrator.cpp:87-168) calibrates one chain. */
 int mcig_set_calibration_split(mcig_mci *h, int on);
+
+/* Multi-lane mixture kernel (default 0: off): with lpc = 4 or 8, a float handle whose single
+ * sampling function is a mixture of at most 8 Gaussians (17..32 coordinates, all-coordinate
+ * uniform or Gaussian move, one step type, unbound domain) runs its calibration, burn-in and
+ * sampling with lpc lanes per chain: lane group l draws and moves coordinates [l*ndim/lpc,
+ * ...), the proposal is gathered with warp shuffles and each lane evaluates its mixture
+ * components.  Results are bit-identical to the one-lane kernel; the point is occupancy
+ * (16,384 chains fill 3.4 warps of an SM with one lane per chain, 27 with 8).  No
+ * counterpart in the reference, whose MCI runs one chain on one thread. */
+int mcig_set_lanes(mcig_mci *h, int lpc);
+/* Metropolis decision certified in double (the precision form; multi-lane kernel only, else
+ * MCIG_ERR_UNSUPPORTED at integrate).  mode 1: the float log-space test decides unless its
+ * margin |log u - (log p(x') - log p(x))| is below (2^-12 + 2^-18 (|log p(x)| + |log p(x')|)),
+ * where the log densities of the float positions are recomputed in double and the double test
+ * log u <= log p(x') - log p(x) decides (MCI::doStepMRT2, MCIntegrator.cpp:343, in log space).
+ * mode 2 (diagnostic) takes the double test on every step.  mcig_get_decision_stats gives,
+ * for the last integrate, the steps tested in double, how many float decisions the double
+ * test reversed, and the largest float margin among the reversed ones. */
+int mcig_set_fp64_decision(mcig_mci *h, int mode);
+int mcig_get_decision_stats(const mcig_mci *h, int64_t *checked, int64_t *reversed, double *max_margin);
 
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
  * from counter (step, c).  */

@@ -24,15 +24,15 @@ UNITS = {
     "sample_generic_f32": [],
     "sample_generic_f32d": [],
     "sample_fast_all": [],
-    "sample_fast_all32": [],
-    "sample_fast_all32d": [],
     "sample_fast_vec": [],
     "sample_fast_pk16": [],
     "sample_fast_pk32": [],
     "sample_fast_pk32d": [],
+    "sample_fast_pk32p": [],
     "mcig_noalloc": ["-fmad=false"],
     "mcig_flow": [],
     "sample_batch": [],
+    "sample_lanes": [],
 }
 
 
@@ -56,13 +56,32 @@ def _deps():
 FALLBACKS = [[], [], ["-Xptxas", "-O2"], [], ["-Xptxas", "-O1"]]
 
 
+def _up_to_date(unit):
+    """The unit's object is newer than its source and every header it includes (the
+    dependency file nvcc wrote with the object)."""
+    obj = os.path.join(BUILD, unit + ".o")
+    dep = os.path.join(BUILD, unit + ".d")
+    if not (os.path.exists(obj) and os.path.exists(dep)):
+        return False
+    with open(dep) as f:
+        text = f.read().replace("\\\n", " ")
+    files = text.split(":", 1)[1].split() if ":" in text else []
+    t = os.path.getmtime(obj)
+    try:
+        return all(os.path.getmtime(x) < t for x in files)
+    except OSError:
+        return False
+
+
 def _compile(unit, flags, verbose, attempts):
     src = os.path.join(CSRC, unit + ".cu")
     obj = os.path.join(BUILD, unit + ".o")
+    if _up_to_date(unit):
+        return obj
     log = []
     for extra in attempts:
         cmd = [_nvcc()] + ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"] + \
-            flags + extra + ["-c", src, "-o", obj]
+            flags + extra + ["-MD", "-MF", os.path.join(BUILD, unit + ".d"), "-c", src, "-o", obj]
         tmp = os.path.join(BUILD, "tmp_" + unit)  # private temporary directory per unit
         os.makedirs(tmp, exist_ok=True)
         r = subprocess.run(cmd, capture_output=True, text=True, env=dict(os.environ, TMPDIR=tmp))

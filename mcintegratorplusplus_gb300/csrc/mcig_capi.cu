@@ -129,6 +129,9 @@ struct mcig_mci {
     int kernel_policy = 0; // 0 auto, 1 general kernel, 2 register-resident kernel
     int fuse_phases = 0;   // 1: calibration, burn-in and sampling in one register-resident launch
     int calib_split = 1;   // calibration's tail split over lanes where mcig_calib.cuh serves it
+    int lanes = 0;         // lanes per chain of the multi-lane mixture kernel (0: one lane per chain)
+    int f64_decide = 0;    // Metropolis decision certified in double (multi-lane kernel): 0 off, 1, 2
+    DBuf<unsigned long long> dstats; // [checked, reversed, largest reversed float margin (float bits)]
     FastConst fc;          // constant data of the register-resident kernel
     // device chain state
     DBuf<double> x, step;
@@ -1009,6 +1012,8 @@ static int fill_common(mcig_mci *h, KParams &kp)
     kp.nfind = h->nfind;
     kp.target = h->target;
     kp.status = h->status.p;
+    kp.f64_decide = h->f64_decide;
+    kp.dstats = h->f64_decide ? h->dstats.p : nullptr;
     return MCIG_OK;
 }
 
@@ -1024,6 +1029,11 @@ static bool fast_eligible(const mcig_mci *h)
     for (auto &o : h->obs) {
         if (o.kind == MCIG_OBS_GAUSSX2) { return false; }
     }
+    if (maxd_bucket(h->ndim) == 32) { // 17..32 coordinates: the one-pdf kernels only
+        if (h->pdfs.size() != 1) { return false; }
+        const int k = h->pdfs[0].kind;
+        if (k != MCIG_PDF_GAUSS && k != MCIG_PDF_GAUSS_SUM && k != MCIG_PDF_GAUSS_PREC && k != MCIG_PDF_GAUSS_MIX) { return false; }
+    }
     int nprec = 0, nmix = 0; // one precision matrix and one mixture (<= 8 components) fit the parameter block
     for (auto &d : h->pdfs) {
         nprec += d.kind == MCIG_PDF_GAUSS_PREC;
@@ -1033,8 +1043,37 @@ static bool fast_eligible(const mcig_mci *h)
     return nprec <= 1 && nmix <= 1;
 }
 
+// the multi-lane mixture kernel (mcig_lanes.cuh) serves float walkers with an all-coordinate
+// uniform or Gaussian move, one step type, the unbound domain, one mixture sampling function
+// of at most 8 components, 17..32 coordinates and observables without exp()
+static bool lanes_eligible(const mcig_mci *h)
+{
+    if (uses_plugin(h) || h->prec == MCIG_PREC_FP64 || h->replay || h->periodic) { return false; }
+    if (h->ndim < 17 || h->ndim > 32 || h->movetype != MCIG_MOVE_ALL || h->ntypes != 1) { return false; }
+    if (h->srrd != MCIG_SRRD_UNIFORM && h->srrd != MCIG_SRRD_GAUSSIAN) { return false; }
+    if (h->pdfs.size() != 1 || h->pdfs[0].kind != MCIG_PDF_GAUSS_MIX || (int)h->pdfs[0].params[0] > 8) { return false; }
+    for (auto &o : h->obs) {
+        if (o.kind == MCIG_OBS_GAUSSX2 || o.kind == MCIG_OBS_X2BLOCK || o.kind >= MCIG_OBS_USER) { return false; }
+    }
+    return true;
+}
+
 static int launch(mcig_mci *h, const KParams &kp)
 {
+    // several lanes per chain: the calibration, burn-in and sampling launches of the mixture
+    // configurations it serves, when asked for (mcig_set_lanes, or kernel policy 3)
+    const bool want_lanes = kp.ndump == 0 && kp.mode != KMODE_FUSED &&
+                            (h->kernel_policy == 3 || (h->kernel_policy == 0 && h->lanes > 0));
+    if (want_lanes && kp.nsteps < ((int64_t)1 << 31) && lanes_eligible(h)) {
+        mcig_launch_fn lf = mcig_lanes_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, 32, h->lanes > 0 ? h->lanes : 8);
+        if (!lf) { return set_err(MCIG_ERR_UNSUPPORTED, "no multi-lane kernel for %d lanes per chain", h->lanes); }
+        lf(kp, &h->fc, h->movetype, 0, 0, 0, h->stream);
+        ++h->launches;
+        CK(cudaGetLastError());
+        return MCIG_OK;
+    }
+    if (h->kernel_policy == 3) { return set_err(MCIG_ERR_UNSUPPORTED, "configuration not served by the multi-lane kernel"); }
+    if (h->f64_decide) { return set_err(MCIG_ERR_UNSUPPORTED, "the FP64-certified decision runs in the multi-lane mixture kernel only (mcig_set_lanes)"); }
     // 64 threads per block (MCIG_FAST_BLOCK): with ~140 registers per thread
     // seven blocks fit an SM, so 65,536 chains are resident in one wave, and
     // small batches still spread over every SM
@@ -1090,9 +1129,49 @@ extern "C" int mcig_set_calibration_split(mcig_mci *h, int on)
     return MCIG_OK;
 }
 
+extern "C" int mcig_set_lanes(mcig_mci *h, int lpc)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    if (lpc != 0 && lpc != 4 && lpc != 8) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "lanes per chain must be 0, 4 or 8"); }
+    h->lanes = lpc;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_set_fp64_decision(mcig_mci *h, int mode)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    if (mode < 0 || mode > 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "FP64 decision mode must be 0, 1 or 2"); }
+    if (mode && !h->dstats.p) {
+        cudaSetDevice(h->device);
+        int rc = h->dstats.alloc(3);
+        if (rc) { return rc; }
+    }
+    h->f64_decide = mode;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_get_decision_stats(const mcig_mci *h, int64_t *checked, int64_t *reversed, double *max_margin)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    unsigned long long v[3] = {0, 0, 0};
+    if (h->dstats.p) {
+        cudaSetDevice(h->device);
+        CK(cudaMemcpy(v, h->dstats.p, sizeof(v), cudaMemcpyDeviceToHost));
+    }
+    if (checked) { *checked = (int64_t)v[0]; }
+    if (reversed) { *reversed = (int64_t)v[1]; }
+    if (max_margin) {
+        const uint32_t b = (uint32_t)v[2];
+        float f;
+        memcpy(&f, &b, sizeof(f));
+        *max_margin = (double)f;
+    }
+    return MCIG_OK;
+}
+
 extern "C" int mcig_set_kernel(mcig_mci *h, int policy)
 {
-    if (policy < 0 || policy > 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "kernel policy must be 0 (auto), 1 (general) or 2 (register-resident)"); }
+    if (policy < 0 || policy > 3) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "kernel policy must be 0 (auto), 1 (general), 2 (register-resident) or 3 (multi-lane)"); }
     h->kernel_policy = policy;
     return MCIG_OK;
 }
@@ -1670,6 +1749,7 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
     h->launches = 0;
     for (double &m : h->ms) { m = 0.; }
     CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
+    if (h->f64_decide) { CK(cudaMemsetAsync(h->dstats.p, 0, 3 * sizeof(unsigned long long), h->stream)); }
     KParams kp;
     if ((rc = fill_common(h, kp))) { return rc; }
     // device buffers first, so that allocation stays outside the timed phases

@@ -64,6 +64,7 @@ struct ObsDesc {
     // n / d == __umulhi(n, magic) >> shift for n < 2^31 (register-resident kernel)
     uint32_t bs_magic, bs_shift, sk_magic, sk_shift;
     double inv_bs; // 1. / bs (Block normalisation, BlockAccumulator.cpp)
+    int lslot;     // multi-lane kernel (mcig_lanes.cuh): first accumulator slot of a lane
 };
 
 struct KParams {
@@ -116,6 +117,11 @@ struct KParams {
     const double *step_max_i; // periodic: 0.5*(ub-lb) per index
     // error reporting
     int *status;
+    // multi-lane mixture kernel (mcig_lanes.cuh): Metropolis decision certified in double near
+    // the float threshold (1), or on every step (2, diagnostic), with counters [checked,
+    // reversed, largest float margin of a reversed decision as float bits] (NULL: none)
+    int f64_decide;
+    unsigned long long *dstats;
 };
 
 // Register-resident kernel only: Philox round keys (key + r*W for r = 0..9), the

@@ -20,6 +20,11 @@ mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk);
 // one sampling function of kind pk (PK_GAUSS or PK_PREC); NULL otherwise
 mcig_launch_fn mcig_calib_launcher_pk16(int pk);
 
+// float kernel with several lanes per chain for one mixture sampling function
+// (mcig_lanes.cuh): all-coordinate move, one step type, unbound domain, maxd 32, lpc 4 or 8
+// lanes per chain; NULL otherwise
+mcig_launch_fn mcig_lanes_launcher(int kahan, int maxd, int lpc);
+
 // general kernel of a plugin (include/mcig/plugin.cuh) over its user functors: launches and
 // returns the launch's cudaError_t of the plugin's own CUDA runtime
 typedef int (*mcig_plugin_launch_fn)(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st);

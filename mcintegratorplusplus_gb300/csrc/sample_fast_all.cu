@@ -1,9 +1,11 @@
-// Register-resident float sampling kernels, all-coordinate move, up to 16
-// dimensions (mcig_fast.cuh); 32 dimensions are in sample_fast_all32.cu.
+// Register-resident float sampling kernels, all-coordinate move, up to 16 dimensions
+// (mcig_fast.cuh).  At 17..32 dimensions the register-resident kernels exist for a single
+// sampling function of one kind (sample_fast_pk32*.cu); other 32-D configurations run
+// the general kernel (a 32-D kernel over every sampling-function kind took over five
+// minutes to compile).
 #include "mcig_fast.cuh"
 #include "mcig_launchers.h"
 
-mcig_launch_fn mcig_fast_launcher_all32(int kahan);
 mcig_launch_fn mcig_fast_launcher_vec(int kahan, int maxd);
 mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk);
 mcig_launch_fn mcig_fast_launcher_pk32(int kahan, int pk);
@@ -14,7 +16,6 @@ static mcig_launch_fn launcher_all(int kahan, int maxd)
     case 4: return kahan ? mcig_fast_launch<4, MCIG_MOVE_ALL, true> : mcig_fast_launch<4, MCIG_MOVE_ALL, false>;
     case 8: return kahan ? mcig_fast_launch<8, MCIG_MOVE_ALL, true> : mcig_fast_launch<8, MCIG_MOVE_ALL, false>;
     case 16: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true> : mcig_fast_launch<16, MCIG_MOVE_ALL, false>;
-    case 32: return mcig_fast_launcher_all32(kahan);
     default: return nullptr;
     }
 }

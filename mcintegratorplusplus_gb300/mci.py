@@ -117,6 +117,20 @@ class MCI:
         """Calibration's tail on 4 lanes per chain where it applies (default on; same results)."""
         _raise(self.L.mcig_set_calibration_split(self._h, int(bool(on))))
 
+    def setLanes(self, lpc):
+        """Lanes per chain of the multi-lane mixture kernel (0 off, 4 or 8)."""
+        _raise(self.L.mcig_set_lanes(self._h, int(lpc)))
+
+    def setFP64Decision(self, mode=1):
+        """Metropolis decision certified in double near the float threshold (1), on every step (2), off (0)."""
+        _raise(self.L.mcig_set_fp64_decision(self._h, int(mode)))
+
+    def getDecisionStats(self):
+        """(steps tested in double, float decisions reversed, largest reversed float margin) of the last integrate."""
+        a, b, m = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        _raise(self.L.mcig_get_decision_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(m)))
+        return a.value, b.value, m.value
+
     def setPrecision(self, precision):
         _raise(self.L.mcig_set_precision(self._h, int(precision)))
 

@@ -147,11 +147,19 @@ def test_fast_kernel_against_fp64_oracle_same_draws(prec_name, split):
     if whole.any():
         rel = np.abs(ca[:K_ORACLE][whole] - oca[whole]) / np.maximum(np.abs(oca[whole]), 1.0)
         assert rel.max() < 1e-4, rel.max()
-    # combined over the oracle's chains: the float result lies well inside the error bar
+    # combined over the oracle's chains: the float result against the FP64 one, in units of
+    # the standard error from the spread of the chain means (the chains that part become
+    # independent samples of the same target, the others agree to float rounding)
     dev_k = ca[:K_ORACLE].mean(0)
     orc_k = oca.mean(0)
-    err_k = np.sqrt((oce ** 2).sum(0)) / K_ORACLE
-    assert np.all(np.abs(dev_k - orc_k) < err_k), (np.abs(dev_k - orc_k) / err_k).max()
+    sem_k = oca.std(0, ddof=1) / np.sqrt(K_ORACLE)
+    zk = np.abs(dev_k - orc_k) / sem_k
+    assert zk.max() < 3.0, zk
+    print("\nfloat kernel vs FP64 oracle (%s, split %s): calibration identical %d/%d, burn-in identical %d/%d, "
+          "sampling: %d/%d chains follow all %d steps, first parting step of the others %s, "
+          "per-chain estimates of followed chains max rel diff %.2e, combined |f32 - f64| / sem max %.3f"
+          % (prec_name, split, same.sum(), K_ORACLE, int(np.sum(dx <= 1e-4)), K_ORACLE, int(whole.sum()), K_ORACLE,
+             NMC, sorted(int(t) for t in first_part[~whole]), rel.max() if whole.any() else float("nan"), zk.max()))
 
     # --- (b) the whole 256-chain run against the analytic target: x.x -> tr Sigma, x_i -> 0,
     # errors from the spread of the chain means (chains are independent)

@@ -96,6 +96,15 @@ int mcig_set_lanes(mcig_mci *h, int lpc);
 int mcig_set_fp64_decision(mcig_mci *h, int mode);
 int mcig_get_decision_stats(const mcig_mci *h, int64_t *checked, int64_t *reversed, double *max_margin);
 
+/* Chunked sampling (default 4; 1 turns it off): where the register-resident one-lane kernel
+ * samples, no observable uses a SimpleAccumulator and float FullAccumulator samples take the
+ * Uncorrelated estimator, the main sampling runs as n launches of equal length (a multiple of
+ * every block length), and the estimator of each finished chunk's Full rows runs on a
+ * low-priority stream beside the next launch.  Results are identical to one launch and the
+ * one-pass estimator; the estimation's pass over the Full samples overlaps the sampling.
+ * No counterpart in the reference, whose MCI::sample (MCIntegrator.cpp:290-321) is one loop. */
+int mcig_set_sampling_chunks(mcig_mci *h, int n);
+
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
  * from counter (step, c).  */
 int mcig_set_seed(mcig_mci *h, uint64_t seed);

@@ -101,6 +101,8 @@ struct mcig_plugin {
     mcig_plugin_launch_fn (*launcher)(int, int) = nullptr;
 };
 
+#define MCIG_MAX_CHUNKS 8
+
 struct mcig_mci {
     int ndim;
     const mcig_plugin *plugin = nullptr; // user functors (MCIG_PDF_USER / MCIG_OBS_USER kinds)
@@ -163,6 +165,12 @@ struct mcig_mci {
     double ms[4] = {0, 0, 0, 0};
     int64_t launches = 0;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // chunked sampling (mcig_set_sampling_chunks): the Uncorrelated estimator of float Full
+    // samples runs on a low-priority stream over each finished chunk beside the next one
+    int chunks = 4;
+    cudaStream_t est_stream = nullptr;
+    cudaEvent_t cev[MCIG_MAX_CHUNKS + 1] = {};
+    DBuf<float4> est_state;
 };
 
 static int nobsdim(const mcig_mci *h)
@@ -347,7 +355,9 @@ extern "C" int mcig_create(int ndim, int64_t nchains, int device, int precision,
     h->device = device;
     h->prec = precision;
     h->typeEnds[0] = ndim;
-    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    int prio_low = 0, prio_high = 0; // the handle's stream gets the highest priority, so that the
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high); // chunk estimators never hold back sampling
+    cudaError_t e = cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_high);
     if (e != cudaSuccess) {
         delete h;
         return set_err(MCIG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
@@ -445,6 +455,9 @@ extern "C" int mcig_destroy(mcig_mci *h)
     h->active.release(); h->bits.release();
     for (auto &b : h->obsdata) { b.release(); }
     for (auto &ev : h->ev) { if (ev) { cudaEventDestroy(ev); } }
+    for (auto &ev : h->cev) { if (ev) { cudaEventDestroy(ev); } }
+    h->est_state.release(); h->dstats.release();
+    if (h->est_stream) { cudaStreamSynchronize(h->est_stream); cudaStreamDestroy(h->est_stream); }
     if (h->stream) { cudaStreamDestroy(h->stream); }
     delete h;
     return MCIG_OK;
@@ -1058,13 +1071,25 @@ static bool lanes_eligible(const mcig_mci *h)
     return true;
 }
 
-static int launch(mcig_mci *h, const KParams &kp)
+// the kernel family a launch of kp runs: 2 the multi-lane mixture kernel, 1 the
+// register-resident one-lane kernel, 0 the general kernel (or a plugin's)
+static int kernel_family(const mcig_mci *h, const KParams &kp)
 {
+    const bool small_n = kp.nsteps < ((int64_t)1 << 31); // 32-bit step counters in the register-resident kernels
     // several lanes per chain: the calibration, burn-in and sampling launches of the mixture
     // configurations it serves, when asked for (mcig_set_lanes, or kernel policy 3)
     const bool want_lanes = kp.ndump == 0 && kp.mode != KMODE_FUSED &&
                             (h->kernel_policy == 3 || (h->kernel_policy == 0 && h->lanes > 0));
-    if (want_lanes && kp.nsteps < ((int64_t)1 << 31) && lanes_eligible(h)) {
+    if (want_lanes && small_n && lanes_eligible(h)) { return 2; }
+    // file output is recorded by the general kernel
+    const bool fast = kp.ndump == 0 && (h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n));
+    return fast ? 1 : 0;
+}
+
+static int launch(mcig_mci *h, const KParams &kp)
+{
+    const int family = kernel_family(h, kp);
+    if (family == 2) {
         mcig_launch_fn lf = mcig_lanes_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, 32, h->lanes > 0 ? h->lanes : 8);
         if (!lf) { return set_err(MCIG_ERR_UNSUPPORTED, "no multi-lane kernel for %d lanes per chain", h->lanes); }
         lf(kp, &h->fc, h->movetype, 0, 0, 0, h->stream);
@@ -1079,9 +1104,8 @@ static int launch(mcig_mci *h, const KParams &kp)
     // small batches still spread over every SM
     const int block = MCIG_FAST_BLOCK;
     const int grid = (int)((h->nchains + block - 1) / block);
-    const bool small_n = kp.nsteps < ((int64_t)1 << 31); // 32-bit step counters in the register-resident kernel
-    // file output is recorded by the general kernel
-    const bool fast = kp.ndump == 0 && (h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n));
+    const bool small_n = kp.nsteps < ((int64_t)1 << 31);
+    const bool fast = family == 1;
     mcig_launch_fn fn = nullptr;
     size_t smem = (size_t)kp.fblob_len * sizeof(float);
     if (fast) {
@@ -1420,7 +1444,7 @@ static int validate_accumulators(const mcig_mci *h, int64_t nmc)
 // estimators of all observables -> per-chain avg/err (host vectors [nchains][nod])
 static int estimate_all(mcig_mci *h, const std::vector<ObsDef> &obs, const std::vector<DBuf<char>> &bufs,
                         const std::vector<int64_t> &nstore, int full32, std::vector<double> &cavg, std::vector<double> &cerr,
-                        bool to_host = true)
+                        bool to_host = true, const std::vector<char> *done = nullptr)
 {
     int nod = 0;
     for (auto &o : obs) { nod += o.nv; }
@@ -1429,6 +1453,10 @@ static int estimate_all(mcig_mci *h, const std::vector<ObsDef> &obs, const std::
     if ((rc = h->est_avg.alloc(nc * std::max(nod, 1))) || (rc = h->est_err.alloc(nc * std::max(nod, 1)))) { return rc; }
     int off = 0;
     for (size_t o = 0; o < obs.size(); ++o) {
+        if (done && (*done)[o]) { // estimated chunk by chunk beside the sampling (sample_chunked)
+            off += obs[o].nv;
+            continue;
+        }
         const int is_float = (obs[o].acc == MCIG_ACC_FULL && full32) ? 1 : 0;
         rc = run_estimator(h, obs[o].estimator, bufs[o].p, is_float, nstore[o], obs[o].nv, (int)nc, h->est_avg.p,
                            h->est_err.p, nod, off, h->scratch, h->stream, &h->launches);
@@ -1735,6 +1763,107 @@ static int write_dump_files(mcig_mci *h, int64_t nmc, const std::vector<int64_t>
     return MCIG_OK;
 }
 
+extern "C" int mcig_set_sampling_chunks(mcig_mci *h, int n)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    if (n < 1 || n > MCIG_MAX_CHUNKS) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "chunks must be in [1, %d]", MCIG_MAX_CHUNKS); }
+    h->chunks = n;
+    return MCIG_OK;
+}
+
+static int64_t gcd64(int64_t a, int64_t b) { return b ? gcd64(b, a % b) : a; }
+
+// MCI::sample of the main run (MCIntegrator.cpp:290-321) as one launch, or, where the
+// register-resident kernel samples and float Full samples take the Uncorrelated estimator,
+// as h->chunks launches of equal length (a multiple of every block length, so no block
+// spans two launches): the estimator of each finished chunk's Full rows runs on a
+// low-priority stream beside the next chunk's sampling, which is bound by instruction issue
+// and leaves HBM bandwidth and issue slots to it.  Results are those of one launch and of
+// the one-pass estimator (same Philox counters, accumulation indices and Kahan add order).
+static int sample_chunked(mcig_mci *h, const KParams &kp, int64_t nmc, std::vector<char> &est_done)
+{
+    KParams s = kp;
+    s.mode = KMODE_SAMPLE;
+    for (size_t o = 0; o < h->obs.size(); ++o) {
+        s.obs[o].data = h->obsdata[o].p;
+        s.obs[o].nstore = h->obs_nstore[o];
+    }
+    bool chunk = h->chunks > 1 && kernel_family(h, s) == 1 && h->full32;
+    int64_t q = 1; // chunk lengths are multiples of q
+    bool any_full = false;
+    for (auto &o : h->obs) {
+        if (o.acc == MCIG_ACC_SIMPLE) { chunk = false; }
+        const int64_t unit = o.acc == MCIG_ACC_BLOCK ? (int64_t)o.blocksize * o.nskip : o.nskip;
+        q = q / gcd64(q, unit) * unit;
+        any_full |= o.acc == MCIG_ACC_FULL && o.estimator == MCIG_EST_UNCORRELATED;
+    }
+    const int64_t len = q * ((nmc / h->chunks + q - 1) / q);
+    chunk = chunk && any_full && len < nmc && q <= nmc / 2;
+    if (!chunk) {
+        s.nsteps = nmc;
+        return launch(h, s);
+    }
+    int rc;
+    if (!h->est_stream) {
+        int prio_low = 0, prio_high = 0;
+        cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+        CK(cudaStreamCreateWithPriority(&h->est_stream, cudaStreamNonBlocking, prio_low));
+        for (auto &e : h->cev) { CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming)); }
+    }
+    // estimator outputs and the running Kahan sums of every chunk-estimated series
+    int nod = 0;
+    size_t nstate = 0;
+    for (auto &o : h->obs) {
+        nod += o.nv;
+        if (o.acc == MCIG_ACC_FULL && o.estimator == MCIG_EST_UNCORRELATED) { nstate += (size_t)o.nv * h->nchains; }
+    }
+    const size_t nc = (size_t)h->nchains;
+    if ((rc = h->est_avg.alloc(nc * std::max(nod, 1))) || (rc = h->est_err.alloc(nc * std::max(nod, 1))) ||
+        (rc = h->est_state.alloc(nstate))) {
+        return rc;
+    }
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
+    int j = 0;
+    for (int64_t r0 = 0; r0 < nmc; r0 += len, ++j) {
+        s.nsteps = std::min(len, nmc - r0);
+        s.r0 = r0;
+        s.acc_counts = r0 > 0;
+        if ((rc = launch(h, s))) { return rc; }
+        CK(cudaEventRecord(h->cev[j], h->stream));
+        CK(cudaStreamWaitEvent(h->est_stream, h->cev[j], 0));
+        size_t soff = 0;
+        int off = 0;
+        for (size_t o = 0; o < h->obs.size(); ++o) {
+            const ObsDef &d = h->obs[o];
+            if (d.acc == MCIG_ACC_FULL && d.estimator == MCIG_EST_UNCORRELATED) {
+                EstArgs a;
+                memset(&a, 0, sizeof(a));
+                a.data = h->obsdata[o].p;
+                a.is_float = 1;
+                a.n = h->obs_nstore[o];
+                a.nv = d.nv;
+                a.nchains = (int)nc;
+                a.avg = h->est_avg.p;
+                a.err = h->est_err.p;
+                a.ldo = nod;
+                a.off = off;
+                a.one_d = (d.nv == 1);
+                // rows of the accumulations of steps [r0, r0 + nsteps)
+                const int64_t i0 = (r0 + d.nskip - 1) / d.nskip, i1 = (r0 + s.nsteps + d.nskip - 1) / d.nskip;
+                est_uncorr_f32_chunk_kernel<<<2 * nsm, 128, 0, h->est_stream>>>(a, i0, i1, h->est_state.p + soff);
+                ++h->launches;
+                CK(cudaGetLastError());
+                est_done[o] = 1;
+                soff += (size_t)d.nv * nc;
+            }
+            off += d.nv;
+        }
+    }
+    CK(cudaEventRecord(h->cev[MCIG_MAX_CHUNKS], h->est_stream)); // joined before the other estimators
+    return MCIG_OK;
+}
+
 extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double *error, int do_find, int do_decorr)
 {
     if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
@@ -1806,7 +1935,10 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
         }
     }
     if (!fuse) { CK(cudaEventRecord(h->ev[2], h->stream)); }
-    if (nmc > 0 && !fuse) {
+    std::vector<char> est_done(h->obs.size(), 0);
+    if (nmc > 0 && !fuse && dump.empty() && !h->record) {
+        if ((rc = sample_chunked(h, kp, nmc, est_done))) { return rc; }
+    } else if (nmc > 0 && !fuse) {
         KParams s = kp;
         s.mode = KMODE_SAMPLE;
         s.nsteps = nmc;
@@ -1832,8 +1964,12 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
         }
     }
     CK(cudaEventRecord(h->ev[3], h->stream));
+    if (std::find(est_done.begin(), est_done.end(), 1) != est_done.end()) { // the chunk estimators' stream
+        CK(cudaStreamWaitEvent(h->stream, h->cev[MCIG_MAX_CHUNKS], 0));
+    }
     if (nmc > 0) {
-        if ((rc = estimate_all(h, h->obs, h->obsdata, h->obs_nstore, h->full32, h->chain_avg, h->chain_err, false))) {
+        if ((rc = estimate_all(h, h->obs, h->obsdata, h->obs_nstore, h->full32, h->chain_avg, h->chain_err, false,
+                               &est_done))) {
             return rc;
         }
     }

@@ -99,6 +99,9 @@ struct KParams {
     int64_t *nacc, *nrej;   // counts of this launch (KMODE_CALIB: of the last iteration)
     uint8_t *bits;          // optional [nsteps][nchains] accept record
     int64_t acc_offset;     // Full accumulators: row of this launch's first accumulation
+    int64_t r0;             // register-resident kernel, chunked sampling: step index of this launch's
+                            // first step in the whole sampling run (accumulation and block indices)
+    int acc_counts;         // 1: add this launch's counts to nacc/nrej (later chunks of a run)
     const uint8_t *active;  // optional: chains with active[c] == 0 skip this launch
     // file output (storeObservablesOnFile / storeWalkerPositionsOnFile): chain 0 records
     // its walker after the steps dump_steps[0..ndump) (ascending) into dump_x[ndump][ndim]
@@ -144,14 +147,12 @@ __device__ __forceinline__ P4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c
                                             uint32_t k1)
 {
 #pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        const uint32_t lo0 = 0xD2511F53u * c0;
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
-        const uint32_t lo1 = 0xCD9E8D57u * c2;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
-        const uint32_t n0 = hi1 ^ c1 ^ k0;
-        const uint32_t n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    for (int r = 0; r < 10; ++r) { // each 32x32 -> 64-bit product is one wide multiply
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
         k0 += 0x9E3779B9u;
         k1 += 0xBB67AE85u;
     }
@@ -168,13 +169,11 @@ __device__ __forceinline__ P4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_
 {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
-        const uint32_t lo0 = 0xD2511F53u * c0;
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
-        const uint32_t lo1 = 0xCD9E8D57u * c2;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
-        const uint32_t n0 = hi1 ^ c1 ^ rk[2 * r];
-        const uint32_t n2 = hi0 ^ c3 ^ rk[2 * r + 1];
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ rk[2 * r];
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ rk[2 * r + 1];
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
     }
     return P4{c0, c1, c2, c3};
 }

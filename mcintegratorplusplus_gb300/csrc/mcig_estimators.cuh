@@ -96,6 +96,51 @@ static __global__ void est_uncorr_f32_kernel(EstArgs a)
     est_store(a, s, average, e);
 }
 
+// The same estimator over rows [i0, i1) of the data, for sampling that runs in chunks:
+// the Kahan sums of each series continue from `state` (zero for i0 == 0) and are saved
+// there, and the chunk that ends at row a.n forms the result.  Every series sees the add
+// sequence of est_uncorr_f32_kernel, so the result is that kernel's bit for bit.  A small
+// grid strides over the series: the kernel runs beside the next chunk's sampling launch
+// and reads the finished rows while the sampling kernel is bound by instruction issue.
+static __global__ void est_uncorr_f32_chunk_kernel(EstArgs a, int64_t i0, int64_t i1, float4 *state)
+{
+    const int64_t S = (int64_t)a.nv * a.nchains;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < S; s += (int64_t)gridDim.x * blockDim.x) {
+        const float *d = (const float *)a.data + s;
+        float4 st = i0 > 0 ? state[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float s1 = st.x, c1 = st.y, s2 = st.z, c2 = st.w;
+        auto add = [&](float x) {
+            float y = x - c1, t = s1 + y;
+            c1 = (t - s1) - y;
+            s1 = t;
+            y = x * x - c2;
+            t = s2 + y;
+            c2 = (t - s2) - y;
+            s2 = t;
+        };
+        int64_t i = i0;
+        for (; i + 32 <= i1; i += 32) {
+            float x[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) { x[k] = d[(i + k) * S]; }
+#pragma unroll
+            for (int k = 0; k < 32; ++k) { add(x[k]); }
+        }
+        for (; i < i1; ++i) { add(d[i * S]); }
+        if (i1 < a.n) {
+            state[s] = make_float4(s1, c1, s2, c2);
+            continue;
+        }
+        const double SMALLEST_ERROR = 1.e-300;
+        const double norm = 1. / a.n;
+        const double average = ((double)s1 - (double)c1) * norm;
+        double e = ((double)s2 - (double)c2) * norm - average * average;
+        if (a.one_d) { e = (e > SMALLEST_ERROR) ? sqrt(e / (a.n - 1.)) : 0.; }
+        else { e = (e > SMALLEST_ERROR) ? sqrt(e * (1. / (a.n - 1.))) : 0.; }
+        est_store(a, s, average, e);
+    }
+}
+
 static __global__ void est_noop_kernel(EstArgs a)
 { // NoopEstimator (:289-293): the first row is the result
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

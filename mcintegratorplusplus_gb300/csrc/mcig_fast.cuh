@@ -407,15 +407,16 @@ struct FastSampler {
         lp = fast_logp<MAXD, PK>(p, fc, x);
         for (int j = 0; j < p.nobsdim && sample; ++j) { Slot::zero(slot(j)); }
         const uint32_t n32 = (uint32_t)n;
+        const uint32_t r0 = (uint32_t)p.r0; // chunked sampling: global index of the first step
         uint32_t na = 0;
         for (uint32_t r = 0; r < n32; ++r) {
             na += step() ? 1u : 0u;
             if (!sample) { continue; }
 #pragma unroll
             for (int o = 0; o < MCIG_FAST_UNROLLED_OBS; ++o) {
-                if (o < p.nobs) { obs_step(p.obs[o], r); }
+                if (o < p.nobs) { obs_step(p.obs[o], r0 + r); }
             }
-            for (int o = MCIG_FAST_UNROLLED_OBS; o < p.nobs; ++o) { obs_step(p.obs[o], r); }
+            for (int o = MCIG_FAST_UNROLLED_OBS; o < p.nobs; ++o) { obs_step(p.obs[o], r0 + r); }
         }
         if (sample) {
             for (int o = 0; o < p.nobs; ++o) { // SimpleAccumulator::_finalize
@@ -426,8 +427,13 @@ struct FastSampler {
                 for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = Slot::get(slot(od.voff + j)) * normf; }
             }
         }
-        p.nacc[c] = na;
-        p.nrej[c] = n - na;
+        if (p.acc_counts) {
+            p.nacc[c] += na;
+            p.nrej[c] += n - na;
+        } else {
+            p.nacc[c] = na;
+            p.nrej[c] = n - na;
+        }
     }
 
     // MCI::findMRT2Step (MCIntegrator.cpp:87-168) for this chain alone

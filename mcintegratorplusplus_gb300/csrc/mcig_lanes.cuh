@@ -7,9 +7,9 @@
 // the LPC lanes of a chain share its work:
 //   * lane group l owns coordinates [l CPL, (l+1) CPL), CPL = MAXD / LPC, i.e. the Philox
 //     move blocks l CPL / 4 ... of the step: it draws and moves only its coordinates;
-//   * the proposal is gathered into every lane with warp shuffles (MAXD values);
-//   * lane group l evaluates mixture components l, l + LPC, ... over the whole proposal,
-//     each component's sum in ascending coordinate order (the one-lane kernel's order);
+//   * the proposal's coordinates reach every lane by warp shuffles, a pair at a time, and
+//     lane group l adds them into mixture components l, l + LPC, ..., each component's sum
+//     in ascending coordinate order (the one-lane kernel's order);
 //   * the maximum over components is a butterfly over the chain's lanes (exact), each lane
 //     exponentiates its own components, and every lane sums the gathered terms in
 //     component order.
@@ -138,35 +138,48 @@ struct LaneMixSampler {
         for (int m = 0; m < CPL; ++m) { sto[m] = (l * CPL + m < p.ndim) ? st[0] : 0.f; }
     }
 
-    __device__ __forceinline__ void gather(const float (&own)[CPL], float (&full)[MAXD]) const
+    // fast_logp_mix<MAXD> of the chain's vector whose own coordinates this lane holds in
+    // `own`, same operation order; the coordinates are gathered one pair at a time as the
+    // component sums consume them (no MAXD-register copy of the vector), and x.x and the sum
+    // of the coordinates (one-lane order: i ascending) are formed in the same pass
+    __device__ __forceinline__ float logp(const float (&own)[CPL], float &xxo, float &sxo) const
     {
+        float a[CPP];
 #pragma unroll
-        for (int i = 0; i < MAXD; ++i) { full[i] = __shfl_sync(FULL, own[i % CPL], (i / CPL) * G + k); }
-    }
-
-    // fast_logp_mix<MAXD> of the gathered vector, same operation order
-    __device__ __forceinline__ float logp(const float (&xf)[MAXD]) const
-    {
+        for (int r = 0; r < CPP; ++r) { a[r] = 0.f; }
+        float xx2 = 0.f, sx2 = 0.f;
+#pragma unroll
+        for (int i = 0; i < MAXD; i += 2) {
+            // at most 8 table loads in flight: the compiler would otherwise hoist all of
+            // them (4 registers each) and spill
+            if (i % 16 == 0) { asm volatile("" ::: "memory"); }
+            const float x0 = __shfl_sync(FULL, own[i % CPL], (i / CPL) * G + k);
+            const float x1 = __shfl_sync(FULL, own[(i + 1) % CPL], ((i + 1) / CPL) * G + k);
+#pragma unroll
+            for (int r = 0; r < CPP; ++r) {
+                const float4 t = tab[(l + LPC * r) * TS + i / 2];
+                float z = (x0 - t.x) * t.y;
+                a[r] = fmaf(z, z, a[r]);
+                z = (x1 - t.z) * t.w;
+                a[r] = fmaf(z, z, a[r]);
+            }
+            if (need_xx) {
+                xx2 = fmaf(x0, x0, xx2);
+                xx2 = fmaf(x1, x1, xx2);
+            }
+            if (need_sx) {
+                sx2 += x0;
+                sx2 += x1;
+            }
+        }
+        xxo = xx2;
+        sxo = sx2;
         float e[CPP];
         float mx = -INFINITY;
 #pragma unroll
         for (int r = 0; r < CPP; ++r) {
             const int cc = l + LPC * r;
-            float a = 0.f;
-            const float4 *row = tab + cc * TS;
-#pragma unroll
-            for (int i = 0; i < MAXD; i += 2) {
-                // at most 8 table loads in flight: the compiler would otherwise hoist all of
-                // them (4 registers each) and spill
-                if (i % 16 == 0) { asm volatile("" ::: "memory"); }
-                const float4 t = row[i / 2];
-                float z = (xf[i] - t.x) * t.y;
-                a = fmaf(z, z, a);
-                z = (xf[i + 1] - t.z) * t.w;
-                a = fmaf(z, z, a);
-            }
-            a = fmaf(-0.5f, a, lcn[cc]);
-            e[r] = (cc < nc) ? a : -INFINITY;
+            e[r] = (cc < nc) ? fmaf(-0.5f, a[r], lcn[cc]) : -INFINITY;
             mx = fmaxf(mx, e[r]);
         }
 #pragma unroll
@@ -228,18 +241,8 @@ struct LaneMixSampler {
 #pragma unroll
             for (int i = 0; i < 4; ++i) { xn[4 * j + i] = fmaf(sto[4 * j + i], d[i], x[4 * j + i]); }
         }
-        float xf[MAXD];
-        gather(xn, xf);
-        const float lpn = logp(xf);
-        float xxn = 0.f, sxn = 0.f;
-        if (need_xx) {
-#pragma unroll
-            for (int i = 0; i < MAXD; ++i) { xxn = fmaf(xf[i], xf[i], xxn); }
-        }
-        if (need_sx) {
-#pragma unroll
-            for (int i = 0; i < MAXD; ++i) { sxn += xf[i]; }
-        }
+        float xxn, sxn;
+        const float lpn = logp(xn, xxn, sxn);
         const float u = accept_draw<float>(philox4x32_10_rk(s0, s1, (uint32_t)c, TAG_ACCEPT << 12, fc.rk));
         const bool acc = decide(u, lpn, xn, upd);
         if (upd) {
@@ -256,19 +259,7 @@ struct LaneMixSampler {
     }
 
     // the walker's log density and sums, evaluated as the one-lane kernel does at a start
-    __device__ __forceinline__ void refresh()
-    {
-        float xf[MAXD];
-        gather(x, xf);
-        lp = logp(xf);
-        xx = 0.f;
-        sx = 0.f;
-#pragma unroll
-        for (int i = 0; i < MAXD; ++i) {
-            xx = fmaf(xf[i], xf[i], xx);
-            sx += xf[i];
-        }
-    }
+    __device__ __forceinline__ void refresh() { lp = logp(x, xx, sx); }
 
     __device__ __forceinline__ ST &slot(int j) { return slots[j * blockDim.x + threadIdx.x]; }
 
@@ -389,9 +380,8 @@ struct LaneMixSampler {
         bool runc = valid && calib_more(p, cons, counter);
         while (__any_sync(FULL, runc)) {
             {
-                float xf[MAXD];
-                gather(x, xf);
-                const float l0 = logp(xf);
+                float xx0, sx0;
+                const float l0 = logp(x, xx0, sx0);
                 if (runc) { lp = l0; }
             }
             int64_t nacc = 0;
@@ -433,7 +423,7 @@ template <int MAXD>
 struct LanesTable { static constexpr size_t bytes = (size_t)8 * (MAXD / 2 + 1) * sizeof(float4) + 8 * sizeof(float); };
 
 template <int MAXD, int LPC, bool KAHAN>
-__global__ void __launch_bounds__(MCIG_FAST_BLOCK, LPC >= 8 ? 12 : 8) mcig_lanes_kernel(const KParams p, const FastConst fc)
+__global__ void __launch_bounds__(MCIG_FAST_BLOCK, LPC >= 8 ? 14 : 8) mcig_lanes_kernel(const KParams p, const FastConst fc)
 {
     using LS = LaneMixSampler<MAXD, LPC, KAHAN>;
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -121,6 +121,10 @@ class MCI:
         """Lanes per chain of the multi-lane mixture kernel (0 off, 4 or 8)."""
         _raise(self.L.mcig_set_lanes(self._h, int(lpc)))
 
+    def setSamplingChunks(self, n):
+        """Main sampling in n launches with the Full-sample estimator overlapped (1: one launch)."""
+        _raise(self.L.mcig_set_sampling_chunks(self._h, int(n)))
+
     def setFP64Decision(self, mode=1):
         """Metropolis decision certified in double near the float threshold (1), on every step (2), off (0)."""
         _raise(self.L.mcig_set_fp64_decision(self._h, int(mode)))

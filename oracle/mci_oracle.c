@@ -191,7 +191,8 @@ typedef struct {
     uint32_t pkey[2], pchain;
     uint64_t pctr;           /* step counter of the chain (the device's ctr) */
     int pmove, psrrd, pveclen, pndim;
-    double *pbuf;            /* [pndim + 2] */
+    int pms_nsteps, pms_srrd, pms_veclen; /* MultiStepMove: sub-steps and their vector move */
+    double *pbuf;            /* [(pms_nsteps + 1) * (pndim + 2)] */
     int pbuf_n, pbuf_pos;
 } drawsrc;
 
@@ -223,12 +224,13 @@ static double orc_u01_d(uint32_t hi, uint32_t lo)
     return (double)((((uint64_t)hi) << 21) | (uint64_t)(lo >> 11)) * 0x1p-53;
 }
 
-/* the move draws of Philox block b (float layout: 4 coordinates, double layout: 2) */
-static void philox_move_block(const drawsrc *d, uint32_t b, double *v)
+/* the move draws of Philox block b of sub-step `sub` (float layout: 4 coordinates, double
+ * layout: 2) with distribution srrd */
+static void philox_move_block(const drawsrc *d, uint32_t sub, int srrd, uint32_t b, double *v)
 {
     uint32_t q[4];
-    philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, (ORC_TAG_MOVE << 12) | b, d->pkey, q);
-    const int gauss = d->psrrd == MCIG_SRRD_GAUSSIAN;
+    philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, (sub << 16) | (ORC_TAG_MOVE << 12) | b, d->pkey, q);
+    const int gauss = srrd == MCIG_SRRD_GAUSSIAN;
     if (d->philox == 1) {
         if (gauss) {
             orc_bm_float(q[0], q[1], &v[0], &v[1]);
@@ -248,28 +250,56 @@ static void philox_move_block(const drawsrc *d, uint32_t b, double *v)
     }
 }
 
-/* the draws of one step in this oracle's consumption order: [vector index,] the moved
- * coordinates' draws (ascending), the acceptance uniform */
-static void philox_fill(drawsrc *d)
+/* the acceptance uniform of sub-step `sub` (0: the step itself) */
+static double philox_accept(const drawsrc *d, uint32_t sub)
+{
+    uint32_t q[4];
+    philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, (sub << 16) | (ORC_TAG_ACCEPT << 12), d->pkey, q);
+    return (d->philox == 1) ? (double)((q[0] >> 8) + 1u) * 0x1p-24 /* (0, 1] */ : orc_u01_d(q[0], q[1]);
+}
+
+/* the draws of one vector move of sub-step `sub` at position n of the buffer: the index
+ * (32-bit multiply-shift of word a of the index block), the vector's draws; returns n */
+static int philox_vec(drawsrc *d, uint32_t sub, int srrd, int veclen, int n)
 {
     const int cpb = (d->philox == 1) ? 4 : 2;
     uint32_t q[4];
-    int n = 0, lo = 0, hi = d->pndim;
-    if (d->pmove == MCIG_MOVE_VEC) { /* index: 32-bit multiply-shift of word a of the index block */
-        const uint32_t nvecs = (uint32_t)(d->pndim / d->pveclen);
-        philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, ORC_TAG_INDEX << 12, d->pkey, q);
-        const int vidx = (int)(((uint64_t)q[0] * nvecs) >> 32);
-        d->pbuf[n++] = (double)vidx;
-        lo = vidx * d->pveclen;
-        hi = lo + d->pveclen;
-    }
+    const uint32_t nvecs = (uint32_t)(d->pndim / veclen);
+    philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, (sub << 16) | (ORC_TAG_INDEX << 12), d->pkey, q);
+    const int vidx = (int)(((uint64_t)q[0] * nvecs) >> 32);
+    d->pbuf[n++] = (double)vidx;
+    const int lo = vidx * veclen;
     double v[4];
-    for (int i = lo; i < hi; ++i) {
-        if (i == lo || i % cpb == 0) { philox_move_block(d, (uint32_t)(i / cpb), v); }
+    for (int i = lo; i < lo + veclen; ++i) {
+        if (i == lo || i % cpb == 0) { philox_move_block(d, sub, srrd, (uint32_t)(i / cpb), v); }
         d->pbuf[n++] = v[i % cpb];
     }
-    philox_block((uint32_t)d->pctr, (uint32_t)(d->pctr >> 32), d->pchain, ORC_TAG_ACCEPT << 12, d->pkey, q);
-    d->pbuf[n++] = (d->philox == 1) ? (double)((q[0] >> 8) + 1u) * 0x1p-24 /* (0, 1] */ : orc_u01_d(q[0], q[1]);
+    return n;
+}
+
+/* the draws of one step in this oracle's consumption order: all-coordinate move: the
+ * coordinates' draws; vector move: index and the vector's draws; MultiStepMove: per
+ * sub-step s the vector move of sub-step 1 + s and its acceptance uniform; then the step's
+ * acceptance uniform */
+static void philox_fill(drawsrc *d)
+{
+    const int cpb = (d->philox == 1) ? 4 : 2;
+    int n = 0;
+    if (d->pmove == MCIG_MOVE_VEC) {
+        n = philox_vec(d, 0, d->psrrd, d->pveclen, n);
+    } else if (d->pmove == MCIG_MOVE_MULTISTEP) {
+        for (int s = 0; s < d->pms_nsteps; ++s) {
+            n = philox_vec(d, (uint32_t)(1 + s), d->pms_srrd, d->pms_veclen, n);
+            d->pbuf[n++] = philox_accept(d, (uint32_t)(1 + s));
+        }
+    } else {
+        double v[4];
+        for (int i = 0; i < d->pndim; ++i) {
+            if (i % cpb == 0) { philox_move_block(d, 0, d->psrrd, (uint32_t)(i / cpb), v); }
+            d->pbuf[n++] = v[i % cpb];
+        }
+    }
+    d->pbuf[n++] = philox_accept(d, 0);
     d->pbuf_n = n;
     d->pbuf_pos = 0;
 }
@@ -1388,13 +1418,14 @@ int orc_set_replay(orc_mci *h, const double *tape, int64_t stride, const int64_t
  * oracle is device chain chain0 + c, key (seed lo, seed hi), step counter ctr0[c] (NULL:
  * 0).  layout 1: the float kernels' draws (mcig_common.cuh move_draws<float>, accept
  * on (0, 1]) evaluated in double from the same Philox words; layout 2: the double
- * kernels' draws (move_draws<double>, accept_draw<double>).  All-coordinate and vector
- * moves with uniform or Gaussian draws; layout 0 returns to the engine. */
+ * kernels' draws (move_draws<double>, accept_draw<double>).  All-coordinate, vector and
+ * MultiStepMove moves with uniform or Gaussian draws; layout 0 returns to the engine. */
 int orc_set_philox(orc_mci *h, uint64_t seed, int64_t chain0, const uint64_t *ctr0, int layout)
 {
     if (layout < 0 || layout > 2) { return fail(MCIG_ERR_INVALID_ARGUMENT, "layout must be 0, 1 or 2"); }
-    if (layout && (h->movetype == MCIG_MOVE_MULTISTEP || (h->srrd != MCIG_SRRD_UNIFORM && h->srrd != MCIG_SRRD_GAUSSIAN))) {
-        return fail(MCIG_ERR_UNSUPPORTED, "Philox draws: all-coordinate or vector moves with uniform or Gaussian draws");
+    const int srrd = h->movetype == MCIG_MOVE_MULTISTEP ? h->ms_srrd : h->srrd;
+    if (layout && srrd != MCIG_SRRD_UNIFORM && srrd != MCIG_SRRD_GAUSSIAN) {
+        return fail(MCIG_ERR_UNSUPPORTED, "Philox draws: moves with uniform or Gaussian draws");
     }
     for (int c = 0; c < h->nchains; ++c) {
         drawsrc *d = &h->ch[c].ds;
@@ -1407,8 +1438,11 @@ int orc_set_philox(orc_mci *h, uint64_t seed, int64_t chain0, const uint64_t *ct
         d->psrrd = h->srrd;
         d->pveclen = h->veclen;
         d->pndim = h->ndim;
+        d->pms_nsteps = h->ms_nsteps;
+        d->pms_srrd = h->ms_srrd;
+        d->pms_veclen = h->ms_veclen;
         free(d->pbuf);
-        d->pbuf = layout ? (double *)calloc((size_t)h->ndim + 2, sizeof(double)) : NULL;
+        d->pbuf = layout ? (double *)calloc((size_t)(h->ms_nsteps + 1) * (h->ndim + 2), sizeof(double)) : NULL;
         d->pbuf_n = d->pbuf_pos = 0;
     }
     return MCIG_OK;

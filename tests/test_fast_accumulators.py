@@ -122,3 +122,31 @@ def test_split_calibration_equals_one_lane(ndim, pdf, nfind):
     np.testing.assert_array_equal(a["x"], b["x"])
     for u, v in zip(a["counts"], b["counts"]):
         np.testing.assert_array_equal(u, v)
+
+
+@pytest.mark.parametrize("nskip", [1, 3])
+def test_chunked_sampling_equals_one_launch(nskip):
+    """Main sampling in chunks with the Full-sample estimator beside the next chunk
+    (mcig_set_sampling_chunks) against one launch: identical accumulator data, chain
+    estimates, averages, errors and counts."""
+    import mcintegratorplusplus_gb300 as mcig
+    res = []
+    for chunks in (1, 4, 3):
+        nc, nmc = 512, 2400
+        m = mcig.MCI(16, nc, precision=mcig.PREC_FP32)
+        m.setSeed(21)
+        m.setFullStorage(32)
+        m.addSamplingFunction(mcig.PDF_GAUSS)
+        m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+        m.setNdecorrelationSteps(100)
+        naccu = 1 + (nmc - 1) // nskip
+        m.addObservable(mcig.OBS_X2SUM, (), naccu // 8, nskip, False, mcig.EST_UNCORRELATED)  # Block
+        m.addObservable(mcig.OBS_XND, (), 1, nskip, False, mcig.EST_UNCORRELATED)              # Full
+        m.addObservable(mcig.OBS_X2SUM, (), 1, 1, False, mcig.EST_UNCORRELATED)                # Full
+        m.setSamplingChunks(chunks)
+        avg, err = m.integrate(nmc)
+        ca, ce = m.getChainResults()
+        res.append([avg, err, ca, ce, *m.getCounts()] + [m.getObsData(o) for o in range(3)])
+    for other in res[1:]:
+        for a, b in zip(res[0], other):
+            assert np.array_equal(a, b)

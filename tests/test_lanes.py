@@ -40,7 +40,10 @@ def start(nc, seed=1):
     return means[comp] + widths[comp] * rng.standard_normal((nc, NDIM))
 
 
-def configure(m, nmc, nblocks=16):
+def configure(m, nmc, nblocks=16, moments=False):
+    """The mixture configuration; moments: x.x, x_i, x_i^2 in Block accumulators only, else
+    a mix of every observable kind and accumulator the multi-lane kernel serves (at most
+    2 ndim + 8 observable values)."""
     params = mixture()[0]
     m.add_sampling_function(5, params)        # GAUSS_MIX
     m.set_trial_move(0, 1, 0)                 # all-coordinate, Gaussian
@@ -49,7 +52,9 @@ def configure(m, nmc, nblocks=16):
     bs = nmc // nblocks
     m.add_observable(0, (), bs, 1, False, 1)  # x.x Block
     m.add_observable(1, (), bs, 1, False, 1)  # x_i Block
-    m.add_observable(2, (), bs, 1, False, 1)  # x_i^2 Block
+    if moments:
+        m.add_observable(2, (), bs, 1, False, 1)  # x_i^2 Block
+        return
     m.add_observable(1, (), 1, 1, False, 1)   # x_i Full
     m.add_observable(8, (5,), 1, 2, False, 1)  # x_5 Full, every 2nd step
     m.add_observable(9, (), 0, 1, False, 0)   # log p Simple
@@ -57,11 +62,11 @@ def configure(m, nmc, nblocks=16):
     m.add_observable(3, (), 1, 1, False, 1)   # x.x / ndim Full
 
 
-def run(mcig, prec, lanes, nc=512, nmc=2048, f64=0, seed=31):
+def run(mcig, prec, lanes, nc=512, nmc=2048, f64=0, seed=31, moments=False):
     m = mcig.MCI(NDIM, nc, device=0, precision=prec)
     m.setSeed(seed)
     m.setFullStorage(32)
-    configure(m, nmc)
+    configure(m, nmc, moments=moments)
     m.setX(start(nc))
     if lanes:
         m.setLanes(lanes)
@@ -74,7 +79,7 @@ def run(mcig, prec, lanes, nc=512, nmc=2048, f64=0, seed=31):
     ca, ce = m.getChainResults()
     out = {"avg": avg, "err": err, "ca": ca, "ce": ce, "steps": m.getMRT2Steps(), "x": m.getX(),
            "ctr": m.getStepCounters(), "counts": np.stack(m.getCounts())}
-    for o in range(8):
+    for o in range(m.getNObs()):
         out["data%d" % o] = m.getObsData(o)
     out["stats"] = m.getDecisionStats() if f64 else None
     return out
@@ -135,8 +140,8 @@ def test_lanes_fp64_decision_against_fp64_oracle_same_draws():
     o.set_philox(77, 0, ctr[:K], layout=1)
     o.set_record(True)
     _, _, oca, _ = o.integrate(nmc, False, False, nthreads=8, per_chain=True)
-    xs_dev = m.getObsDataChains(3, 0, K).reshape(K, nmc, NDIM)
-    xs_orc = o.obs_data(3).reshape(K, nmc, NDIM)
+    xs_dev = m.getObsDataChains(2, 0, K).reshape(K, nmc, NDIM)  # x_i Full
+    xs_orc = o.obs_data(2).reshape(K, nmc, NDIM)
     first = np.full(K, nmc)
     for c in range(K):
         bits, s0 = o.get_accept_bits(c)
@@ -161,7 +166,7 @@ def test_lanes_analytic_moments():
     _, _, _, _, m1, m2 = mixture()
     exact = np.concatenate([[m2.sum()], m1, m2])
     nc = 4096
-    r = run(mcig, mcig.PREC_FP32, 8, nc=nc, nmc=4096, f64=1, seed=5)
+    r = run(mcig, mcig.PREC_FP32, 8, nc=nc, nmc=4096, f64=1, seed=5, moments=True)
     ca = r["ca"][:, :1 + 2 * NDIM]
     z = np.abs(ca.mean(0) - exact) / (ca.std(0, ddof=1) / np.sqrt(nc))
     assert z.max() < 3.5, z  # 65 moments: the largest of 65 normal deviates

@@ -96,13 +96,15 @@ int mcig_set_lanes(mcig_mci *h, int lpc);
 int mcig_set_fp64_decision(mcig_mci *h, int mode);
 int mcig_get_decision_stats(const mcig_mci *h, int64_t *checked, int64_t *reversed, double *max_margin);
 
-/* Chunked sampling (default 4; 1 turns it off): where the register-resident one-lane kernel
+/* Chunked sampling (default 1: off): where the register-resident one-lane kernel
  * samples, no observable uses a SimpleAccumulator and float FullAccumulator samples take the
  * Uncorrelated estimator, the main sampling runs as n launches of equal length (a multiple of
  * every block length), and the estimator of each finished chunk's Full rows runs on a
  * low-priority stream beside the next launch.  Results are identical to one launch and the
- * one-pass estimator; the estimation's pass over the Full samples overlaps the sampling.
- * No counterpart in the reference, whose MCI::sample (MCIntegrator.cpp:290-321) is one loop. */
+ * one-pass estimator; the estimation's pass over the Full samples can overlap the sampling
+ * where the sampling leaves the SMs room (with 65,536 chains of the 16-D workload it does not:
+ * measured slower, hence off).  No counterpart in the reference, whose MCI::sample
+ * (MCIntegrator.cpp:290-321) is one loop. */
 int mcig_set_sampling_chunks(mcig_mci *h, int n);
 
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
@@ -267,10 +269,17 @@ int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int period, int6
 /* ------------------------------------------------------------------------
  * Batched integration: many independent MCI::integrate calls (one handle each,
  * any ndim <= 64, its own sampling functions, move, observables and seed) run
- * by one persistent kernel per ndim bucket (1-8, 9-16, 17-32, 33-64), whose
- * warps pull (integral, chain) work units longest-first from an atomic queue;
- * the launches, the estimators and the read-back are one CUDA graph.
- * Handles must use MCIG_PREC_FP32, a sampling function, burn-in N >= 0 and
+ * by ONE persistent kernel launch whose warps pull work items (up to 32 chains of
+ * one integral) longest-first from one atomic queue over the whole batch; the
+ * launch, the estimators and the read-back are one CUDA graph.  Integrals of the
+ * block-separable form (single-coordinate MultiStepMove, isotropic Gaussian
+ * factors over coordinate ranges as sampling functions and sub-pdfs, x.x per
+ * factor or in all) run a sampler that keeps the walker in shared memory and the
+ * log densities as per-range sums of squares; every other integral runs the
+ * general sampler in the same launch.  All handles use one precision and draw
+ * source: MCIG_PREC_FP32 / FP32_ACC64 with Philox, or MCIG_PREC_FP64 with Philox
+ * or replayed draws (the general double sampler: each chain's numbers are those of
+ * its own integrate).  Handles need a sampling function, burn-in N >= 0 and
  * observables with the Uncorrelated (Block/Full, double data) or Noop estimator.
  * ------------------------------------------------------------------------ */
 typedef struct mcig_batch mcig_batch;
@@ -281,10 +290,12 @@ int mcig_batch_run(mcig_batch *b, double *avg, double *err);
 int mcig_batch_destroy(mcig_batch *b);
 /* device time of the last run (graph launch to completion), milliseconds */
 int mcig_batch_last_ms(const mcig_batch *b, double *ms);
-/* chains per block of each ndim bucket (4 values) */
-int mcig_batch_get_blocks(const mcig_batch *b, int *blocks);
-int mcig_batch_set_blocks(mcig_batch *b, const int *blocks);
-/* time 32/64/128/256 chains per block per bucket, keep the fastest; cache file optional */
+/* threads per block of the launch and, per ndim bucket (1-8, 9-16, 17-32, 33-64), the
+ * unroll (1, 2, 4) of the block-separable sampler's sub-step loop */
+int mcig_batch_get_tuning(const mcig_batch *b, int *block, int *unroll /* [4] */);
+int mcig_batch_set_tuning(mcig_batch *b, int block, const int *unroll /* [4], NULL: unchanged */);
+/* time 64/128/256 threads per block, then per bucket the three unrolls, keep the fastest;
+ * cache file optional (keyed by the batch's shape) */
 int mcig_batch_autotune(mcig_batch *b, const char *cache_path);
 
 /* ------------------------------------------------------------------------

@@ -88,8 +88,8 @@ SIGNATURES = {
     "mcig_batch_run": (c_int, [c_void_p, P_double, P_double]),
     "mcig_batch_destroy": (c_int, [c_void_p]),
     "mcig_batch_last_ms": (c_int, [c_void_p, P_double]),
-    "mcig_batch_get_blocks": (c_int, [c_void_p, P_int]),
-    "mcig_batch_set_blocks": (c_int, [c_void_p, P_int]),
+    "mcig_batch_get_tuning": (c_int, [c_void_p, P_int, P_int]),
+    "mcig_batch_set_tuning": (c_int, [c_void_p, c_int, P_int]),
     "mcig_batch_autotune": (c_int, [c_void_p, ctypes.c_char_p]),
     "mcig_flow_nparams": (c_int64, [c_int, c_int]),
     "mcig_flow_create": (c_int, [c_int, c_int, c_int, ctypes.c_uint64, c_int, ctypes.POINTER(c_void_p)]),

@@ -11,6 +11,36 @@ struct BatchPhase {
     int movetype;
 };
 
+// one work item of the persistent launch: `count` (<= 32) consecutive chains of one
+// integral, one chain per lane of the warp that takes it; `variant` selects the code:
+// 0 the general sampler, 1 + u the block-separable sampler with its sub-step loop
+// unrolled 2^u times
+struct BatchTask {
+    int integral;
+    int chain0;
+    int count;
+    int variant;
+};
+
+#define MCIG_BS_MAXR 4   // sums of x_i^2 over coordinate ranges kept by the block-separable sampler
+#define MCIG_BS_MAXNS 8  // MultiStepMove sub-steps of the block-separable sampler
+#define MCIG_BS_MAXOBS 4 // observables of the block-separable sampler
+#define MCIG_BS_MAXV 16  // observable values of the block-separable sampler
+
+// Block-separable configuration of an integral (host-made): every sampling function and
+// every MultiStepMove sub-pdf is an isotropic Gaussian factor exp(-c sum_{a<=i<b} x_i^2)
+// over a coordinate range, so the log densities are sums over the ranges' sums of squares
+// S_r; pc[r] (sc[r]) is the sum of the coefficients c of the sampling functions (sub-pdfs)
+// over range r.  Observables read the sums: value j of observable o is S[orng[o] + j].
+// The ranges of the sampling functions, the sub-pdfs and the observables must coincide and
+// number at most MCIG_BS_MAXR (the uneven-batch form: 2-4 factors, x.x per factor).
+struct BatchSep {
+    int nr;
+    int ra[MCIG_BS_MAXR], rb[MCIG_BS_MAXR];
+    float pc[MCIG_BS_MAXR], sc[MCIG_BS_MAXR];
+    int orng[MCIG_BS_MAXOBS];
+};
+
 // one estimator series: n values at data[i * stride]
 struct BatchSeries {
     const double *data;
@@ -18,6 +48,12 @@ struct BatchSeries {
     int one_d, noop;
 };
 
-void mcig_batch_launch(const KParams *cfg, const BatchPhase *ph, const int2 *units, int nunits, int *counter, int grid,
-                       int block, cudaStream_t st);
+// prec MCIG_PREC_*, rng RNG_PHILOX / RNG_TAPE (tape: FP64); walk, nslot, nundo: the
+// block-separable sampler's shared memory per lane (largest ndim, observable values and
+// MultiStepMove sub-steps of its integrals)
+void mcig_batch_launch(int prec, int rng, const KParams *cfg, const BatchPhase *ph, const BatchSep *sep,
+                       const BatchTask *tasks, int ntasks, int *counter, int grid, int block, int walk, int nslot,
+                       int nundo, cudaStream_t st);
+// resident blocks per SM of the launch at this block size, for sizing the persistent grid
+int mcig_batch_blocks_per_sm(int prec, int rng, int block, int walk, int nslot, int nundo);
 void mcig_batch_estimate_launch(const BatchSeries *series, int nseries, double *avg, double *err, cudaStream_t st);

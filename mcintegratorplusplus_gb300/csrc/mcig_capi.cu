@@ -166,8 +166,11 @@ struct mcig_mci {
     int64_t launches = 0;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // chunked sampling (mcig_set_sampling_chunks): the Uncorrelated estimator of float Full
-    // samples runs on a low-priority stream over each finished chunk beside the next one
-    int chunks = 4;
+    // samples runs on a low-priority stream over each finished chunk beside the next one;
+    // off by default (at 65,536 chains of the 16-D workload the sampling kernel holds the
+    // SMs' registers and the estimator ran mostly after it: 10.9 ms of estimation tail
+    // against 8.1 ms for the one-pass estimator)
+    int chunks = 1;
     cudaStream_t est_stream = nullptr;
     cudaEvent_t cev[MCIG_MAX_CHUNKS + 1] = {};
     DBuf<float4> est_state;
@@ -2343,16 +2346,21 @@ static int bucket_of(int ndim) { return ndim <= 8 ? 0 : (ndim <= 16 ? 1 : (ndim 
 struct mcig_batch {
     std::vector<mcig_mci *> hs;
     std::vector<int64_t> nmc;
-    int device = 0;
+    int device = 0, prec = MCIG_PREC_FP32, rng = RNG_PHILOX;
     cudaStream_t st = nullptr;
-    cudaStream_t bst[MCIG_NBUCKETS] = {nullptr, nullptr, nullptr, nullptr};
-    cudaEvent_t fork = nullptr, join[MCIG_NBUCKETS] = {nullptr, nullptr, nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
     DBuf<KParams> cfg;
     DBuf<BatchPhase> ph;
-    DBuf<int2> units[MCIG_NBUCKETS];
-    int nunits[MCIG_NBUCKETS] = {0, 0, 0, 0};
-    int block[MCIG_NBUCKETS] = {64, 64, 64, 64};
-    DBuf<int> counters;
+    DBuf<BatchSep> sep;
+    DBuf<BatchTask> tasks;
+    std::vector<BatchTask> htasks;
+    std::vector<int> task_bucket;         // ndim bucket of each task (for the per-bucket unroll)
+    std::vector<char> bs;                 // integral served by the block-separable sampler
+    int ntasks = 0;
+    int block = 128;                      // threads per block of the launch
+    int unroll[MCIG_NBUCKETS] = {0, 0, 0, 0}; // sub-step loop unrolled 2^u times, per ndim bucket
+    int walk = 0, nslot = 0, nundo = 0;   // shared memory per lane of the block-separable sampler
+    DBuf<int> counter;
     DBuf<BatchSeries> series;
     int nseries = 0;
     DBuf<double> s_avg, s_err;
@@ -2384,28 +2392,85 @@ void mcig_batch_estimate_launch(const BatchSeries *series, int nseries, double *
     batch_estimate_kernel<<<(nseries + 127) / 128, 128, 0, st>>>(series, nseries, avg, err);
 }
 
-static int batch_grid(int nunits, int block)
+// the block-separable form (sample_batch.cu): single-coordinate MultiStepMove whose
+// sub-pdfs and sampling functions are isotropic Gaussian factors over coordinate ranges,
+// observables x.x per factor (X2BLOCK) or in all (X2SUM) on the same ranges
+static bool batch_sep(const mcig_mci *h, BatchSep &b)
 {
-    const int warps = (nunits + 31) / 32;
-    const int wpb = block / 32;
-    return std::max(1, std::min((warps + wpb - 1) / wpb, 152 * 16));
+    memset(&b, 0, sizeof(b));
+    if (h->prec == MCIG_PREC_FP64 || h->replay || uses_plugin(h) || h->periodic || h->ntypes != 1) { return false; }
+    if (h->movetype != MCIG_MOVE_MULTISTEP || h->ms_veclen != 1 || h->ms_nsteps < 1 || h->ms_nsteps > MCIG_BS_MAXNS) { return false; }
+    if (h->ms_srrd != MCIG_SRRD_UNIFORM && h->ms_srrd != MCIG_SRRD_GAUSSIAN) { return false; }
+    if (h->obs.size() > MCIG_BS_MAXOBS || nobsdim(h) > MCIG_BS_MAXV) { return false; }
+    auto range_of = [&](int a, int e) -> int {
+        for (int r = 0; r < b.nr; ++r) {
+            if (b.ra[r] == a && b.rb[r] == e) { return r; }
+        }
+        if (b.nr >= MCIG_BS_MAXR) { return -1; }
+        b.ra[b.nr] = a;
+        b.rb[b.nr] = e;
+        return b.nr++;
+    };
+    for (size_t o = 0; o < h->obs.size(); ++o) { // observables first: their values are consecutive ranges
+        const ObsDef &d = h->obs[o];
+        if (d.kind == MCIG_OBS_X2SUM) {
+            b.orng[o] = b.nr;
+            if (range_of(0, h->ndim) != b.orng[o]) { return false; }
+        } else if (d.kind == MCIG_OBS_X2BLOCK) {
+            b.orng[o] = b.nr;
+            const int nb = (int)d.params[0];
+            for (int k = 0; k < nb; ++k) {
+                if (range_of((int)d.params[1 + k], (int)d.params[2 + k]) != b.orng[o] + k) { return false; }
+            }
+        } else {
+            return false;
+        }
+    }
+    for (auto &d : h->pdfs) {
+        if (d.kind != MCIG_PDF_GAUSS_BLOCK) { return false; }
+        const int r = range_of((int)d.params[0], (int)d.params[1]);
+        if (r < 0) { return false; }
+        b.pc[r] += (float)(1. / (2. * d.params[2] * d.params[2]));
+    }
+    for (auto &d : h->ms_pdfs) {
+        if (d.kind != MCIG_PDF_GAUSS_BLOCK) { return false; }
+        const int r = range_of((int)d.params[0], (int)d.params[1]);
+        if (r < 0) { return false; }
+        b.sc[r] += (float)(1. / (2. * d.params[2] * d.params[2]));
+    }
+    return true;
+}
+
+// the tasks' code variants from the per-bucket unroll, uploaded
+static int batch_upload_tasks(mcig_batch *b)
+{
+    for (int t = 0; t < b->ntasks; ++t) {
+        BatchTask &k = b->htasks[t];
+        k.variant = b->bs[k.integral] ? 1 + b->unroll[b->task_bucket[t]] : 0;
+    }
+    CK(cudaMemcpy(b->tasks.p, b->htasks.data(), b->ntasks * sizeof(BatchTask), cudaMemcpyHostToDevice));
+    return MCIG_OK;
+}
+
+// the persistent grid: every block resident at once
+static int batch_grid(const mcig_batch *b, int block)
+{
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->device);
+    const int per_sm = std::max(1, mcig_batch_blocks_per_sm(b->prec, b->rng, block, b->walk, b->nslot, b->nundo));
+    const int need = (b->ntasks * 32 + block - 1) / block;
+    return std::max(1, std::min(per_sm * nsm, need));
 }
 
 static int batch_build_graph(mcig_batch *b)
 {
     if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    const int grid = batch_grid(b, b->block); // occupancy query before the capture starts
     CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-    cudaMemsetAsync(b->counters.p, 0, MCIG_NBUCKETS * sizeof(int), b->st);
-    cudaEventRecord(b->fork, b->st);
-    for (int k = 0; k < MCIG_NBUCKETS; ++k) {
-        if (!b->nunits[k]) { continue; }
-        cudaStreamWaitEvent(b->bst[k], b->fork, 0);
-        mcig_batch_launch(b->cfg.p, b->ph.p, b->units[k].p, b->nunits[k], b->counters.p + k,
-                          batch_grid(b->nunits[k], b->block[k]), b->block[k], b->bst[k]);
-        cudaEventRecord(b->join[k], b->bst[k]);
-        cudaStreamWaitEvent(b->st, b->join[k], 0);
-    }
+    cudaMemsetAsync(b->counter.p, 0, sizeof(int), b->st);
+    mcig_batch_launch(b->prec, b->rng, b->cfg.p, b->ph.p, b->sep.p, b->tasks.p, b->ntasks, b->counter.p, grid, b->block,
+                      b->walk, b->nslot, b->nundo, b->st);
     if (b->nseries) {
         mcig_batch_estimate_launch(b->series.p, b->nseries, b->s_avg.p, b->s_err.p, b->st);
         cudaMemcpyAsync(b->h_avg, b->s_avg.p, b->nseries * sizeof(double), cudaMemcpyDeviceToHost, b->st);
@@ -2424,13 +2489,10 @@ extern "C" int mcig_batch_destroy(mcig_batch *b)
     if (b->st) { cudaStreamSynchronize(b->st); }
     if (b->gexec) { cudaGraphExecDestroy(b->gexec); }
     if (b->graph) { cudaGraphDestroy(b->graph); }
-    b->cfg.release(); b->ph.release(); b->counters.release(); b->series.release(); b->s_avg.release(); b->s_err.release();
-    for (auto &u : b->units) { u.release(); }
+    b->cfg.release(); b->ph.release(); b->sep.release(); b->tasks.release(); b->counter.release();
+    b->series.release(); b->s_avg.release(); b->s_err.release();
     if (b->h_avg) { cudaFreeHost(b->h_avg); }
     if (b->h_err) { cudaFreeHost(b->h_err); }
-    for (auto &s : b->bst) { if (s) { cudaStreamDestroy(s); } }
-    for (auto &e : b->join) { if (e) { cudaEventDestroy(e); } }
-    if (b->fork) { cudaEventDestroy(b->fork); }
     if (b->t0) { cudaEventDestroy(b->t0); }
     if (b->t1) { cudaEventDestroy(b->t1); }
     if (b->st) { cudaStreamDestroy(b->st); }
@@ -2443,18 +2505,21 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
     if (!handles || !nmc || n < 1 || !out) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: bad arguments"); }
     *out = nullptr;
     const int dev = handles[0]->device;
+    const int prec = handles[0]->prec;
+    const bool replay = handles[0]->replay;
     for (int i = 0; i < n; ++i) {
         mcig_mci *h = handles[i];
         if (!h || h->device != dev) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: every handle must exist on the same device"); }
-        if (h->prec != MCIG_PREC_FP32 || h->replay) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: handles must use MCIG_PREC_FP32 and Philox"); }
+        if (h->prec != prec || h->replay != replay) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: every handle must use the same precision and draw source"); }
         if (h->pdfs.empty()) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: every integral needs a sampling function"); }
         if (uses_plugin(h)) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: plugin kinds are integrated one handle at a time"); }
-        if (nmc[i] < 1) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: nmc must be >= 1"); }
+        if (nmc[i] < 1 || nmc[i] >= ((int64_t)1 << 31)) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: nmc must be in [1, 2^31)"); }
         if (do_decorr && h->ndecorr < 0) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: automatic decorrelation is not batched (use N > 0)"); }
         for (auto &o : h->obs) {
             const bool ok = (o.estimator == MCIG_EST_UNCORRELATED && o.acc != MCIG_ACC_SIMPLE) ||
                             (o.estimator == MCIG_EST_NOOP);
             if (!ok) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: observables use the Uncorrelated or Noop estimator"); }
+            if (o.acc == MCIG_ACC_FULL && h->full32) { return set_err(MCIG_ERR_UNSUPPORTED, "batch: FullAccumulator data must be double"); }
         }
         int rc = validate_accumulators(h, nmc[i]);
         if (rc) { return rc; }
@@ -2464,20 +2529,22 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
     b->hs.assign(handles, handles + n);
     b->nmc.assign(nmc, nmc + n);
     b->device = dev;
+    b->prec = prec;
+    b->rng = replay ? RNG_TAPE : RNG_PHILOX;
     cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
-    for (auto &s : b->bst) { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); }
-    cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    for (auto &e : b->join) { cudaEventCreateWithFlags(&e, cudaEventDisableTiming); }
     cudaEventCreate(&b->t0);
     cudaEventCreate(&b->t1);
     std::vector<KParams> cfg(n);
     std::vector<BatchPhase> ph(n);
-    std::vector<std::vector<std::pair<double, int2>>> ub(MCIG_NBUCKETS);
+    std::vector<BatchSep> sep(n);
+    b->bs.assign(n, 0);
+    std::vector<std::pair<double, std::pair<BatchTask, int>>> tl; // (cost, (task, bucket))
     int rc = MCIG_OK;
     for (int i = 0; i < n && !rc; ++i) {
         mcig_mci *h = handles[i];
         if ((rc = fill_common(h, cfg[i]))) { break; }
         if ((rc = alloc_obs_data(h, h->obs, nmc[i], h->obsdata, h->obs_nstore, h->full32))) { break; }
+        cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream);
         cudaStreamSynchronize(h->stream); // parameter uploads of the handle's stream
         KParams &k = cfg[i];
         k.mode = KMODE_SAMPLE;
@@ -2490,26 +2557,39 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
         ph[i].do_find = (do_find && h->nfind != 0) ? 1 : 0;
         ph[i].ndecorr = do_decorr ? h->ndecorr : 0;
         ph[i].movetype = h->movetype;
-        const double cost = (double)(nmc[i] + (ph[i].do_find ? 10 * ph[i].min_stat : 0) + ph[i].ndecorr) * (h->ndim + 8) *
-                            (h->movetype == MCIG_MOVE_MULTISTEP ? 1 + h->ms_nsteps : 1);
-        for (int64_t c = 0; c < h->nchains; ++c) { ub[bucket_of(h->ndim)].push_back({cost, make_int2(i, (int)c)}); }
+        b->bs[i] = (b->prec != MCIG_PREC_FP64) && batch_sep(h, sep[i]);
+        if (b->bs[i]) {
+            b->walk = std::max(b->walk, h->ndim);
+            b->nslot = std::max(b->nslot, nobsdim(h));
+            b->nundo = std::max(b->nundo, h->ms_nsteps);
+        }
+        // cost of a chain: its steps times the work of a step
+        const double per_step = b->bs[i] ? (double)(2 + 3 * h->ms_nsteps) :
+                                (double)(h->ndim + 8) * (h->movetype == MCIG_MOVE_MULTISTEP ? 1 + h->ms_nsteps : 1);
+        const double cost = (double)(nmc[i] + (ph[i].do_find ? 10 * ph[i].min_stat : 0) + ph[i].ndecorr) * per_step;
+        for (int64_t c0 = 0; c0 < h->nchains; c0 += 32) {
+            BatchTask t{i, (int)c0, (int)std::min<int64_t>(32, h->nchains - c0), 0};
+            tl.push_back({cost, {t, bucket_of(h->ndim)}});
+        }
+    }
+    // one queue over the whole batch, longest first: the tail holds the short items
+    std::stable_sort(tl.begin(), tl.end(), [](const std::pair<double, std::pair<BatchTask, int>> &x,
+                                              const std::pair<double, std::pair<BatchTask, int>> &y) { return x.first > y.first; });
+    b->ntasks = (int)tl.size();
+    for (auto &e : tl) {
+        b->htasks.push_back(e.second.first);
+        b->task_bucket.push_back(e.second.second);
     }
     if (!rc) { rc = b->cfg.alloc(n); }
     if (!rc) { rc = b->ph.alloc(n); }
-    if (!rc) { rc = b->counters.alloc(MCIG_NBUCKETS); }
+    if (!rc) { rc = b->sep.alloc(n); }
+    if (!rc) { rc = b->tasks.alloc(std::max(b->ntasks, 1)); }
+    if (!rc) { rc = b->counter.alloc(1); }
     if (rc) { mcig_batch_destroy(b); return rc; }
     cudaMemcpy(b->cfg.p, cfg.data(), n * sizeof(KParams), cudaMemcpyHostToDevice);
     cudaMemcpy(b->ph.p, ph.data(), n * sizeof(BatchPhase), cudaMemcpyHostToDevice);
-    for (int k = 0; k < MCIG_NBUCKETS; ++k) { // longest first: the tail of the queue holds the short units
-        std::stable_sort(ub[k].begin(), ub[k].end(), [](const std::pair<double, int2> &a, const std::pair<double, int2> &c) { return a.first > c.first; });
-        std::vector<int2> u(ub[k].size());
-        for (size_t j = 0; j < u.size(); ++j) { u[j] = ub[k][j].second; }
-        b->nunits[k] = (int)u.size();
-        if (!u.empty()) {
-            if ((rc = b->units[k].alloc(u.size()))) { mcig_batch_destroy(b); return rc; }
-            cudaMemcpy(b->units[k].p, u.data(), u.size() * sizeof(int2), cudaMemcpyHostToDevice);
-        }
-    }
+    cudaMemcpy(b->sep.p, sep.data(), n * sizeof(BatchSep), cudaMemcpyHostToDevice);
+    if ((rc = batch_upload_tasks(b))) { mcig_batch_destroy(b); return rc; }
     // estimator series: every (handle, observable, chain, value)
     std::vector<BatchSeries> ser;
     for (int i = 0; i < n; ++i) {
@@ -2531,7 +2611,6 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
                     b->series_slot.push_back((int)(c * nod + off + j));
                 }
             }
-            if (d.acc == MCIG_ACC_FULL && h->full32) { mcig_batch_destroy(b); return set_err(MCIG_ERR_UNSUPPORTED, "batch: FullAccumulator data must be double"); }
             off += d.nv;
         }
     }
@@ -2550,8 +2629,8 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
     return MCIG_OK;
 }
 
-// one run: the graph (persistent kernels + estimators + read-back), then the
-// MPIMCI combination per integral; avg/err hold the integrals' results in order
+// one run: the graph (persistent kernel + estimators + read-back), then the MPIMCI
+// combination per integral; avg/err hold the integrals' results in order
 extern "C" int mcig_batch_run(mcig_batch *b, double *avg, double *err)
 {
     CK(cudaSetDevice(b->device));
@@ -2560,6 +2639,13 @@ extern "C" int mcig_batch_run(mcig_batch *b, double *avg, double *err)
     CK(cudaEventRecord(b->t1, b->st));
     CK(cudaStreamSynchronize(b->st));
     cudaEventElapsedTime(&b->last_ms, b->t0, b->t1);
+    if (b->rng == RNG_TAPE) { // replay tapes that ran out
+        for (auto *h : b->hs) {
+            int s1 = 0;
+            CK(cudaMemcpy(&s1, h->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (s1 & 1) { return set_err(MCIG_ERR_RUNTIME, "replay tape exhausted"); }
+        }
+    }
     // per-chain results into the handles, then combination
     for (auto *h : b->hs) {
         const int nod = nobsdim(h);
@@ -2595,62 +2681,111 @@ extern "C" int mcig_batch_last_ms(const mcig_batch *b, double *ms)
     return MCIG_OK;
 }
 
-extern "C" int mcig_batch_get_blocks(const mcig_batch *b, int *blocks)
+extern "C" int mcig_batch_get_tuning(const mcig_batch *b, int *block, int *unroll)
 {
-    for (int k = 0; k < MCIG_NBUCKETS; ++k) { blocks[k] = b->block[k]; }
+    if (block) { *block = b->block; }
+    if (unroll) {
+        for (int k = 0; k < MCIG_NBUCKETS; ++k) { unroll[k] = 1 << b->unroll[k]; }
+    }
     return MCIG_OK;
 }
 
-extern "C" int mcig_batch_set_blocks(mcig_batch *b, const int *blocks)
+extern "C" int mcig_batch_set_tuning(mcig_batch *b, int block, const int *unroll)
 {
+    if (block < 32 || block > 256 || block % 32) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: the block size is a multiple of 32 in [32, 256]"); }
+    int u[MCIG_NBUCKETS];
     for (int k = 0; k < MCIG_NBUCKETS; ++k) {
-        if (blocks[k] < 32 || blocks[k] > 256 || blocks[k] % 32) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: block sizes are multiples of 32 in [32, 256]"); }
+        const int v = unroll ? unroll[k] : (1 << b->unroll[k]);
+        if (v != 1 && v != 2 && v != 4) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "batch: unroll factors are 1, 2 or 4"); }
+        u[k] = v == 1 ? 0 : (v == 2 ? 1 : 2);
     }
     CK(cudaSetDevice(b->device));
-    for (int k = 0; k < MCIG_NBUCKETS; ++k) { b->block[k] = blocks[k]; }
-    return batch_build_graph(b);
+    CK(cudaStreamSynchronize(b->st));
+    b->block = block;
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) { b->unroll[k] = u[k]; }
+    int rc = batch_upload_tasks(b);
+    return rc ? rc : batch_build_graph(b);
 }
 
-// Autotuner: for each ndim bucket, time the persistent kernel alone at 32, 64,
-// 128 and 256 chains per block and keep the fastest; the choice is cached in a
-// JSON file keyed by bucket and work size, so later batches of the same shape
-// skip the timing.  Tuning launches advance the chains like any sampling run.
+// time one run of the persistent launch alone at the current tuning (ms)
+static int batch_time(mcig_batch *b, float *ms)
+{
+    const int grid = batch_grid(b, b->block);
+    CK(cudaMemsetAsync(b->counter.p, 0, sizeof(int), b->st));
+    CK(cudaEventRecord(b->t0, b->st));
+    mcig_batch_launch(b->prec, b->rng, b->cfg.p, b->ph.p, b->sep.p, b->tasks.p, b->ntasks, b->counter.p, grid, b->block,
+                      b->walk, b->nslot, b->nundo, b->st);
+    CK(cudaEventRecord(b->t1, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    CK(cudaGetLastError());
+    cudaEventElapsedTime(ms, b->t0, b->t1);
+    return MCIG_OK;
+}
+
+// Autotuner: the threads per block of the launch (64, 128, 256), then, per ndim bucket with
+// block-separable integrals, the unroll of the sub-step loop (1, 2, 4), each by timing the
+// persistent launch alone; the choice is cached in a text file keyed by the batch's shape
+// (tasks per bucket), so later batches of the same shape skip the timing.  Tuning launches
+// advance the chains like any sampling run.
 extern "C" int mcig_batch_autotune(mcig_batch *b, const char *cache_path)
 {
     CK(cudaSetDevice(b->device));
-    std::map<std::string, int> cache;
+    int per[MCIG_NBUCKETS] = {0, 0, 0, 0}, bsper[MCIG_NBUCKETS] = {0, 0, 0, 0};
+    for (int t = 0; t < b->ntasks; ++t) {
+        ++per[b->task_bucket[t]];
+        bsper[b->task_bucket[t]] += b->bs[b->htasks[t].integral] ? 1 : 0;
+    }
+    std::string key = "prec" + std::to_string(b->prec);
+    for (int k = 0; k < MCIG_NBUCKETS; ++k) {
+        int lg = 0;
+        while ((1 << lg) < per[k]) { ++lg; }
+        key += "_b" + std::to_string(k) + "t2^" + std::to_string(lg) + (bsper[k] ? "s" : "g");
+    }
+    std::map<std::string, std::vector<int>> cache;
     if (cache_path) {
         std::ifstream in(cache_path);
-        std::string key;
-        int val;
-        while (in >> key >> val) { cache[key] = val; }
+        std::string k;
+        int v[1 + MCIG_NBUCKETS];
+        while (in >> k >> v[0] >> v[1] >> v[2] >> v[3] >> v[4]) { cache[k] = std::vector<int>(v, v + 1 + MCIG_NBUCKETS); }
     }
-    const int cand[] = {32, 64, 128, 256};
+    int rc;
+    if (cache.count(key)) {
+        const std::vector<int> &v = cache[key];
+        b->block = v[0];
+        for (int k = 0; k < MCIG_NBUCKETS; ++k) { b->unroll[k] = v[1 + k]; }
+        if ((rc = batch_upload_tasks(b))) { return rc; }
+        return batch_build_graph(b);
+    }
+    float best = 1e30f, ms = 0.f;
+    int bestb = b->block;
+    for (int bsz : {64, 128, 256}) {
+        b->block = bsz;
+        if ((rc = batch_time(b, &ms))) { return rc; }
+        if (ms < best) { best = ms; bestb = bsz; }
+    }
+    b->block = bestb;
     for (int k = 0; k < MCIG_NBUCKETS; ++k) {
-        if (!b->nunits[k]) { continue; }
-        int lg = 0;
-        while ((1 << lg) < b->nunits[k]) { ++lg; }
-        const std::string key = "bucket" + std::to_string(k) + "_units2^" + std::to_string(lg);
-        if (cache.count(key)) { b->block[k] = cache[key]; continue; }
-        float best = 1e30f;
-        int bestb = b->block[k];
-        for (int bs : cand) {
-            CK(cudaMemsetAsync(b->counters.p + k, 0, sizeof(int), b->st));
-            CK(cudaEventRecord(b->t0, b->st));
-            mcig_batch_launch(b->cfg.p, b->ph.p, b->units[k].p, b->nunits[k], b->counters.p + k,
-                              batch_grid(b->nunits[k], bs), bs, b->st);
-            CK(cudaEventRecord(b->t1, b->st));
-            CK(cudaStreamSynchronize(b->st));
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, b->t0, b->t1);
-            if (ms < best) { best = ms; bestb = bs; }
+        if (!bsper[k]) { continue; }
+        int bestu = b->unroll[k];
+        best = 1e30f;
+        for (int u = 0; u < 3; ++u) {
+            b->unroll[k] = u;
+            if ((rc = batch_upload_tasks(b)) || (rc = batch_time(b, &ms))) { return rc; }
+            if (ms < best) { best = ms; bestu = u; }
         }
-        b->block[k] = bestb;
-        cache[key] = bestb;
+        b->unroll[k] = bestu;
     }
+    if ((rc = batch_upload_tasks(b))) { return rc; }
     if (cache_path) {
+        std::vector<int> v{b->block};
+        for (int k = 0; k < MCIG_NBUCKETS; ++k) { v.push_back(b->unroll[k]); }
+        cache[key] = v;
         std::ofstream o(cache_path);
-        for (auto &kv : cache) { o << kv.first << " " << kv.second << "\n"; }
+        for (auto &e : cache) {
+            o << e.first;
+            for (int x : e.second) { o << " " << x; }
+            o << "\n";
+        }
     }
     return batch_build_graph(b);
 }

@@ -479,7 +479,7 @@ class Plugin:
 
 
 class Batch:
-    """Many independent integrals (one MCI each) in one persistent launch per ndim bucket (mcig_batch_*)."""
+    """Many independent integrals (one MCI each) in one persistent launch (mcig_batch_*)."""
 
     def __init__(self, mcis, nmc, doFindMRT2step=True, doDecorrelation=True):
         self.L = _lib.load()
@@ -508,18 +508,20 @@ class Batch:
         _raise(self.L.mcig_batch_last_ms(self._h, ctypes.byref(v)))
         return v.value
 
-    def blocks(self):
-        b = (ctypes.c_int * 4)()
-        _raise(self.L.mcig_batch_get_blocks(self._h, b))
-        return list(b)
+    def tuning(self):
+        """(threads per block, [unroll of the four ndim buckets])"""
+        blk = ctypes.c_int()
+        u = (ctypes.c_int * 4)()
+        _raise(self.L.mcig_batch_get_tuning(self._h, ctypes.byref(blk), u))
+        return blk.value, list(u)
 
-    def set_blocks(self, blocks):
-        b = (ctypes.c_int * 4)(*[int(v) for v in blocks])
-        _raise(self.L.mcig_batch_set_blocks(self._h, b))
+    def set_tuning(self, block, unroll=None):
+        u = None if unroll is None else (ctypes.c_int * 4)(*[int(v) for v in unroll])
+        _raise(self.L.mcig_batch_set_tuning(self._h, int(block), u))
 
     def autotune(self, cache_path=None):
         _raise(self.L.mcig_batch_autotune(self._h, cache_path.encode() if cache_path else None))
-        return self.blocks()
+        return self.tuning()
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -131,7 +131,7 @@ def test_chunked_sampling_equals_one_launch(nskip):
     estimates, averages, errors and counts."""
     import mcintegratorplusplus_gb300 as mcig
     res = []
-    for chunks in (1, 4, 3):
+    for chunks in (1, 4, 3):  # 1: one launch (the default)
         nc, nmc = 512, 2400
         m = mcig.MCI(16, nc, precision=mcig.PREC_FP32)
         m.setSeed(21)

@@ -135,8 +135,9 @@ int mcig_set_ndecorrelation_steps(mcig_mci *h, int64_t n);
 /* MCI::setTrialMove(SRRDType, veclen, ntypes, typeEnds) (MCIntegrator.cpp:431-446)
  * and setTrialMove(MoveType) (:423-429).  movetype MCIG_MOVE_ALL ignores
  * veclen; MCIG_MOVE_VEC uses veclen >= 1; MCIG_MOVE_MULTISTEP installs the
- * default MultiStepMove(ndim) (MultiStepMove.hpp:49-52).  Only the uniform and
- * Gaussian distributions run on the device (MCIG_ERR_UNSUPPORTED otherwise). */
+ * default MultiStepMove(ndim) (MultiStepMove.hpp:49-52).  Every SRRDType runs on the
+ * device: in replay mode from the reference's recorded draws (bit for bit), with Philox draws
+ * as the transforms of mcig_common.cuh move_draws_srrd. */
 int mcig_set_trial_move(mcig_mci *h, int movetype, int srrd, int veclen, int ntypes, const int *typeEnds);
 /* MultiStepMove(ndim, nsteps) with sub-move SRRDVecMove(ndim/veclen, veclen, step)
  * (MultiStepMove.hpp:40-52, src/MultiStepMove.cpp:6-75) */

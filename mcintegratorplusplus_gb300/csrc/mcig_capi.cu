@@ -2128,8 +2128,12 @@ int mcig_flow_train_device(mcig_flow *f, const float *d_x, int64_t nsrc, int ste
 int mcig_flow_pass_device_cm(mcig_flow *f, int dir, const float *d_in, const double *in_cm, int64_t nstride, int64_t n,
                              float *out_cm, float *d_logq, cudaStream_t st);
 int mcig_flow_dim(const mcig_flow *f);
+int mcig_flow_propose_device(mcig_flow *f, uint64_t cycle, uint32_t key0, uint32_t key1, int64_t nstride, int64_t n,
+                             float *out_cm, float *d_logq, cudaStream_t st);
+int mcig_flow_density_cmf_device(mcig_flow *f, const float *in_cmf, int64_t nstride, int64_t n, float *d_logq,
+                                 cudaStream_t st);
 
-enum { TAG_FLOW_Z = 3, TAG_FLOW_ACCEPT = 4 };
+enum { TAG_FLOW_ACCEPT = 4 }; // (the proposal's z uses tag 3 in the generative pass)
 
 // walkers [ndim][nchains] (double) -> rows [nchains][ndim] (float)
 __global__ void walkers_to_rows_kernel(const double *x, int ndim, int nc, float *out)
@@ -2137,23 +2141,6 @@ __global__ void walkers_to_rows_kernel(const double *x, int ndim, int nc, float 
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) { return; }
     for (int i = 0; i < ndim; ++i) { out[(size_t)c * ndim + i] = (float)x[(size_t)i * nc + c]; }
-}
-
-// standard normal z for the flow proposal of cycle `cycle` (Philox, Box-Muller)
-__global__ void flow_z_kernel(KParams p, uint64_t cycle, float *z)
-{
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= p.nchains) { return; }
-    for (int b = 0; b < (p.ndim + 3) / 4; ++b) {
-        const P4 q = philox4x32_10((uint32_t)cycle, (uint32_t)(cycle >> 32), (uint32_t)c, (TAG_FLOW_Z << 12) | b,
-                                   p.key0 ^ 0x6A09E667u, p.key1 ^ 0xBB67AE85u);
-        float d[4];
-        box_muller_f(q.a, q.b, d[0], d[1]);
-        box_muller_f(q.c, q.d, d[2], d[3]);
-        for (int k = 0; k < 4; ++k) {
-            if (b * 4 + k < p.ndim) { z[(size_t)c * p.ndim + b * 4 + k] = d[k]; }
-        }
-    }
 }
 
 // Metropolis-Hastings test of the flow proposal x' for every chain:
@@ -2221,9 +2208,9 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     if ((rc = alloc_obs_data(h, h->obs, nmc, h->obsdata, h->obs_nstore, h->full32))) { return rc; }
     const size_t nc = (size_t)h->nchains;
     const int D = h->ndim;
-    DBuf<float> xf, z, xprop, lq_cur, lq_prop;
+    DBuf<float> xf, xprop, lq_cur, lq_prop;
     DBuf<int64_t> nflow;
-    if ((rc = xf.alloc(nc * D)) || (rc = z.alloc(nc * D)) || (rc = xprop.alloc(nc * D)) || (rc = lq_cur.alloc(nc)) ||
+    if ((rc = xf.alloc(nc * D)) || (rc = xprop.alloc(nc * D)) || (rc = lq_cur.alloc(nc)) ||
         (rc = lq_prop.alloc(nc)) || (rc = nflow.alloc(nc))) {
         return rc;
     }
@@ -2250,13 +2237,16 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     }
     uint64_t cycle = 0;
     // one independence proposal for every chain; krow = Full row to record, -1 none
+    // log q of the current walkers and of the proposals both come from the density pass, one
+    // deterministic function, so the Metropolis-Hastings ratio uses the same q on both sides
+    // (the generative pass's own log q of x' differs from it by the bf16 rounding of its MLP
+    // inputs); the proposal's z is drawn inside the generative pass
     auto flow_cycle = [&](int64_t krow) -> int {
-        int r; // log q of the current walkers (read chain-minor), proposal x' = f(z) (written chain-minor)
-        if ((r = mcig_flow_pass_device_cm(f, 1, nullptr, h->x.p, (int64_t)nc, (int64_t)nc, nullptr, lq_cur.p, h->stream))) {
-            return r;
-        }
-        flow_z_kernel<<<tg, tb, 0, h->stream>>>(sp, cycle, z.p);
-        if ((r = mcig_flow_pass_device_cm(f, 0, z.p, nullptr, (int64_t)nc, (int64_t)nc, xprop.p, lq_prop.p, h->stream))) {
+        int r;
+        if ((r = mcig_flow_pass_device_cm(f, 1, nullptr, h->x.p, (int64_t)nc, (int64_t)nc, nullptr, lq_cur.p, h->stream)) ||
+            (r = mcig_flow_propose_device(f, cycle, kp.key0 ^ 0x6A09E667u, kp.key1 ^ 0xBB67AE85u, (int64_t)nc, (int64_t)nc,
+                                          xprop.p, lq_prop.p, h->stream)) ||
+            (r = mcig_flow_density_cmf_device(f, xprop.p, (int64_t)nc, (int64_t)nc, lq_prop.p, h->stream))) {
             return r;
         }
         flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p);

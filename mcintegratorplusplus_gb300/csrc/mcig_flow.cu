@@ -84,7 +84,36 @@ struct FlowArgs {
     const double *in_cm;
     float *out_cm;
     int64_t cm_stride;
+    const float *in_cmf;      // chain-minor float input in_cmf[c * cm_stride + row] (replaces in)
+    // generative direction: z drawn in the kernel (replaces in): coordinate i of row r is
+    // Box-Muller normal i % 4 of Philox block (zcycle lo, zcycle hi, r, FLOW_TAG_Z << 12 | i / 4)
+    // with key (zk0, zk1)
+    int zgen;
+    uint32_t zk0, zk1;
+    uint64_t zcycle;
 };
+
+#define FLOW_TAG_Z 3
+
+// the standard normal z of row (chain) `row`, coordinate i, of flow proposal cycle `cycle`
+__device__ __forceinline__ float flow_z_value(const FlowArgs &f, int row, int i)
+{
+    const P4 q = philox4x32_10((uint32_t)f.zcycle, (uint32_t)(f.zcycle >> 32), (uint32_t)row,
+                               (FLOW_TAG_Z << 12) | (uint32_t)(i >> 2), f.zk0, f.zk1);
+    float z0, z1;
+    const int k = i & 3;
+    box_muller_f(k < 2 ? q.a : q.c, k < 2 ? q.b : q.d, z0, z1);
+    return (k & 1) ? z1 : z0;
+}
+
+// input value of row r (in the whole set), coordinate c, from whichever source the pass reads
+__device__ __forceinline__ float flow_input(const FlowArgs &f, int r, int c)
+{
+    if (f.zgen) { return flow_z_value(f, r, c); }
+    if (f.in_cm) { return (float)f.in_cm[(int64_t)c * f.cm_stride + r]; }
+    if (f.in_cmf) { return f.in_cmf[(int64_t)c * f.cm_stride + r]; }
+    return f.in[(int64_t)r * f.D + c];
+}
 
 // ------------------------------------------------------------------------
 // bf16 tensor-core helpers
@@ -415,10 +444,10 @@ __global__ void __launch_bounds__(FLOW_PASS_THREADS, 1) flow_pass_kernel(FlowArg
     const int rows = min(FLOW_PASS_ROWS, f.n - base);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, pair = warp % FLOW_PASS_PAIRS, half = warp / FLOW_PASS_PAIRS, r0 = pair * 16;
     const float invd = 1.f / (float)d;
-    if (f.in_cm) { // chain-minor walkers: coalesced over the rows, one coordinate at a time
+    if (f.in_cm || f.in_cmf || f.zgen) { // chain-minor walkers (coalesced over the rows) or drawn z
         for (int i = threadIdx.x; i < D * FLOW_PASS_ROWS; i += blockDim.x) {
             const int c = i / FLOW_PASS_ROWS, r = i % FLOW_PASS_ROWS;
-            float v = (r < rows) ? (float)f.in_cm[(int64_t)c * f.cm_stride + base + r] : 0.f;
+            float v = (r < rows) ? flow_input(f, base + r, c) : 0.f;
             if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); }
             s.Y[r][c] = v;
         }
@@ -491,7 +520,7 @@ __global__ void __launch_bounds__(FLOW_PASS_THREADS, 1) flow_pass_kernel(FlowArg
         if (lane < D) {
             float z, o;
             if (f.dir == 0) { // z was the input
-                z = f.in_cm ? (float)f.in_cm[(int64_t)lane * f.cm_stride + base + r] : f.in[(int64_t)(base + r) * D + lane];
+                z = flow_input(f, base + r, lane);
                 o = f.mu[lane] + __expf(f.logsig[lane]) * s.Y[r][lane];
             } else {
                 z = s.Y[r][lane];
@@ -992,6 +1021,7 @@ int mcig_flow_pass_device_cm(mcig_flow *f, int dir, const float *d_in, const dou
                              float *out_cm, float *d_logq, cudaStream_t st)
 {
     FlowArgs a;
+    memset(&a, 0, sizeof(a));
     a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = dir;
     a.in = d_in; a.out = nullptr; a.logq = d_logq;
     a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
@@ -1001,10 +1031,43 @@ int mcig_flow_pass_device_cm(mcig_flow *f, int dir, const float *d_in, const dou
     return flow_pass_launch(f, a, n, st);
 }
 
+// the flow proposal x' = f(z) of one cycle for n chains: z drawn in the pass from Philox
+// (key, cycle), x' written chain-minor (stride nstride), log q of the generative pass to d_logq
+int mcig_flow_propose_device(mcig_flow *f, uint64_t cycle, uint32_t key0, uint32_t key1, int64_t nstride, int64_t n,
+                             float *out_cm, float *d_logq, cudaStream_t st)
+{
+    FlowArgs a;
+    memset(&a, 0, sizeof(a));
+    a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = 0;
+    a.logq = d_logq;
+    a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
+    a.perm = f->perm; a.wb = f->wb; a.theta = f->theta;
+    a.wstride = WB_LAYER; a.pstride = f->pstride;
+    a.out_cm = out_cm; a.cm_stride = nstride;
+    a.zgen = 1; a.zk0 = key0; a.zk1 = key1; a.zcycle = cycle;
+    return flow_pass_launch(f, a, n, st);
+}
+
+// the density pass (log q) of n chain-minor float walkers (stride nstride)
+int mcig_flow_density_cmf_device(mcig_flow *f, const float *in_cmf, int64_t nstride, int64_t n, float *d_logq,
+                                 cudaStream_t st)
+{
+    FlowArgs a;
+    memset(&a, 0, sizeof(a));
+    a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = 1;
+    a.logq = d_logq;
+    a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
+    a.perm = f->perm; a.wb = f->wb; a.theta = f->theta;
+    a.wstride = WB_LAYER; a.pstride = f->pstride;
+    a.in_cmf = in_cmf; a.cm_stride = nstride;
+    return flow_pass_launch(f, a, n, st);
+}
+
 int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, float *d_out, float *d_logq, float *d_tape,
                           cudaStream_t st)
 {
     FlowArgs a;
+    memset(&a, 0, sizeof(a));
     a.in_cm = nullptr; a.out_cm = nullptr; a.cm_stride = 0;
     a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = dir;
     a.in = d_in; a.out = d_out; a.logq = d_logq;

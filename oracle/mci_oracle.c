@@ -381,9 +381,94 @@ static int draw_index(drawsrc *d, int n)
     return i;
 }
 
+/* ---- the other distributions of createSymRRD (include/mci/TrialMoveInterface.hpp:82-200),
+ * restated from libstdc++ (GCC 13.3, bits/random.tcc and bits/random.h) with their default
+ * parameters.  A distribution object keeps state between draws: the normal_distribution inside
+ * it caches its second value, so each move holds three normal states: [0] the distribution's own
+ * normal_distribution, [1] and [2] those of its gamma_distribution members. */
+
+/* gamma_distribution<double>(alpha, beta)::operator() (random.tcc, Marsaglia & Tsang, ACM TOMS
+ * 26 (2000) 363-372), with param_type::_M_initialize's constants; nd: the object's normal */
+static double gamma_draw(mt64 *m, normstate *nd, double alpha, double beta)
+{
+    const double malpha = alpha < 1.0 ? alpha + 1.0 : alpha;
+    const double a2 = 1.0 / sqrt(9.0 * (malpha - 1.0 / 3.0));
+    const double a1 = malpha - 1.0 / 3.0;
+    double u, v, n;
+    do {
+        do {
+            n = polar_normal(m, nd);
+            v = 1.0 + a2 * n;
+        } while (v <= 0.0);
+        v = v * v * v;
+        u = canonical(m);
+    } while (u > 1.0 - 0.0331 * n * n * n * n && log(u) > (0.5 * n * n + a1 * (1.0 - v + log(v))));
+    if (alpha == malpha) { return a1 * v * beta; }
+    do {
+        u = canonical(m);
+    } while (u == 0.0);
+    return pow(u, 1.0 / alpha) * a1 * v * beta;
+}
+
+/* bernoulli_distribution(0.5)::operator() of SymmetrizedPRRD (TrialMoveInterface.hpp:82-98):
+ * the positive value first, then the sign */
+static double symmetrized(mt64 *m, double val)
+{
+    return (canonical(m) - 0.0 < 0.5 * (1.0 - 0.0)) ? val : -val;
+}
+
+/* one draw of SRRDType srrd (Factories.hpp:115-128) from the engine */
+static double srrd_engine(mt64 *m, int srrd, normstate *st)
+{
+    switch (srrd) {
+    case MCIG_SRRD_UNIFORM: return canonical(m) * 2.0 + -1.0;
+    case MCIG_SRRD_GAUSSIAN: return polar_normal(m, &st[0]);
+    case MCIG_SRRD_STUDENT: { /* student_t_distribution(n = 1): _M_nd * sqrt(n / _M_gd), gamma(n/2, 2);
+                               * GCC evaluates the normal first */
+        const double z = polar_normal(m, &st[0]);
+        return z * sqrt(1.0 / gamma_draw(m, &st[1], 1.0 / 2, 2.0));
+    }
+    case MCIG_SRRD_CAUCHY: { /* cauchy_distribution(0, 1) */
+        double u;
+        do {
+            u = canonical(m);
+        } while (u == 0.5);
+        const double pi = 3.1415926535897932384626433832795029;
+        return 0.0 + 1.0 * tan(pi * u);
+    }
+    case MCIG_SRRD_EXPONENTIAL: return symmetrized(m, -log(1.0 - canonical(m)) / 1.0);
+    case MCIG_SRRD_GAMMA: return symmetrized(m, gamma_draw(m, &st[1], 1.0, 1.0));
+    case MCIG_SRRD_WEIBULL: return symmetrized(m, 1.0 * pow(-log(1.0 - canonical(m)), 1.0 / 1.0));
+    case MCIG_SRRD_LOGNORMAL: return symmetrized(m, exp(1.0 * polar_normal(m, &st[0]) + 0.0));
+    case MCIG_SRRD_CHISQ: return symmetrized(m, 2 * gamma_draw(m, &st[1], 1.0 / 2, 1.0));
+    default: { /* FISHER: fisher_f_distribution(m = 1, n = 1): (gamma_x(m/2) n) / (gamma_y(n/2) m) */
+        const double gx = gamma_draw(m, &st[1], 1.0 / 2, 1.0) * 1.0;
+        const double gy = gamma_draw(m, &st[2], 1.0 / 2, 1.0) * 1.0;
+        return symmetrized(m, gx / gy);
+    }
+    }
+}
+
+/* n draws of SRRDType srrd from a fresh distribution object and std::mt19937_64(seed) */
+void orc_srrd_stream(int srrd, uint64_t seed, int64_t n, double *out)
+{
+    mt64 m;
+    mt_seed(&m, seed);
+    normstate st[3] = {{0, 0.}, {0, 0.}, {0, 0.}};
+    for (int64_t i = 0; i < n; ++i) { out[i] = srrd_engine(&m, srrd, st); }
+}
+
+/* the move draw of SRRDType srrd: tape, Philox (uniform and Gaussian) or the engine */
 static double draw_srrd(drawsrc *d, int srrd, normstate *st)
 {
-    return (srrd == MCIG_SRRD_GAUSSIAN) ? draw_normal(d, st) : draw_upm1(d);
+    if (srrd == MCIG_SRRD_GAUSSIAN) { return draw_normal(d, &st[0]); }
+    if (srrd == MCIG_SRRD_UNIFORM) { return draw_upm1(d); }
+    double v;
+    if (d->philox) { return philox_next(d); } /* not reached: orc_set_philox takes uniform and Gaussian only */
+    if (d->tape) { tape_next(d, &v); return v; }
+    v = srrd_engine(&d->mt, srrd, st);
+    rec_push(d, v);
+    return v;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1033,7 +1118,7 @@ typedef struct {
     int *cidx;
     int nchanged, accepted;
     double *step; /* [ntypes]: step sizes of the move (MultiStepMove: of its sub-move) */
-    normstate nd_move;
+    normstate nd_move[3]; /* the move's distribution: its normal_distribution and those of its gamma members */
     drawsrc ds;
     int64_t acc, rej;
     double *po[MAXPDF], *pn[MAXPDF];
@@ -1228,7 +1313,7 @@ static void reset_steps(orc_mci *h, int ntypes, double v)
         free(h->ch[c].step);
         h->ch[c].step = (double *)malloc((size_t)ntypes * sizeof(double));
         for (int i = 0; i < ntypes; ++i) { h->ch[c].step[i] = v; }
-        h->ch[c].nd_move.avail = 0; /* a new move object has a fresh distribution */
+        for (int k = 0; k < 3; ++k) { h->ch[c].nd_move[k].avail = 0; } /* a new move object has a fresh distribution */
     }
 }
 
@@ -1236,7 +1321,7 @@ static void reset_steps(orc_mci *h, int ntypes, double v)
  * setTrialMove(MoveType) (:423-429) via the factories (Factories.hpp:148-227) */
 int orc_set_trial_move(orc_mci *h, int movetype, int srrd, int veclen, int ntypes, const int *typeEnds)
 {
-    if (srrd != MCIG_SRRD_UNIFORM && srrd != MCIG_SRRD_GAUSSIAN) { return fail(MCIG_ERR_UNSUPPORTED, "only uniform and gaussian SRRD moves"); }
+    if (srrd < MCIG_SRRD_UNIFORM || srrd > MCIG_SRRD_FISHER) { return fail(MCIG_ERR_INVALID_ARGUMENT, "unknown SRRDType"); }
     if (movetype == MCIG_MOVE_MULTISTEP) { return orc_set_multistep_move(h, h->ndim, MCIG_SRRD_UNIFORM, 1, 0.05); }
     if (ntypes < 1) { ntypes = 1; }
     int vl = (movetype == MCIG_MOVE_VEC) ? (veclen < 1 ? 1 : veclen) : 0;
@@ -1549,7 +1634,7 @@ static double multistep_move(const orc_mci *h, chainst *c)
     pdfcont_init(h->ms_npdf, h->ms_pdf, c->x, c->spo, c->spn);
     const double oldPDF = pdfcont_old_value(h->ms_npdf, h->ms_pdf, c->spo);
     for (int s = 0; s < h->ms_nsteps; ++s) {
-        vec_move(h, c, h->ms_srrd, h->ms_veclen, &c->nd_move);
+        vec_move(h, c, h->ms_srrd, h->ms_veclen, c->nd_move);
         const double pdfAcc = pdfcont_accept(h->ms_npdf, h->ms_pdf, c, c->spo, c->spn);
         const int acc = (draw_u01(&c->ds) <= pdfAcc * 1.);
         if (acc) {
@@ -1575,13 +1660,13 @@ static void step_mrt2(const orc_mci *h, chainst *c)
         int xi = 0;
         for (int t = 0; t < h->ntypes; ++t) {
             while (xi < h->typeEnds[t]) {
-                c->xn[xi] = c->xn[xi] + c->step[t] * draw_srrd(&c->ds, h->srrd, &c->nd_move);
+                c->xn[xi] = c->xn[xi] + c->step[t] * draw_srrd(&c->ds, h->srrd, c->nd_move);
                 ++xi;
             }
         }
         c->nchanged = nd;
     } else if (h->movetype == MCIG_MOVE_VEC) {
-        vec_move(h, c, h->srrd, h->veclen, &c->nd_move);
+        vec_move(h, c, h->srrd, h->veclen, c->nd_move);
     } else {
         moveAcc = multistep_move(h, c);
     }

@@ -35,6 +35,9 @@ void orc_canonical_stream(uint64_t seed, int64_t n, double *out);
 void orc_normal_stream(uint64_t seed, int64_t n, double *out);
 void orc_uniform_int_stream(uint64_t seed, int64_t n, int64_t nvals, int64_t *out);
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* n draws of SRRDType srrd (createSymRRD's distribution with its default parameters) from a
+ * fresh distribution object and std::mt19937_64(seed) */
+void orc_srrd_stream(int srrd, uint64_t seed, int64_t n, double *out);
 
 /* --- the integrator (one reference MCI per chain) --- */
 orc_mci *orc_create(int ndim, int nchains);

@@ -310,6 +310,13 @@ def uniform_int_stream(seed, n, nvals):
     return out
 
 
+def srrd_stream(srrd, seed, n):
+    """n draws of SRRDType srrd (createSymRRD's default distribution) from a fresh object."""
+    out = np.zeros(n)
+    lib().orc_srrd_stream(int(srrd), ctypes.c_uint64(seed), ctypes.c_int64(n), _dp(out))
+    return out
+
+
 def philox4x32_10(ctr, key):
     c = (ctypes.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in ctr])
     k = (ctypes.c_uint32 * 2)(*[int(v) & 0xFFFFFFFF for v in key])

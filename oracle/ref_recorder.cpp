@@ -25,6 +25,7 @@ extern "C" {
 #include <cstdio>
 #include <string>
 #include <vector>
+#include <unistd.h>
 
 using namespace mci;
 
@@ -75,7 +76,8 @@ struct RunSpec {
     const char *name;
     int ndim;
     uint64_t seed;
-    int move;      // 0 all uniform, 1 all gaussian, 2 vec uniform veclen, 3 multistep, 4 typed all uniform, 5 vec gaussian
+    int move;      // 0 all uniform, 1 all gaussian, 2 vec uniform veclen, 3 multistep, 4 typed all uniform, 5 vec gaussian,
+                   // 10 + k: SRRDType k with veclen (0: all coordinates)
     int veclen;
     int pdf;       // 0 Gauss(nd), 1 ThreeDimGaussianPDF, 2 ExpNDPDF(nd), 3 none
     int obsset;    // 0 X2Sum+XND, 1 XSquared, 2 X2Sum+X2, 3 GaussXSquared
@@ -113,7 +115,9 @@ static void run_case(const RunSpec &r, bool last)
     }
     case 4: mci.setTrialMove(SRRDType::Uniform, 0, 2, typeEnds); break;
     case 5: mci.setTrialMove(SRRDType::Gaussian, r.veclen); break;
-    default: break;
+    default:
+        if (r.move >= 10) { mci.setTrialMove(static_cast<SRRDType>(r.move - 10), r.veclen); } // SRRDType move - 10
+        break;
     }
     mci.setTargetAcceptanceRate(r.target);
     mci.setNfindMRT2Iterations(r.nfind);
@@ -163,6 +167,47 @@ static void run_case(const RunSpec &r, bool last)
     std::printf("}%s\n", last ? "" : ",");
 }
 
+static std::string json_escape_file(const std::string &path)
+{
+    std::FILE *f = std::fopen(path.c_str(), "rb");
+    std::string out;
+    if (!f) { return out; }
+    int ch;
+    while ((ch = std::fgetc(f)) != EOF) {
+        if (ch == '\n') { out += "\\n"; }
+        else if (ch == '"' || ch == '\\') { out.push_back('\\'); out.push_back((char)ch); }
+        else { out.push_back((char)ch); }
+    }
+    std::fclose(f);
+    std::remove(path.c_str());
+    return out;
+}
+
+// the reference's own observable and walker files of a main sampling run
+// (MCI::storeObservablesOnFile / storeWalkerPositionsOnFile, src/MCIntegrator.cpp:495-542):
+// Gauss(3), uniform all-move, calibration and 200 burn-in steps in a first integrate call,
+// then 1,000 recorded steps with x.x (Simple, nskip 1) and x_i (Simple, nskip 3)
+static void run_file_case()
+{
+    MCI mci(3);
+    mci.setSeed(4321);
+    mci.addSamplingFunction(Gauss(3));
+    mci.setNfindMRT2Iterations(-50);
+    mci.setNdecorrelationSteps(200);
+    mci.addObservable(X2Sum(3), 0, 1, false, EstimatorType::Noop);
+    mci.addObservable(XND(3), 0, 3, false, EstimatorType::Noop);
+    double avg[4], err[4];
+    mci.integrate(0, avg, err, true, true);
+    const std::string po = "/tmp/mcig_ref_obs_" + std::to_string((long long)getpid()) + ".txt";
+    const std::string pw = "/tmp/mcig_ref_wlk_" + std::to_string((long long)getpid()) + ".txt";
+    mci.storeObservablesOnFile(po, 100);
+    mci.storeWalkerPositionsOnFile(pw, 50);
+    mci.integrate(1000, avg, err, false, false);
+    std::printf("\"file_case\": {\"seed\": 4321, \"ndecorr\": 200, \"nmc\": 1000, \"obs_freq\": 100, \"wlk_freq\": 50},\n");
+    std::printf("\"file_obs\": \"%s\",\n", json_escape_file(po).c_str());
+    std::printf("\"file_wlk\": \"%s\",\n", json_escape_file(pw).c_str());
+}
+
 int main()
 {
     std::printf("{\n");
@@ -187,6 +232,24 @@ int main()
         std::vector<double> iv(16);
         for (int i = 0; i < 16; ++i) { iv[i] = ui(g4); }
         put_array("uniform_int3_seed1234", iv.data(), 16);
+    }
+    // the other move distributions (createSymRRD, TrialMoveInterface.hpp:113-200): 64 draws of a
+    // fresh object each from mt19937_64(1234)
+    {
+        std::vector<double> v(64);
+        auto rec = [&](const char *name, auto dist) {
+            std::mt19937_64 g(1234);
+            for (int i = 0; i < 64; ++i) { v[i] = dist(g); }
+            put_array(name, v.data(), 64);
+        };
+        rec("srrd2_seed1234", createSymRRD<std::student_t_distribution<double>>());
+        rec("srrd3_seed1234", createSymRRD<std::cauchy_distribution<double>>());
+        rec("srrd4_seed1234", createSymRRD<SymmetrizedPRRD<std::exponential_distribution<double>>>());
+        rec("srrd5_seed1234", createSymRRD<SymmetrizedPRRD<std::gamma_distribution<double>>>());
+        rec("srrd6_seed1234", createSymRRD<SymmetrizedPRRD<std::weibull_distribution<double>>>());
+        rec("srrd7_seed1234", createSymRRD<SymmetrizedPRRD<std::lognormal_distribution<double>>>());
+        rec("srrd8_seed1234", createSymRRD<SymmetrizedPRRD<std::chi_squared_distribution<double>>>());
+        rec("srrd9_seed1234", createSymRRD<SymmetrizedPRRD<std::fisher_f_distribution<double>>>());
     }
     // estimators on a fixed correlated series (test/ut1/main.cpp:251-314 pattern)
     {
@@ -251,6 +314,7 @@ int main()
             put_array(c.name, a->getData(), a->getNData());
         }
     }
+    run_file_case();
     // full integrations
     const RunSpec runs[] = {
         // name, nd, seed, move, veclen, pdf, obsset, bs, skip, estim, nfind, ndecorr, nmc, periodic, target, nbits
@@ -265,6 +329,14 @@ int main()
         {"periodic_3dgauss", 3, 5649871, 0, 0, 1, 1, 1, 1, -1, 10, 1000, 10000, 1, 0.5, 4096},
         {"nopdf_periodic", 3, 5649871, 0, 0, 3, 3, 1, 1, 1, 0, 0, 10000, 1, 0.5, 64},
         {"auto_decorr", 3, 2024, 0, 0, 0, 0, 1, 1, -1, -50, -10000, 8192, 0, 0.5, 8192},
+        {"srrd_student_all", 3, 211, 12, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
+        {"srrd_cauchy_all", 3, 311, 13, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
+        {"srrd_exponential_vec1", 4, 411, 14, 1, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
+        {"srrd_gamma_all", 3, 511, 15, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
+        {"srrd_weibull_all", 3, 611, 16, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
+        {"srrd_lognormal_all", 3, 711, 17, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
+        {"srrd_chisq_vec1", 4, 811, 18, 1, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
+        {"srrd_fisher_all", 3, 911, 19, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096},
     };
     const int nruns = sizeof(runs) / sizeof(runs[0]);
     for (int i = 0; i < nruns; ++i) { run_case(runs[i], i == nruns - 1); }

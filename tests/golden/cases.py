@@ -33,6 +33,15 @@ RUNS = [
     ("periodic_3dgauss", 3, 5649871, 0, 0, 1, 1, 1, 1, -1, 10, 1000, 10000, 1, 0.5, 4096),
     ("nopdf_periodic", 3, 5649871, 0, 0, 3, 3, 1, 1, EST_UNCORRELATED, 0, 0, 10000, 1, 0.5, 64),
     ("auto_decorr", 3, 2024, 0, 0, 0, 0, 1, 1, -1, -50, -10000, 8192, 0, 0.5, 8192),
+    # move 10 + k: SRRDType k (all coordinates, or single-coordinate vector moves with veclen 1)
+    ("srrd_student_all", 3, 211, 12, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
+    ("srrd_cauchy_all", 3, 311, 13, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
+    ("srrd_exponential_vec1", 4, 411, 14, 1, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
+    ("srrd_gamma_all", 3, 511, 15, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
+    ("srrd_weibull_all", 3, 611, 16, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
+    ("srrd_lognormal_all", 3, 711, 17, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
+    ("srrd_chisq_vec1", 4, 811, 18, 1, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
+    ("srrd_fisher_all", 3, 911, 19, 0, 0, 0, 16, 1, -1, -50, 500, 4096, 0, 0.5, 4096),
 ]
 
 FIELDS = ("name", "ndim", "seed", "move", "veclen", "pdf", "obsset", "blocksize", "nskip", "estim",
@@ -92,6 +101,8 @@ def configure(m, r, set_seed):
         m.set_trial_move(MOVE_ALL, SRRD_UNIFORM, 0, 2, [1, nd])
     elif mv == 5:
         m.set_trial_move(MOVE_VEC, SRRD_GAUSSIAN, r["veclen"])
+    elif mv >= 10:
+        m.set_trial_move(MOVE_VEC if r["veclen"] else MOVE_ALL, mv - 10, r["veclen"])
     m.set_target_acceptance_rate(r["target"])
     m.set_nfind_mrt2_iterations(r["nfind"])
     m.set_ndecorrelation_steps(r["ndecorr"])

@@ -41,3 +41,42 @@ def test_observable_and_walker_files(tmp_path):
     assert not fo.exists()
     with pytest.raises(ValueError):
         g.storeObservablesOnFile(fo, 0)
+
+
+def test_files_equal_the_references_own_files_byte_for_byte(tmp_path):
+    """The reference's own observable and walker files of a main sampling run (recorded by
+    oracle/ref_recorder.cpp into tests/golden/reference_golden.json), against the device's files
+    of the same run in FP64 replay: the draws are the reference's (the oracle records them;
+    it reproduces the reference's engine and distributions bit for bit), so every line must
+    be identical, byte for byte."""
+    import mcintegratorplusplus_gb300 as mcig
+    from oracle import oracle as orc
+    import cases
+
+    g = cases.golden()
+    fc = g["file_case"]
+
+    def configure(m):
+        m.add_sampling_function(mcig.PDF_GAUSS)
+        m.set_nfind_mrt2_iterations(-50)
+        m.set_ndecorrelation_steps(fc["ndecorr"])
+        m.add_observable(mcig.OBS_X2SUM, (), 0, 1, False, mcig.EST_NOOP)
+        m.add_observable(mcig.OBS_XND, (), 0, 3, False, mcig.EST_NOOP)
+
+    o = orc.OracleMCI(3, 1)
+    o.set_seeds([fc["seed"]])
+    configure(o)
+    o.set_record(True)
+    o.integrate(0, True, True)
+    o.integrate(fc["nmc"], False, False)
+    tape, lens = o.get_tapes()
+    d = mcig.MCI(3, 1, precision=mcig.PREC_FP64)
+    configure(d)
+    d.setReplay(tape, lens)
+    d.integrate(0, True, True)
+    fo, fw = tmp_path / "observables.txt", tmp_path / "walker.txt"
+    d.storeObservablesOnFile(fo, fc["obs_freq"])
+    d.storeWalkerPositionsOnFile(fw, fc["wlk_freq"])
+    d.integrate(fc["nmc"], False, False)
+    assert fw.read_text() == g["file_wlk"]
+    assert fo.read_text() == g["file_obs"]

@@ -166,3 +166,41 @@ def test_learned_proposal_beats_plain_mh(mcig):
     assert acc > 0.05
     assert abs(a_f) < 4.0 * max(e_f, np.sqrt(var_x1 / ess_f))  # analytic mean 0
     assert ess_f > 5.0 * ess_p
+
+
+@pytest.mark.gpu
+def test_flow_sampler_unbiased_on_asymmetric_statistics(mcig):
+    """The flow-assisted sampler (both log q of the Metropolis-Hastings ratio from the same
+    density pass) against statistics a symmetric bias would not hide: <x_i^2> of every
+    coordinate (analytic 1 + mean_k m_ki^2) and the occupancy of each of the four modes
+    (analytic 1/4), both within 3 standard errors from the spread of the chain means."""
+    params, means, _ = c5_target()
+    nchains, nmc, nsub = 2048, 1 << 13, 256
+    m = mcig.MCI(D, nchains, precision=mcig.PREC_FP32)
+    m.setSeed(91)
+    rng = np.random.default_rng(8)
+    m.setX(rng.standard_normal((nchains, D)) * 3.0)
+    m.addSamplingFunction(mcig.PDF_GAUSS_MIX, params)
+    m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+    m.setNdecorrelationSteps(1000)
+    m.setFullStorage(32)
+    m.addObservable(mcig.OBS_X2, (), 1, 1, False, mcig.EST_UNCORRELATED)
+    m.addObservable(mcig.OBS_XND, (), 1, 1, False, mcig.EST_UNCORRELATED)
+    f = mcig.Flow(D, L, H, seed=6)
+    _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=2048, train_steps=400, batch=2048, lr=2e-3)
+    assert acc > 0.3
+    ca, _ = m.getChainResults()
+    x2 = ca[:, :D]
+    exact = 1.0 + (means ** 2).mean(axis=0)
+    z = np.abs(x2.mean(0) - exact) / (x2.std(0, ddof=1) / np.sqrt(nchains))
+    assert z.max() < 3.5, z  # 24 coordinates: the largest of 24 normal deviates
+    occ = np.zeros((nsub, 4))  # [chain][mode]: fraction of the chain's samples nearest each mode
+    for c0 in range(0, nsub, 32):
+        xs = m.getObsDataChains(1, c0, 32).reshape(32, nmc, D)
+        d2 = (xs ** 2).sum(-1)[:, :, None] - 2.0 * xs @ means.T + (means ** 2).sum(-1)[None, None]
+        near = np.argmin(d2, axis=2)
+        occ[c0:c0 + 32] = np.stack([(near == k).mean(axis=1) for k in range(4)], axis=1)
+    zo = np.abs(occ.mean(0) - 0.25) / (occ.std(0, ddof=1) / np.sqrt(nsub))
+    assert zo.max() < 3.0, (occ.mean(0), zo)
+    print("\nflow sampler: <x_i^2> max z %.2f, mode occupancy %s (max z %.2f), flow acceptance %.3f"
+          % (z.max(), np.round(occ.mean(0), 4), zo.max(), acc))

@@ -23,6 +23,15 @@ def test_distributions_match_libstdcxx():
     assert list(orc.uniform_int_stream(1234, 16, 3)) == [int(v) for v in G["uniform_int3_seed1234"]]
 
 
+@pytest.mark.parametrize("srrd", range(2, 10))
+def test_other_move_distributions_match_libstdcxx(srrd):
+    """Student t, Cauchy and the symmetrized exponential, gamma, Weibull, lognormal,
+    chi-squared and Fisher distributions of the reference's moves: 64 draws of each, bit for
+    bit (they drive the reference's SRRD moves; the tape carries them to the device)."""
+    g = cases.golden()
+    np.testing.assert_array_equal(orc.srrd_stream(srrd, 1234, 64), np.array(g["srrd%d_seed1234" % srrd]))
+
+
 def test_philox_known_answers():
     # Random123 known-answer vectors for philox4x32-10
     assert orc.philox4x32_10([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]

@@ -322,16 +322,17 @@ template <> struct AccSlot<true> {
 // proto values of plugin sampling functions: protoold / protonew of the main chain's (upo,
 // upn) and of MultiStepMove's sub-pdfs (mpo, mpn), the k-th at k * max_nproto; an empty base
 // of the built-in kernels
-template <class R, int CAP, bool ON> struct UserProtoStore {
+template <class R, int CAP, int PCAP, bool ON> struct UserProtoStore {
     R upo[CAP], upn[CAP], mpo[CAP], mpn[CAP];
+    R uprep[PCAP]; // observationCallback output of each plugin pdf, the k-th at k * max_nprep
 };
-template <class R, int CAP> struct UserProtoStore<R, CAP, false> {
-    static constexpr R *upo = nullptr, *upn = nullptr, *mpo = nullptr, *mpn = nullptr;
+template <class R, int CAP, int PCAP> struct UserProtoStore<R, CAP, PCAP, false> {
+    static constexpr R *upo = nullptr, *upn = nullptr, *mpo = nullptr, *mpn = nullptr, *uprep = nullptr;
 };
 
 // U: the plugin's functor lists (mcig_plugin.cuh); mcig::NoPlugin for the built-in kernels
 template <class R, int RNG, bool KAHAN, class U = mcig::NoPlugin>
-struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, (U::npdf > 0)> {
+struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXPDF * U::max_nprep, (U::npdf > 0)> {
     static constexpr bool EXACT = std::is_same<R, double>::value;
     static constexpr int NV = 2 * MCIG_MAXDIM + 8;
     using AccV = typename std::conditional<KAHAN, float, double>::type;
@@ -697,6 +698,31 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, (U::npdf 
         p.nrej[c] = n - na;
     }
 
+    // the dependencies a dependent plugin observable reads at the walker x: the plugin pdfs'
+    // proto values and observationCallback data (SamplingFunctionContainer::prepareObservation,
+    // SamplingFunctionContainer.cpp:50-55), and the step's observable values so far
+    __device__ void prepare_deps(mcig::UserDeps<R> &d, const R *vals)
+    {
+        d.npdf = p.npdf;
+        d.obsvals = vals;
+        for (int k = 0; k < MCIG_MAXPDF; ++k) {
+            d.nproto[k] = 0;
+            d.proto[k] = nullptr;
+            d.prep[k] = nullptr;
+        }
+        if constexpr (USER_PDF) {
+            for (int k = 0; k < p.npdf; ++k) {
+                if (!user_pdf(p.pdf[k])) { continue; }
+                d.nproto[k] = p.pdf[k].nproto;
+                d.proto[k] = this->upo + k * MP;
+                R *pr = this->uprep + k * U::max_nprep;
+                if (U::prepare(p.pdf[k].kind - MCIG_PDF_USER, uargs(p.pdf[k].poff, p.pdf[k].np), (const R *)x, d.proto[k], pr)) {
+                    d.prep[k] = pr;
+                }
+            }
+        }
+    }
+
     // MCI::sample(npoints, container, flagMC) (MCIntegrator.cpp:290-321) with the
     // accumulators: observable o is evaluated at the walker position after steps
     // r = 0, nskip, 2 nskip, ... (AccumulatorInterface.cpp:21-29, :99-114).  The
@@ -721,8 +747,11 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, (U::npdf 
             kacc[o] = 0;
             bidx[o] = 0;
         }
+        mcig::UserDeps<R> deps;
+        bool prepared = false;
         for (int64_t r = 0; r < n; ++r) {
             const bool a = step(movetype);
+            prepared = false;
             if (c == 0 && dpos < p.ndump && r == p.dump_steps[dpos]) {
                 for (int i = 0; i < p.ndim; ++i) { p.dump_x[dpos * p.ndim + i] = (double)x[i]; }
                 ++dpos;
@@ -734,19 +763,32 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, (U::npdf 
                 if (skipleft[o] > 0) { --skipleft[o]; continue; } // accumulate when nskip divides r
                 skipleft[o] = od.nskip - 1;
                 const int64_t k = kacc[o]++; // accumulation index r / nskip
-                if (user_obs(od)) { U::observe(od.kind - MCIG_OBS_USER, uargs(od.poff, od.np), (const R *)x, vals); }
-                else { obs_eval<R>(p, od, x, vals, blob); }
+                // plugin kernels keep every value of the step at its offset, for dependent observables
+                R *const v = USER_OBS ? vals + od.voff : vals;
+                if (user_obs(od)) {
+                    if constexpr (U::any_deps) {
+                        if (!prepared) { // SamplingFunctionContainer::prepareObservation at this walker
+                            prepare_deps(deps, vals);
+                            prepared = true;
+                        }
+                        U::observe_deps(od.kind - MCIG_OBS_USER, uargs(od.poff, od.np), (const R *)x, v, deps);
+                    } else {
+                        U::observe(od.kind - MCIG_OBS_USER, uargs(od.poff, od.np), (const R *)x, v);
+                    }
+                } else {
+                    obs_eval<R>(p, od, x, v, blob);
+                }
                 if (od.acc == MCIG_ACC_FULL) { // FullAccumulator::_accumulate (FullAccumulator.cpp:14-18)
                     const size_t row = (size_t)(p.acc_offset + k);
                     if (od.full32) {
                         float *dst = (float *)od.data + row * od.nv * p.nchains + c;
-                        for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (float)vals[j]; }
+                        for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (float)v[j]; }
                     } else {
                         double *dst = (double *)od.data + row * od.nv * p.nchains + c;
-                        for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (double)vals[j]; }
+                        for (int j = 0; j < od.nv; ++j) { dst[(size_t)j * p.nchains] = (double)v[j]; }
                     }
                 } else {
-                    for (int j = 0; j < od.nv; ++j) { sums[od.voff + j].add((AccV)vals[j]); }
+                    for (int j = 0; j < od.nv; ++j) { sums[od.voff + j].add((AccV)v[j]); }
                     if (od.acc == MCIG_ACC_BLOCK && --bleft[o] == 0) { // blocksize divides k + 1
                         // block sum times 1./blocksize (BlockAccumulator.cpp:20-41)
                         bleft[o] = od.bs;

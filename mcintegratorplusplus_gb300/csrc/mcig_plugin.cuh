@@ -19,13 +19,21 @@
 //   optional:
 //   template <class R> __device__ static R updatedAcceptance(const UserArgs &, const UserWalker<R> &,
 //                                                             const R *protoold, R *protonew);
+//   static constexpr int max_nprep;                     // with observationCallback: its values
+//   template <class R> __device__ static void observationCallback(const UserArgs &, const R *x,
+//                                                                  const R *protov, R *prep);
 // Observable struct:
 //   static int nobs(int ndim);
 //   template <class R> __device__ static void observableFunction(const UserArgs &, const R *x, R *out);
+//   or, for an observable that depends on the sampling functions or earlier observables:
+//   template <class R> __device__ static void observableFunction(const UserArgs &, const R *x, R *out,
+//                                                                 const UserDeps<R> &deps);
 #pragma once
 
 #include <type_traits>
 #include <utility>
+
+#include "mcig_common.cuh"
 
 namespace mcig {
 
@@ -46,8 +54,41 @@ template <class R> struct UserWalker {
     int lo;
 };
 
+// What a dependent observable reads (DependentObservableInterface.hpp:24-53: registerDeps
+// hands it pointers into the sampling functions and the earlier accumulators): for the
+// handle's sampling function k, its proto values at the walker (protoold after the step; NULL
+// for built-in kinds, whose protos are not kept) and the data its observationCallback prepared
+// for this observation (SamplingFunctionInterface::prepareObservation, :59-62; NULL without
+// one); and the values of the observables accumulated before this one in the same step, at
+// their value offsets (the reference's rule: a dependent observable reads only earlier
+// observables whose nskip divides its own).
+template <class R> struct UserDeps {
+    int npdf;
+    int nproto[MCIG_MAXPDF];
+    const R *proto[MCIG_MAXPDF];
+    const R *prep[MCIG_MAXPDF];
+    const R *obsvals;
+};
+
 template <class... P> struct PdfList {};
 template <class... O> struct ObsList {};
+
+// optional members of a sampling function: observationCallback(args, x, protov, prep) with
+// max_nprep prepared values; of an observable: observableFunction(args, x, out, deps)
+template <class T, class R, class = void> struct HasObservationCallback : std::false_type {};
+template <class T, class R>
+struct HasObservationCallback<T, R,
+                              std::void_t<decltype(T::observationCallback(std::declval<const UserArgs &>(),
+                                                                          std::declval<const R *>(), std::declval<const R *>(),
+                                                                          std::declval<R *>()))>> : std::true_type {};
+template <class T, class R, class = void> struct HasObsDeps : std::false_type {};
+template <class T, class R>
+struct HasObsDeps<T, R,
+                  std::void_t<decltype(T::observableFunction(std::declval<const UserArgs &>(), std::declval<const R *>(),
+                                                             std::declval<R *>(), std::declval<const UserDeps<R> &>()))>>
+    : std::true_type {};
+template <class T, class = void> struct MaxNPrep { static constexpr int value = 0; };
+template <class T> struct MaxNPrep<T, std::void_t<decltype(T::max_nprep)>> { static constexpr int value = T::max_nprep; };
 
 template <class T, class R, class = void> struct HasUpdatedAcceptance : std::false_type {};
 template <class T, class R>
@@ -83,6 +124,8 @@ template <class... P, class... O> struct UserTable<PdfList<P...>, ObsList<O...>>
     static constexpr int npdf = (int)sizeof...(P);
     static constexpr int nobs = (int)sizeof...(O);
     static constexpr int max_nproto = cmax(P::max_nproto...);
+    static constexpr int max_nprep = cmax(MaxNPrep<P>::value...); // 1 when no sampling function prepares data
+    static constexpr bool any_deps = (HasObsDeps<O, double>::value || ... || false);
 
     static int nproto(int k, int ndim)
     {
@@ -125,6 +168,35 @@ template <class... P, class... O> struct UserTable<PdfList<P...>, ObsList<O...>>
     {
         int i = 0;
         ((k == i++ ? O::observableFunction(a, x, out) : (void)0), ...);
+    }
+    // observableFunction with the dependencies where the observable takes them
+    template <class R> __device__ static void observe_deps(int k, const UserArgs &a, const R *x, R *out, const UserDeps<R> &d)
+    {
+        int i = 0;
+        ((k == i++ ? observe_one<O, R>(a, x, out, d) : (void)0), ...);
+    }
+    template <class OO, class R> __device__ static void observe_one(const UserArgs &a, const R *x, R *out, const UserDeps<R> &d)
+    {
+        if constexpr (HasObsDeps<OO, R>::value) { OO::observableFunction(a, x, out, d); }
+        else { OO::observableFunction(a, x, out); }
+    }
+    // SamplingFunctionInterface::prepareObservation (:59-62): observationCallback(x, protoold);
+    // false for a sampling function without one
+    template <class R> __device__ static bool prepare(int k, const UserArgs &a, const R *x, const R *pv, R *prep)
+    {
+        bool has = false;
+        int i = 0;
+        ((k == i++ ? (void)(has = prepare_one<P, R>(a, x, pv, prep)) : (void)0), ...);
+        return has;
+    }
+    template <class PP, class R> __device__ static bool prepare_one(const UserArgs &a, const R *x, const R *pv, R *prep)
+    {
+        if constexpr (HasObservationCallback<PP, R>::value) {
+            PP::observationCallback(a, x, pv, prep);
+            return true;
+        } else {
+            return false;
+        }
     }
 };
 

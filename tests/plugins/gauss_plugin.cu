@@ -37,6 +37,13 @@ struct IndexGauss {
         }
         return exp(-e);
     }
+    // SamplingFunctionInterface::observationCallback (:104): what it prepares for the dependent
+    // observables at an observed walker, here the gradient of log p, -2 x_i
+    static constexpr int max_nprep = 64;
+    template <class R> __device__ static void observationCallback(const mcig::UserArgs &a, const R *in, const R *, R *prep)
+    {
+        for (int i = 0; i < a.ndim; ++i) { prep[i] = (R)(-2) * in[i]; }
+    }
 };
 
 // exp(-sum_i x_i^2) with a single proto value (ThreeDimGaussianPDF, :123-148, any ndim);
@@ -103,6 +110,45 @@ struct ShiftedPosition {
     }
 };
 
+// Dependent observables (DependentObservableInterface.hpp:24-53):
+// log of the product of the plugin sampling functions from their proto values at the walker,
+// -sum_k sum_i protov_k[i] (the index-proto Gauss's log density; the built-in LOGPDF order)
+struct LogPdfFromProtos {
+    static int nobs(int) { return 1; }
+    template <class R>
+    __device__ static void observableFunction(const mcig::UserArgs &, const R *, R *out, const mcig::UserDeps<R> &d)
+    {
+        R s = (R)0;
+        for (int k = 0; k < d.npdf; ++k) {
+            if (!d.proto[k]) { continue; }
+            R t = (R)0;
+            for (int i = 0; i < d.nproto[k]; ++i) { t = t + d.proto[k][i]; }
+            s = s - t;
+        }
+        out[0] = s;
+    }
+};
+
+// the first sampling function's prepared data (its observationCallback: the gradient of log p)
+struct PreparedGradient {
+    static int nobs(int ndim) { return ndim; }
+    template <class R>
+    __device__ static void observableFunction(const mcig::UserArgs &a, const R *, R *out, const mcig::UserDeps<R> &d)
+    {
+        for (int i = 0; i < a.ndim; ++i) { out[i] = d.prep[0] ? d.prep[0][i] : (R)0; }
+    }
+};
+
+// the square of the step's first observable value (an earlier observable, nskip synced)
+struct SquareOfFirst {
+    static int nobs(int) { return 1; }
+    template <class R>
+    __device__ static void observableFunction(const mcig::UserArgs &, const R *, R *out, const mcig::UserDeps<R> &d)
+    {
+        out[0] = d.obsvals[0] * d.obsvals[0];
+    }
+};
+
 using TestPdfs = mcig::PdfList<IndexGauss, SumGauss, ScaledBlockGauss>;
-using TestObss = mcig::ObsList<SquaredNorm, Position, ShiftedPosition>;
+using TestObss = mcig::ObsList<SquaredNorm, Position, ShiftedPosition, LogPdfFromProtos, PreparedGradient, SquareOfFirst>;
 MCIG_PLUGIN(TestPdfs, TestObss)

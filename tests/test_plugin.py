@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "plugins", "_build", "gauss_plugin.so")
 
 # kinds of the test plugin
 IDX_GAUSS, SUM_GAUSS, BLOCK_GAUSS = 0, 1, 2
-SQNORM, POSITION, SHIFTED = 0, 1, 2
+SQNORM, POSITION, SHIFTED, LOGPDF_DEP, GRAD_DEP, SQUARE_DEP = 0, 1, 2, 3, 4, 5
 
 
 @pytest.fixture(scope="module")
@@ -34,14 +34,14 @@ def test_plugin_exports_and_loads(plugin_path):
     library that is not a plugin."""
     P = ctypes.CDLL(plugin_path)
     assert P.mcig_plugin_abi() == 1
-    assert P.mcig_plugin_npdf() == 3 and P.mcig_plugin_nobs() == 3
+    assert P.mcig_plugin_npdf() == 3 and P.mcig_plugin_nobs() == 6
     assert P.mcig_plugin_pdf_nproto(IDX_GAUSS, 5) == 5
     assert P.mcig_plugin_pdf_nproto(IDX_GAUSS, 65) == -1  # above max_nproto
     assert P.mcig_plugin_pdf_nproto(SUM_GAUSS, 40) == 1
     assert P.mcig_plugin_obs_nvals(POSITION, 7) == 7 and P.mcig_plugin_obs_nvals(SQNORM, 7) == 1
     import mcintegratorplusplus_gb300 as mcig
     pl = mcig.Plugin(plugin_path)
-    assert (pl.npdf, pl.nobs) == (3, 3)
+    assert (pl.npdf, pl.nobs) == (3, 6)
     assert pl.pdf(2) == mcig.PDF_USER + 2 and pl.obs(1) == mcig.OBS_USER + 1
     from mcintegratorplusplus_gb300 import _lib
     with pytest.raises(ValueError, match="plugin"):
@@ -102,6 +102,33 @@ def test_vec_move_updated_acceptance_equals_builtin_gauss(mcig, plugin):
              [(mcig.OBS_X2SUM, (), 16, 1, E[0]), (mcig.OBS_XND, (), 1, 2, E[1])])
     _assert_same(u, b)
     assert 0.3 < u["acc"] < 0.7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec_name", ["fp64", "fp32"])
+def test_dependent_observables(mcig, plugin, prec_name):
+    """Observables that depend on the sampling functions and on earlier observables
+    (DependentObservableInterface.hpp:24-53): the log density from the plugin pdf's proto
+    values equals the built-in LOGPDF observable of the same walk (FP64, bit for bit), the
+    data its observationCallback prepared (the gradient -2 x) equals -2 x of the walker, and
+    the square of the step's first observable equals the square of x.x."""
+    prec = mcig.PREC_FP64 if prec_name == "fp64" else mcig.PREC_FP32
+    move = (mcig.MOVE_VEC, mcig.SRRD_UNIFORM, 1)
+    E = mcig.EST_UNCORRELATED
+    u = _run(mcig, plugin, 5, 32, prec, move, [(plugin.pdf(IDX_GAUSS), ())],
+             [(plugin.obs(SQNORM), (), 1, 1, E), (plugin.obs(LOGPDF_DEP), (), 1, 1, E),
+              (plugin.obs(GRAD_DEP), (), 1, 1, E), (plugin.obs(SQUARE_DEP), (), 1, 1, E),
+              (plugin.obs(POSITION), (), 1, 1, E)], nmc=1024)
+    sq, lp, grad, sq2, pos = u["data"]
+    np.testing.assert_array_equal(grad, -2 * pos)
+    np.testing.assert_array_equal(sq2, sq * sq)
+    if prec == mcig.PREC_FP64:
+        b = _run(mcig, plugin, 5, 32, prec, move, [(mcig.PDF_GAUSS, ())],
+                 [(mcig.OBS_X2SUM, (), 1, 1, E), (mcig.OBS_LOGPDF, (), 1, 1, E)], nmc=1024)
+        np.testing.assert_array_equal(sq, b["data"][0])
+        np.testing.assert_array_equal(lp, b["data"][1])
+    else:
+        np.testing.assert_allclose(lp, -sq, rtol=1e-5)
 
 
 @pytest.mark.gpu

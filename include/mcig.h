@@ -320,6 +320,17 @@ int mcig_plugin_unload(mcig_plugin *pl);
 int mcig_plugin_counts(const mcig_plugin *pl, int *npdf, int *nobs);
 /* attach (or, with NULL, detach) the plugin whose kinds the handle may use */
 int mcig_set_plugin(mcig_mci *h, const mcig_plugin *pl);
+/* number of trial moves of the plugin (MCIG_PLUGIN_MOVES; 0 for MCIG_PLUGIN) */
+int mcig_plugin_nmoves(const mcig_plugin *pl, int *nmove);
+/* the plugin's k-th trial move as the handle's move: MCI::setTrialMove(unique_ptr<
+ * TrialMoveInterface>) (MCIntegrator.hpp:140, MCIntegrator.cpp:423-432).  params are
+ * handed to the move (UserArgs); its step sizes (at most MCIG_MAXTYPES = 4, set to the move's
+ * step0 values in every chain) are calibrated by findMRT2Step like the built-in moves' and
+ * read with mcig_get_mrt2step; a move without step sizes skips the calibration.  The move
+ * runs in the plugin's general kernel, at the top level (not as a MultiStepMove sub-move).
+ * Errors: no plugin, k out of range, nproto above the move's max_nproto, more than
+ * MCIG_MAXTYPES step sizes, a step size index out of range. */
+int mcig_set_user_move(mcig_mci *h, int k, const double *params, int nparams);
 
 /* Philox4x32-10 block (for known-answer tests of the device generator) */
 int mcig_philox_block(int device, const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

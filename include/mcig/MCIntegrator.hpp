@@ -82,9 +82,17 @@ inline void check(int rc)
 inline const double *ptr(const std::vector<double> &v) { return v.empty() ? nullptr : v.data(); }
 } // namespace detail
 
-// user sampling functions and observables compiled for the device (mcig/plugin.cuh): the
-// loaded library; its k-th functors are pdf(k, params) and obs(k, params).  It must outlive
-// every MCI that uses it.
+// a trial move of a plugin (TrialMoveInterface as a device struct): its index in the
+// plugin's move list and the parameters handed to it
+struct UserMove
+{
+    int k;
+    std::vector<double> params;
+};
+
+// user sampling functions, observables and trial moves compiled for the device
+// (mcig/plugin.cuh): the loaded library; its k-th functors are pdf(k, params), obs(k, params)
+// and move(k, params).  It must outlive every MCI that uses it.
 class Plugin
 {
 private:
@@ -98,6 +106,7 @@ public:
     const mcig_plugin *handle() const { return _p; }
     static SamplingFunction pdf(int k, std::vector<double> params = {}) { return {MCIG_PDF_USER + k, std::move(params)}; }
     static Observable obs(int k, std::vector<double> params = {}) { return {MCIG_OBS_USER + k, std::move(params)}; }
+    static UserMove move(int k, std::vector<double> params = {}) { return {k, std::move(params)}; }
 };
 
 class MCI
@@ -170,6 +179,8 @@ public:
 
     // --- trial moves
     void setTrialMove(MoveType m) { detail::check(mcig_set_trial_move(_h, static_cast<int>(m), MCIG_SRRD_UNIFORM, 1, 1, nullptr)); }
+    // MCI::setTrialMove(std::unique_ptr<TrialMoveInterface>): a plugin's move (setPlugin first)
+    void setTrialMove(const UserMove &m) { detail::check(mcig_set_user_move(_h, m.k, detail::ptr(m.params), (int)m.params.size())); }
     void setTrialMove(SRRDType srrd, int veclen = 0, int ntypes = 1, int typeEnds[] = nullptr)
     {
         detail::check(mcig_set_trial_move(_h, veclen > 0 ? MCIG_MOVE_VEC : MCIG_MOVE_ALL, static_cast<int>(srrd),

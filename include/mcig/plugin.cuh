@@ -27,6 +27,26 @@
 //   using MyObss = mcig::ObsList<MyObs>;
 //   MCIG_PLUGIN(MyPdfs, MyObss)
 //
+// With user trial moves (TrialMoveInterface, include/mci/TrialMoveInterface.hpp:18-75):
+//
+//   struct MyGaussMove {                                 // x' = x + s z, z ~ N(0, I), one step size
+//       static int nstep(const mcig::UserArgs &) { return 1; }
+//       static double step0(const mcig::UserArgs &, int) { return 0.05; }
+//       static int step_index(const mcig::UserArgs &, int) { return 0; }
+//       static double change_rate(const mcig::UserArgs &) { return 1.; }
+//       template <class R>
+//       __device__ static R trialMove(const mcig::UserArgs &a, mcig::UserMoveWalker<R> &w, const R *steps,
+//                                     mcig::UserRng<R> &rng, const R *, R *)
+//       {
+//           for (int i = 0; i < a.ndim; ++i) { w.xnew[i] = w.xold[i] + steps[0] * rng.normal(); }
+//           w.nchanged = a.ndim;
+//           return (R)1;                                 // symmetric move
+//       }
+//   };
+//   MCIG_PLUGIN_MOVES(MyPdfs, MyObss, mcig::MoveList<MyGaussMove>)
+//
+// and mcig_set_user_move(handle, k, params, nparams) installs the k-th move.
+//
 // Build (mcintegratorplusplus_gb300.build.build_plugin does this): the source compiled twice,
 // once with -DMCIG_PLUGIN_PART=1 -fmad=false (double path, the reference's operation order)
 // and once with -DMCIG_PLUGIN_PART=2 (float path), both objects linked with -shared; one
@@ -77,6 +97,27 @@ int launch(const KParams &p, int movetype, int grid, int block, size_t smem, cud
         return (n < 0 || n > TABLE::max_nproto) ? -1 : n;                                                         \
     }                                                                                                             \
     extern "C" int mcig_plugin_obs_nvals(int k, int ndim) { return TABLE::nvals(k, ndim); }                      \
+    extern "C" int mcig_plugin_nmove(void) { return TABLE::nmove; }                                               \
+    extern "C" int mcig_plugin_move_info(int k, int ndim, const double *params, int nparams, int *nproto,         \
+                                         int *nstep, double *change_rate)                                         \
+    {                                                                                                             \
+        if (k < 0 || k >= TABLE::nmove) { return -1; }                                                           \
+        const mcig::UserArgs a{ndim, params, nparams};                                                            \
+        const int np = TABLE::move_nproto(k, ndim);                                                               \
+        *nproto = (np < 0 || np > TABLE::move_max_nproto) ? -1 : np;                                              \
+        *nstep = TABLE::move_nstep(k, a);                                                                         \
+        *change_rate = TABLE::move_change_rate(k, a);                                                             \
+        return 0;                                                                                                 \
+    }                                                                                                             \
+    extern "C" int mcig_plugin_move_steps(int k, int ndim, const double *params, int nparams, int nstep,          \
+                                          double *step0, int *stepidx)                                            \
+    {                                                                                                             \
+        if (k < 0 || k >= TABLE::nmove) { return -1; }                                                           \
+        const mcig::UserArgs a{ndim, params, nparams};                                                            \
+        for (int t = 0; t < nstep; ++t) { step0[t] = TABLE::move_step0(k, a, t); }                                \
+        for (int i = 0; i < ndim; ++i) { stepidx[i] = TABLE::move_step_index(k, a, i); }                          \
+        return 0;                                                                                                 \
+    }                                                                                                             \
     extern "C" mcig_plugin_launch_fn mcig_plugin_launcher_f32(int precision);                                     \
     extern "C" mcig_plugin_launch_fn mcig_plugin_launcher(int precision, int rng)                                 \
     {                                                                                                             \
@@ -88,18 +129,19 @@ int launch(const KParams &p, int movetype, int grid, int block, size_t smem, cud
     }
 
 #if !defined(MCIG_PLUGIN_PART)
-#define MCIG_PLUGIN(PDFS, OBSS)                                                                                   \
-    using mcig_plugin_table_ = mcig::UserTable<PDFS, OBSS>;                                                       \
+#define MCIG_PLUGIN_MOVES(PDFS, OBSS, MOVES)                                                                      \
+    using mcig_plugin_table_ = mcig::UserTable<PDFS, OBSS, MOVES>;                                                \
     MCIG_PLUGIN_MAIN_(mcig_plugin_table_)                                                                         \
     MCIG_PLUGIN_F32_(mcig_plugin_table_)
 #elif MCIG_PLUGIN_PART == 1
-#define MCIG_PLUGIN(PDFS, OBSS)                                                                                   \
-    using mcig_plugin_table_ = mcig::UserTable<PDFS, OBSS>;                                                       \
+#define MCIG_PLUGIN_MOVES(PDFS, OBSS, MOVES)                                                                      \
+    using mcig_plugin_table_ = mcig::UserTable<PDFS, OBSS, MOVES>;                                                \
     MCIG_PLUGIN_MAIN_(mcig_plugin_table_)
 #else
-#define MCIG_PLUGIN(PDFS, OBSS)                                                                                   \
-    using mcig_plugin_table_ = mcig::UserTable<PDFS, OBSS>;                                                       \
+#define MCIG_PLUGIN_MOVES(PDFS, OBSS, MOVES)                                                                      \
+    using mcig_plugin_table_ = mcig::UserTable<PDFS, OBSS, MOVES>;                                                \
     MCIG_PLUGIN_F32_(mcig_plugin_table_)
 #endif
+#define MCIG_PLUGIN(PDFS, OBSS) MCIG_PLUGIN_MOVES(PDFS, OBSS, mcig::MoveList<>)
 
 #endif

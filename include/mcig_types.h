@@ -32,8 +32,9 @@ enum mcig_status {
     MCIG_ERR_TIMEOUT = 6           /* a bounded device wait ran out */
 };
 
-/* MoveType (Factories.hpp:104-109) */
-enum mcig_move_type { MCIG_MOVE_ALL = 0, MCIG_MOVE_VEC = 1, MCIG_MOVE_MULTISTEP = 2 };
+/* MoveType (Factories.hpp:104-109); MCIG_MOVE_USER: a trial move of the attached plugin
+ * (mcig_set_user_move), the reference's setTrialMove(std::unique_ptr<TrialMoveInterface>) */
+enum mcig_move_type { MCIG_MOVE_ALL = 0, MCIG_MOVE_VEC = 1, MCIG_MOVE_MULTISTEP = 2, MCIG_MOVE_USER = 3 };
 
 /* SRRDType (Factories.hpp:115-128) */
 enum mcig_srrd {

@@ -107,6 +107,8 @@ SIGNATURES = {
     "mcig_plugin_unload": (c_int, [c_void_p]),
     "mcig_plugin_counts": (c_int, [c_void_p, P_int, P_int]),
     "mcig_set_plugin": (c_int, [c_void_p, c_void_p]),
+    "mcig_plugin_nmoves": (c_int, [c_void_p, P_int]),
+    "mcig_set_user_move": (c_int, [c_void_p, c_int, P_double, c_int]),
 }
 
 

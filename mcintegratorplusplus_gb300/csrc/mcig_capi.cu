@@ -95,10 +95,13 @@ struct ObsDef {
 // a loaded plugin (include/mcig/plugin.cuh): its user functors and its general kernel
 struct mcig_plugin {
     void *dl = nullptr;
-    int npdf = 0, nobs = 0;
+    int npdf = 0, nobs = 0, nmove = 0;
     int (*pdf_nproto)(int, int) = nullptr;
     int (*obs_nvals)(int, int) = nullptr;
     mcig_plugin_launch_fn (*launcher)(int, int) = nullptr;
+    // trial moves (optional exports of MCIG_PLUGIN_MOVES)
+    int (*move_info)(int, int, const double *, int, int *, int *, double *) = nullptr;
+    int (*move_steps)(int, int, const double *, int, int, double *, int *) = nullptr;
 };
 
 #define MCIG_MAX_CHUNKS 8
@@ -115,6 +118,11 @@ struct mcig_mci {
     int movetype = MCIG_MOVE_ALL, srrd = MCIG_SRRD_UNIFORM, veclen = 0, ntypes = 1;
     int typeEnds[MCIG_MAXTYPES] = {0, 0, 0, 0};
     int ms_nsteps = 0, ms_srrd = 0, ms_veclen = 1;
+    // user trial move (MCIG_MOVE_USER): plugin move index, parameters, proto values, the step
+    // size index of every coordinate (getStepSizeIndex)
+    int umove = 0, umove_nproto = 0;
+    std::vector<double> umove_params;
+    std::vector<int> umove_stepidx;
     std::vector<PdfDef> ms_pdfs, pdfs;
     std::vector<ObsDef> obs;
     int periodic = 0;
@@ -295,7 +303,7 @@ static bool uses_plugin(const mcig_mci *h)
     for (auto &o : h->obs) {
         if (is_user_obs(o.kind)) { return true; }
     }
-    return false;
+    return h->movetype == MCIG_MOVE_USER;
 }
 
 // what the plugin kernel does not serve
@@ -406,6 +414,10 @@ extern "C" int mcig_plugin_load(const char *path, mcig_plugin **out)
     }
     pl->npdf = npdf();
     pl->nobs = nobs();
+    auto nmove = (int (*)(void))sym("mcig_plugin_nmove");
+    pl->move_info = (int (*)(int, int, const double *, int, int *, int *, double *))sym("mcig_plugin_move_info");
+    pl->move_steps = (int (*)(int, int, const double *, int, int, double *, int *))sym("mcig_plugin_move_steps");
+    pl->nmove = (nmove && pl->move_info && pl->move_steps) ? nmove() : 0;
     if (pl->npdf > MCIG_MAXUSER || pl->nobs > MCIG_MAXUSER) {
         delete pl;
         dlclose(dl);
@@ -429,6 +441,13 @@ extern "C" int mcig_plugin_counts(const mcig_plugin *pl, int *npdf, int *nobs)
     if (!pl) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin is NULL"); }
     if (npdf) { *npdf = pl->npdf; }
     if (nobs) { *nobs = pl->nobs; }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_plugin_nmoves(const mcig_plugin *pl, int *nmove)
+{
+    if (!pl || !nmove) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "plugin or nmove is NULL"); }
+    *nmove = pl->nmove;
     return MCIG_OK;
 }
 
@@ -644,6 +663,46 @@ extern "C" int mcig_set_trial_move(mcig_mci *h, int movetype, int srrd, int vecl
     for (int i = 0; i < MCIG_MAXTYPES; ++i) { h->typeEnds[i] = (ntypes > 1 && i < ntypes) ? typeEnds[i] : h->ndim; }
     cudaSetDevice(h->device);
     return fill_steps(h, 0.05);
+}
+
+extern "C" int mcig_set_user_move(mcig_mci *h, int k, const double *params, int nparams)
+{
+    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
+    if (!h->plugin) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "a user trial move needs a plugin: the handle has no plugin"); }
+    if (k < 0 || k >= h->plugin->nmove) {
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "the plugin has %d trial moves, not a move %d", h->plugin->nmove, k);
+    }
+    if (nparams < 0 || (nparams > 0 && !params)) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "move parameters"); }
+    const std::vector<double> par(params, params + nparams);
+    int nproto = 0, nstep = 0;
+    double rate = 0.;
+    if (h->plugin->move_info(k, h->ndim, par.data(), nparams, &nproto, &nstep, &rate) != 0 || nproto < 0) {
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "trial move %d: nproto(%d) is above its max_nproto", k, h->ndim);
+    }
+    if (nstep < 0 || nstep > MCIG_MAXTYPES) {
+        return set_err(MCIG_ERR_UNSUPPORTED, "trial move %d has %d step sizes; at most %d on the device", k, nstep, MCIG_MAXTYPES);
+    }
+    std::vector<double> s0(std::max(nstep, 1), 0.);
+    std::vector<int> idx(h->ndim, 0);
+    h->plugin->move_steps(k, h->ndim, par.data(), nparams, nstep, s0.data(), idx.data());
+    for (int i = 0; i < h->ndim && nstep > 0; ++i) {
+        if (idx[i] < 0 || idx[i] >= nstep) {
+            return set_err(MCIG_ERR_INVALID_ARGUMENT, "trial move %d: step size index %d of coordinate %d is not in [0, %d)", k, idx[i], i, nstep);
+        }
+    }
+    h->movetype = MCIG_MOVE_USER;
+    h->umove = k;
+    h->umove_nproto = nproto;
+    h->umove_params = par;
+    h->umove_stepidx = idx;
+    h->ms_pdfs.clear();
+    h->ntypes = nstep;
+    for (int i = 0; i < MCIG_MAXTYPES; ++i) { h->typeEnds[i] = h->ndim; }
+    cudaSetDevice(h->device);
+    if (nstep == 0) { return MCIG_OK; }
+    int rc = fill_steps(h, s0[0]);
+    for (int t = 1; t < nstep && rc == MCIG_OK; ++t) { rc = mcig_set_mrt2step_i(h, t, s0[t]); }
+    return rc;
 }
 
 extern "C" int mcig_multistep_add_pdf(mcig_mci *h, int kind, const double *params, int nparams)
@@ -945,6 +1004,25 @@ static int fill_common(mcig_mci *h, KParams &kp)
     std::vector<double> P;
     std::vector<float> F;
     int rc;
+    if (h->movetype == MCIG_MOVE_USER) {
+        kp.umove = h->umove;
+        kp.umove_nproto = h->umove_nproto;
+        kp.umove_poff = (int)P.size();
+        kp.umove_np = (int)h->umove_params.size();
+        P.insert(P.end(), h->umove_params.begin(), h->umove_params.end());
+        // findMRT2Step's clamp (MCIntegrator.cpp:146-151): step size t at most 0.5 * the domain
+        // size of every coordinate i with getStepSizeIndex(i) == t
+        kp.step_lim_off = (int)P.size();
+        for (int t = 0; t < std::max(h->ntypes, 1); ++t) {
+            double lim = 0.5 * (2. * (double)3.4028234663852886e+38);
+            for (int i = 0; i < h->ndim; ++i) {
+                if (h->umove_stepidx[i] != t) { continue; }
+                const double li = h->periodic ? 0.5 * (h->ub[i] - h->lb[i]) : 0.5 * (2. * (double)3.4028234663852886e+38);
+                lim = std::min(lim, li);
+            }
+            P.push_back(lim);
+        }
+    }
     kp.npdf = (int)h->pdfs.size();
     for (int k = 0; k < kp.npdf; ++k) {
         if ((rc = build_pdf_desc(h, h->pdfs[k], P, F, kp.pdf[k]))) { return rc; }
@@ -1899,7 +1977,8 @@ extern "C" int mcig_integrate(mcig_mci *h, int64_t nmc, double *average, double 
     // the three phases in one launch of the register-resident kernel, where that kernel
     // serves each of them (fixed burn-in, no file output): every chain runs
     // findMRT2Step, initialDecorrelation and sample one after the other on its own
-    const bool calib = !h->pdfs.empty() && do_find && h->nfind != 0;
+    // MCI::findMRT2Step returns at once for a move without step sizes (MCIntegrator.cpp:94)
+    const bool calib = !h->pdfs.empty() && do_find && h->nfind != 0 && nstepsizes(h) > 0;
     const bool burnin = !h->pdfs.empty() && do_decorr && h->ndecorr > 0;
     const int64_t lim = (int64_t)1 << 31;
     const bool fuse = h->fuse_phases && nmc > 0 && nmc < lim && h->ndecorr < lim && dump.empty() && !h->record &&

@@ -78,6 +78,11 @@ struct KParams {
     int typeEnds[MCIG_MAXTYPES];
     int ms_nsteps, ms_srrd, ms_veclen, ms_npdf;
     PdfDesc ms_pdf[MCIG_MAXPDF];
+    // user trial move (MCIG_MOVE_USER): index in the plugin's move list, its parameters at
+    // params[umove_poff .. + umove_np), its proto values, and the upper limit of each step
+    // size at params[step_lim_off + t] (the smallest 0.5 * domain size over the coordinates
+    // that step size t moves)
+    int umove, umove_poff, umove_np, umove_nproto, step_lim_off;
     // sampling functions
     int npdf;
     PdfDesc pdf[MCIG_MAXPDF];

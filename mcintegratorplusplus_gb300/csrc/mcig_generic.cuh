@@ -329,15 +329,26 @@ template <class R, int CAP, int PCAP, bool ON> struct UserProtoStore {
 template <class R, int CAP, int PCAP> struct UserProtoStore<R, CAP, PCAP, false> {
     static constexpr R *upo = nullptr, *upn = nullptr, *mpo = nullptr, *mpn = nullptr, *uprep = nullptr;
 };
+// a user trial move's protoold / protonew and the changed indices it reports
+template <class R, int CAP, bool ON> struct UserMoveStore {
+    R vpo[CAP], vpn[CAP];
+    int chidx[MCIG_MAXDIM];
+};
+template <class R, int CAP> struct UserMoveStore<R, CAP, false> {
+    static constexpr R *vpo = nullptr, *vpn = nullptr;
+    static constexpr int *chidx = nullptr;
+};
 
 // U: the plugin's functor lists (mcig_plugin.cuh); mcig::NoPlugin for the built-in kernels
 template <class R, int RNG, bool KAHAN, class U = mcig::NoPlugin>
-struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXPDF * U::max_nprep, (U::npdf > 0)> {
+struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXPDF * U::max_nprep, (U::npdf > 0)>,
+                        UserMoveStore<R, U::move_max_nproto, (U::nmove > 0)> {
     static constexpr bool EXACT = std::is_same<R, double>::value;
     static constexpr int NV = 2 * MCIG_MAXDIM + 8;
     using AccV = typename std::conditional<KAHAN, float, double>::type;
     static constexpr bool USER_PDF = U::npdf > 0;
     static constexpr bool USER_OBS = U::nobs > 0;
+    static constexpr bool USER_MOVE = U::nmove > 0;
     static constexpr int MP = U::max_nproto; // proto values per plugin pdf
 
     const KParams &p;
@@ -418,9 +429,11 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXP
         for (int j = 0; j < d.nproto; ++j) { pn[j] = po[j]; }
     }
     // SamplingFunctionInterface::computeAcceptance of a plugin sampling function: updates pn
-    __device__ R user_accept(const PdfDesc &d, const R *xo, const R *xnew, bool partial, int lo, int hi, const R *po, R *pn)
+    // idx: the changed indices of a user trial move (nchanged of them), else NULL and [lo, hi)
+    __device__ R user_accept(const PdfDesc &d, const R *xo, const R *xnew, bool partial, int lo, int hi, const R *po, R *pn,
+                             const int *idx = nullptr, int nchanged = 0)
     {
-        const mcig::UserWalker<R> w{xo, xnew, hi - lo, lo};
+        const mcig::UserWalker<R> w{xo, xnew, idx ? nchanged : hi - lo, lo, idx};
         return U::accept(d.kind - MCIG_PDF_USER, uargs(d.poff, d.np), w, partial, po, pn);
     }
     // newToOld (src, dst) = (pn, po) on acceptance, oldToNew = (po, pn) on rejection
@@ -443,6 +456,49 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXP
             if (user_pdf(p.pdf[k])) { user_init(p.pdf[k], x, this->upo + k * MP, this->upn + k * MP); }
             else { lp[k] = pdf_state(p.pdf[k], x); }
         }
+        if constexpr (USER_MOVE) { // _trialMove->initializeProtoValues(xold) (MCIntegrator.cpp:261)
+            if (p.umove_nproto > 0) {
+                U::move_proto(p.umove, uargs(p.umove_poff, p.umove_np), (const R *)x, this->vpo);
+                copy_protos(this->vpo, this->vpn, p.umove_nproto);
+            }
+        }
+    }
+
+    // TrialMoveInterface::computeTrialMove of a plugin move: xn = the proposal (xn == x on
+    // entry); returns the move's acceptance factor (double) or its log (float); nch and the
+    // changed indices in chidx, lo/hi their hull
+    template <bool ON = USER_MOVE> __device__ R user_move(int &nch, int &lo, int &hi)
+    {
+        for (int i = 0; i < p.ndim; ++i) { xn[i] = x[i]; }
+        mcig::UserMoveWalker<R> mw{p.ndim, x, xn, p.ndim, this->chidx};
+        mcig::UserRng<R> rng;
+        rng.blk = 0;
+        rng.iblk = 0;
+        rng.nw = 0;
+        rng.has_spare = false;
+        rng.ncache = 0;
+        rng.cache_srrd = -1;
+        rng.spare = (R)0;
+        rng.tape = nullptr;
+        rng.tpos = &tpos;
+        rng.tlen = tlen;
+        rng.err = &tape_err;
+        if constexpr (RNG == RNG_TAPE) { rng.tape = tape; }
+        else { rng.ph = ph; }
+        const R a = U::move(p.umove, uargs(p.umove_poff, p.umove_np), mw, st, rng, this->vpo, this->vpn);
+        nch = mw.nchanged < 0 ? 0 : (mw.nchanged > p.ndim ? p.ndim : mw.nchanged);
+        if (nch >= p.ndim) {
+            lo = 0;
+            hi = p.ndim;
+        } else if (nch == 0) {
+            lo = 0;
+            hi = 0;
+        } else {
+            lo = this->chidx[0];
+            hi = this->chidx[nch - 1] + 1;
+        }
+        if constexpr (EXACT) { return a; }
+        else { return logf(a); }
     }
 
     // draw j of the move group (substep, TAG_MOVE): coordinate-indexed for Philox
@@ -606,17 +662,29 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXP
         R moveAcc = EXACT ? (R)1 : (R)0;
         bool partial = false;
         int lo = 0, hi = p.ndim;
+        const int *uidx = nullptr; // the changed indices of a user move with nchanged < ndim
+        int nch = 0;
         if (movetype == MCIG_MOVE_ALL) {
             all_move(p.srrd);
         } else if (movetype == MCIG_MOVE_VEC) {
             lo = vec_move(x, 0, p.srrd, p.veclen);
             hi = lo + p.veclen;
             partial = p.veclen < p.ndim;
+        } else if (movetype == MCIG_MOVE_USER) {
+            if constexpr (USER_MOVE) {
+                moveAcc = user_move(nch, lo, hi);
+                partial = nch < p.ndim;
+                if (partial) { uidx = this->chidx; }
+            }
         } else {
             moveAcc = multistep();
         }
-        if (p.periodic) {
-            for (int i = lo; i < hi; ++i) { periodic_wrap(xn[i], p.lb[i], p.ub[i]); }
+        if (p.periodic) { // applyDomain on the changed indices (xn == x elsewhere in [lo, hi))
+            if (uidx) {
+                for (int j = 0; j < nch; ++j) { periodic_wrap(xn[uidx[j]], p.lb[uidx[j]], p.ub[uidx[j]]); }
+            } else {
+                for (int i = lo; i < hi; ++i) { periodic_wrap(xn[i], p.lb[i], p.ub[i]); }
+            }
         }
         R lpn[MCIG_MAXPDF];
         bool acc;
@@ -624,8 +692,11 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXP
             double a = 1.;
             for (int k = 0; k < p.npdf; ++k) {
                 double pn = lp[k];
-                if (user_pdf(p.pdf[k])) { a *= user_accept(p.pdf[k], x, xn, partial, lo, hi, this->upo + k * MP, this->upn + k * MP); }
-                else { a *= pdf_accept_d(p, p.pdf[k], x, xn, partial, lo, hi, lp[k], pn); }
+                if (user_pdf(p.pdf[k])) {
+                    a *= user_accept(p.pdf[k], x, xn, partial, lo, hi, this->upo + k * MP, this->upn + k * MP, uidx, nch);
+                } else {
+                    a *= pdf_accept_d(p, p.pdf[k], x, xn, partial, lo, hi, lp[k], pn);
+                }
                 lpn[k] = pn;
             }
             acc = (accept_u(0) <= a * moveAcc);
@@ -634,7 +705,7 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXP
             for (int k = 0; k < p.npdf; ++k) {
                 if (user_pdf(p.pdf[k])) {
                     lpn[k] = lp[k];
-                    dl += logf(user_accept(p.pdf[k], x, xn, partial, lo, hi, this->upo + k * MP, this->upn + k * MP));
+                    dl += logf(user_accept(p.pdf[k], x, xn, partial, lo, hi, this->upo + k * MP, this->upn + k * MP, uidx, nch));
                     continue;
                 }
                 lpn[k] = pdf_logp_f(p, p.pdf[k], xn, blob);
@@ -651,6 +722,12 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXP
                 if (!user_pdf(p.pdf[k])) { continue; }
                 if (acc) { copy_protos(this->upn + k * MP, this->upo + k * MP, p.pdf[k].nproto); }
                 else { copy_protos(this->upo + k * MP, this->upn + k * MP, p.pdf[k].nproto); }
+            }
+        }
+        if constexpr (USER_MOVE) { // _trialMove->newToOld() / oldToNew()
+            if (movetype == MCIG_MOVE_USER && p.umove_nproto > 0) {
+                if (acc) { copy_protos(this->vpn, this->vpo, p.umove_nproto); }
+                else { copy_protos(this->vpo, this->vpn, p.umove_nproto); }
             }
         }
         end_step();
@@ -831,11 +908,18 @@ struct GenericSampler : UserProtoStore<R, MCIG_MAXPDF * U::max_nproto, MCIG_MAXP
             f = (f < 2.) ? f : 2.;
             double sd[MCIG_MAXTYPES];
             for (int t = 0; t < p.ntypes; ++t) { sd[t] = (double)st[t] * f; } // scaleStepSizes
-            for (int i = 0; i < p.ndim; ++i) {
-                int t = 0;
-                while (t + 1 < p.ntypes && i >= p.typeEnds[t]) { ++t; }
-                const double lim = p.step_max_i ? p.step_max_i[i] : p.step_max;
-                if (sd[t] > lim) { sd[t] = lim; }
+            if (movetype == MCIG_MOVE_USER) { // the move's getStepSizeIndex, folded into a limit per step size
+                for (int t = 0; t < p.ntypes; ++t) {
+                    const double lim = p.params[p.step_lim_off + t];
+                    if (sd[t] > lim) { sd[t] = lim; }
+                }
+            } else {
+                for (int i = 0; i < p.ndim; ++i) {
+                    int t = 0;
+                    while (t + 1 < p.ntypes && i >= p.typeEnds[t]) { ++t; }
+                    const double lim = p.step_max_i ? p.step_max_i[i] : p.step_max;
+                    if (sd[t] > lim) { sd[t] = lim; }
+                }
             }
             for (int t = 0; t < p.ntypes; ++t) {
                 if (sd[t] < SMALLEST) { sd[t] = SMALLEST; }

@@ -36,46 +36,78 @@
 
 #include "mcig_calib.cuh"
 
-// log of the mixture density in double (the reference formula of the double kernels'
-// pdf_proto_scalar_d and of the oracle): pp = [nc, w[nc], m[nc][nd], s[nc][nd], lc[nc]]
-__device__ __noinline__ double lanes_mix_logp_d(const double *pp, int nd, int nc, const double *xd)
-{
-    const double *m = pp + 1 + nc, *sg = pp + 1 + nc + nc * nd, *lc = pp + 1 + nc + 2 * nc * nd;
-    double e[16];
-    double mx = -INFINITY;
-    for (int q = 0; q < nc; ++q) {
-        double a = lc[q];
-        for (int i = 0; i < nd; ++i) {
-            const double z = (xd[i] - m[q * nd + i]) / sg[q * nd + i];
-            a += -0.5 * (z * z);
-        }
-        e[q] = a;
-        mx = a > mx ? a : mx;
-    }
-    double sum = 0.;
-    for (int q = 0; q < nc; ++q) { sum += exp(e[q] - mx); }
-    return mx + log(sum);
-}
-
 // own coordinates of a lane, passed by value to the out-of-line double decision
 template <int CPL> struct LaneVec { float v[CPL]; };
 
 // The Metropolis decision in double for the chain of this lane (every lane of the warp
 // calls it: the walker and the proposal are gathered with shuffles): log(u) <= log p(x') -
-// log p(x) at the float positions x (own part xo) and x' (own part xno).  Out of line, so
-// that the rare double path takes no registers from the sampling loop.
+// log p(x) at the float positions x (own part xo) and x' (own part xno), log p in double by
+// the reference formula of the double kernels' pdf_proto_scalar_d and of the oracle, with
+// pp = [nc, w[nc], m[nc][nd], s[nc][nd], lc[nc]]:
+//   e_q = lc_q + sum_i -0.5 ((x_i - m_qi) / s_qi)^2 (ascending i), M = max_q e_q,
+//   log p = M + log(sum_q exp(e_q - M)) (ascending q).
+// The chain's LPC lanes share it as the float path shares the float mixture: lane group l
+// evaluates components l, l + LPC, ..., the maximum is a butterfly over the chain's lanes
+// (exact), and every lane sums the gathered terms in component order, so each lane computes
+// nc / LPC components instead of all of them, with the same result bit for bit.  Out of
+// line, so that the rare double path takes no registers from the sampling loop.
 template <int MAXD, int LPC>
-__device__ __noinline__ bool lanes_decide_d(const double *pp, int nd, int nc, int k, float u, LaneVec<MAXD / LPC> xo,
-                                            LaneVec<MAXD / LPC> xno)
+__device__ __noinline__ bool lanes_decide_d(const double *pp, int nd, int nc, int l, int k, float u,
+                                            LaneVec<MAXD / LPC> xo, LaneVec<MAXD / LPC> xno)
 {
-    constexpr int CPL = MAXD / LPC, G = 32 / LPC;
+    constexpr int CPL = MAXD / LPC, G = 32 / LPC, CPP = 8 / LPC;
+    constexpr unsigned FULL = 0xffffffffu;
     double xd[MAXD], xnd[MAXD];
 #pragma unroll
     for (int i = 0; i < MAXD; ++i) {
-        xd[i] = (double)__shfl_sync(0xffffffffu, xo.v[i % CPL], (i / CPL) * G + k);
-        xnd[i] = (double)__shfl_sync(0xffffffffu, xno.v[i % CPL], (i / CPL) * G + k);
+        xd[i] = (double)__shfl_sync(FULL, xo.v[i % CPL], (i / CPL) * G + k);
+        xnd[i] = (double)__shfl_sync(FULL, xno.v[i % CPL], (i / CPL) * G + k);
     }
-    return log((double)u) <= lanes_mix_logp_d(pp, nd, nc, xnd) - lanes_mix_logp_d(pp, nd, nc, xd);
+    const double *m = pp + 1 + nc, *sg = pp + 1 + nc + nc * nd, *lc = pp + 1 + nc + 2 * nc * nd;
+    double eo[CPP], en[CPP];
+    double mo = -INFINITY, mn = -INFINITY;
+#pragma unroll
+    for (int r = 0; r < CPP; ++r) {
+        const int q = l + LPC * r;
+        double a = -INFINITY, b = -INFINITY;
+        if (q < nc) {
+            a = lc[q];
+            b = lc[q];
+            for (int i = 0; i < nd; ++i) {
+                const double zo = (xd[i] - m[q * nd + i]) / sg[q * nd + i];
+                a += -0.5 * (zo * zo);
+                const double zn = (xnd[i] - m[q * nd + i]) / sg[q * nd + i];
+                b += -0.5 * (zn * zn);
+            }
+        }
+        eo[r] = a;
+        en[r] = b;
+        mo = a > mo ? a : mo;
+        mn = b > mn ? b : mn;
+    }
+#pragma unroll
+    for (int s = G; s < 32; s <<= 1) {
+        const double oo = __shfl_xor_sync(FULL, mo, s), on = __shfl_xor_sync(FULL, mn, s);
+        mo = oo > mo ? oo : mo;
+        mn = on > mn ? on : mn;
+    }
+    double to[CPP], tn[CPP];
+#pragma unroll
+    for (int r = 0; r < CPP; ++r) {
+        to[r] = (l + LPC * r < nc) ? exp(eo[r] - mo) : 0.;
+        tn[r] = (l + LPC * r < nc) ? exp(en[r] - mn) : 0.;
+    }
+    double so = 0., sn = 0.;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) { // component q sits in lane group q % LPC, slot q / LPC
+        const double a = __shfl_sync(FULL, to[q / LPC], (q % LPC) * G + k);
+        const double b = __shfl_sync(FULL, tn[q / LPC], (q % LPC) * G + k);
+        if (q < nc) {
+            so += a;
+            sn += b;
+        }
+    }
+    return log((double)u) <= (mn + log(sn)) - (mo + log(so));
 }
 
 template <int MAXD, int LPC, bool KAHAN>
@@ -211,7 +243,7 @@ struct LaneMixSampler {
                     xo.v[m] = x[m];
                     xno.v[m] = xn[m];
                 }
-                const bool a64 = lanes_decide_d<MAXD, LPC>(p.params + p.pdf[0].poff, p.ndim, nc, k, u, xo, xno);
+                const bool a64 = lanes_decide_d<MAXD, LPC>(p.params + p.pdf[0].poff, p.ndim, nc, l, k, u, xo, xno);
                 if (near) {
                     if (p.dstats && l == 0) {
                         atomicAdd(p.dstats, 1ull);

@@ -187,6 +187,12 @@ class MCI:
             te = (ctypes.c_int * len(typeEnds))(*[int(v) for v in typeEnds])
         _raise(self.L.mcig_set_trial_move(self._h, int(movetype), int(srrd), int(veclen), int(ntypes), te))
 
+    def setUserMove(self, k, params=None):
+        """The attached plugin's k-th trial move as this MCI's move (MCI::setTrialMove with a
+        TrialMoveInterface object); params are handed to the move."""
+        p, n = _params(params)
+        _raise(self.L.mcig_set_user_move(self._h, int(k), _dp(p), n))
+
     def setMultiStepMove(self, nsteps, sub_srrd=SRRD_UNIFORM, sub_veclen=1, sub_step=0.05):
         _raise(self.L.mcig_set_multistep_move(self._h, int(nsteps), int(sub_srrd), int(sub_veclen), float(sub_step)))
 
@@ -468,6 +474,9 @@ class Plugin:
         npdf, nobs = ctypes.c_int(), ctypes.c_int()
         _raise(self.L.mcig_plugin_counts(self._h, ctypes.byref(npdf), ctypes.byref(nobs)))
         self.npdf, self.nobs = npdf.value, nobs.value
+        nmove = ctypes.c_int()
+        _raise(self.L.mcig_plugin_nmoves(self._h, ctypes.byref(nmove)))
+        self.nmove = nmove.value
 
     def pdf(self, k):
         """kind of the k-th sampling function"""

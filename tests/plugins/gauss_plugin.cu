@@ -1,7 +1,8 @@
 // Test plugin: user functors written the way a user of the reference writes
-// SamplingFunctionInterface / ObservableFunctionInterface classes, with the arithmetic of the
-// reference's test classes (test/common/TestMCIFunctions.hpp), so that integrals with them equal
-// integrals with the built-in kinds bit for bit.
+// SamplingFunctionInterface / ObservableFunctionInterface / TrialMoveInterface classes, with
+// the arithmetic of the reference's test classes (test/common/TestMCIFunctions.hpp) and
+// built-in moves, so that integrals with them equal integrals with the built-in kinds bit
+// for bit.
 #include <mcig/plugin.cuh>
 
 // exp(-sum_i x_i^2) with one proto value per index (Gauss, TestMCIFunctions.hpp:151-190)
@@ -31,7 +32,8 @@ struct IndexGauss {
     __device__ static R updatedAcceptance(const mcig::UserArgs &, const mcig::UserWalker<R> &w, const R *po, R *pn)
     {
         R e = (R)0;
-        for (int i = w.lo; i < w.lo + w.nchanged; ++i) {
+        for (int j = 0; j < w.nchanged; ++j) {
+            const int i = w.changed(j);
             pn[i] = w.xnew[i] * w.xnew[i];
             e = e + (pn[i] - po[i]);
         }
@@ -149,6 +151,98 @@ struct SquareOfFirst {
     }
 };
 
+// Trial moves (TrialMoveInterface, include/mci/TrialMoveInterface.hpp:18-75)
+
+// x' = x + s z, z ~ N(0, I): the arithmetic and draws of SRRDAllMove with the normal
+// distribution (SRRDAllMove.hpp:67-80), one step size
+struct GaussAllMove {
+    static int nstep(const mcig::UserArgs &) { return 1; }
+    static double step0(const mcig::UserArgs &, int) { return 0.05; }
+    static int step_index(const mcig::UserArgs &, int) { return 0; }
+    static double change_rate(const mcig::UserArgs &) { return 1.; }
+    template <class R>
+    __device__ static R trialMove(const mcig::UserArgs &a, mcig::UserMoveWalker<R> &w, const R *steps,
+                                  mcig::UserRng<R> &rng, const R *, R *)
+    {
+        for (int i = 0; i < a.ndim; ++i) { w.xnew[i] = w.xold[i] + steps[0] * rng.normal(); }
+        w.nchanged = a.ndim;
+        return (R)1;
+    }
+};
+
+// one coordinate, uniform on [-s, s): SRRDVecMove with vector length 1 and the uniform
+// distribution (SRRDVecMove.hpp:75-96): index first, then the displacement
+struct SingleIndexMove {
+    static int nstep(const mcig::UserArgs &) { return 1; }
+    static double step0(const mcig::UserArgs &, int) { return 0.05; }
+    static int step_index(const mcig::UserArgs &, int) { return 0; }
+    static double change_rate(const mcig::UserArgs &a) { return 1. / a.ndim; }
+    template <class R>
+    __device__ static R trialMove(const mcig::UserArgs &a, mcig::UserMoveWalker<R> &w, const R *steps,
+                                  mcig::UserRng<R> &rng, const R *, R *)
+    {
+        const int i = rng.index(a.ndim);
+        w.xnew[i] = w.xold[i] + steps[0] * rng.draw(MCIG_SRRD_UNIFORM);
+        w.nchanged = 1;
+        w.changedIdx[0] = i;
+        return (R)1;
+    }
+};
+
+// two coordinates half the dimension apart (i and i + ndim/2 mod ndim, not adjacent), each
+// with a Gaussian displacement; the first half of the coordinates has step size 0, the
+// second half step size 1 (ndim >= 2)
+struct PairMove {
+    static int nstep(const mcig::UserArgs &) { return 2; }
+    static double step0(const mcig::UserArgs &, int t) { return t == 0 ? 0.05 : 0.1; }
+    static int step_index(const mcig::UserArgs &a, int xidx) { return xidx < a.ndim / 2 ? 0 : 1; }
+    static double change_rate(const mcig::UserArgs &a) { return 2. / a.ndim; }
+    template <class R>
+    __device__ static R trialMove(const mcig::UserArgs &a, mcig::UserMoveWalker<R> &w, const R *steps,
+                                  mcig::UserRng<R> &rng, const R *, R *)
+    {
+        const int h = a.ndim / 2;
+        const int i = rng.index(a.ndim);
+        const int j = (i + h) % a.ndim;
+        const int lo = i < j ? i : j, hi = i < j ? j : i;
+        w.xnew[lo] = w.xold[lo] + steps[lo < h ? 0 : 1] * rng.normal();
+        w.xnew[hi] = w.xold[hi] + steps[hi < h ? 0 : 1] * rng.normal();
+        w.nchanged = 2;
+        w.changedIdx[0] = lo;
+        w.changedIdx[1] = hi;
+        return (R)1;
+    }
+};
+
+// independence proposal x' ~ N(0, sigma^2 I), sigma = params[0]: not symmetric, so the move's
+// acceptance factor is q(x) / q(x') = exp(|x'|^2 / (2 sigma^2) - |x|^2 / (2 sigma^2)), with
+// the proto value |x|^2 / (2 sigma^2) kept for the old and the new position; no step sizes
+struct IndependenceMove {
+    static constexpr int max_nproto = 1;
+    static int nproto(int) { return 1; }
+    static int nstep(const mcig::UserArgs &) { return 0; }
+    static double step0(const mcig::UserArgs &, int) { return 0.; }
+    static int step_index(const mcig::UserArgs &, int) { return 0; }
+    static double change_rate(const mcig::UserArgs &) { return 1.; }
+    template <class R> __device__ static void protoFunction(const mcig::UserArgs &a, const R *x, R *pv)
+    {
+        R s = (R)0;
+        for (int i = 0; i < a.ndim; ++i) { s = s + x[i] * x[i]; }
+        pv[0] = s / (R)(2. * a.params[0] * a.params[0]);
+    }
+    template <class R>
+    __device__ static R trialMove(const mcig::UserArgs &a, mcig::UserMoveWalker<R> &w, const R *,
+                                  mcig::UserRng<R> &rng, const R *po, R *pn)
+    {
+        const R sg = (R)a.params[0];
+        for (int i = 0; i < a.ndim; ++i) { w.xnew[i] = sg * rng.normal(); }
+        w.nchanged = a.ndim;
+        protoFunction(a, (const R *)w.xnew, pn);
+        return exp(pn[0] - po[0]);
+    }
+};
+
 using TestPdfs = mcig::PdfList<IndexGauss, SumGauss, ScaledBlockGauss>;
 using TestObss = mcig::ObsList<SquaredNorm, Position, ShiftedPosition, LogPdfFromProtos, PreparedGradient, SquareOfFirst>;
-MCIG_PLUGIN(TestPdfs, TestObss)
+using TestMoves = mcig::MoveList<GaussAllMove, SingleIndexMove, PairMove, IndependenceMove>;
+MCIG_PLUGIN_MOVES(TestPdfs, TestObss, TestMoves)

@@ -409,7 +409,12 @@ def run_c3(args):
         nmcs.append(nmc)
         chains.append(nch)
     b = mcig.Batch(mcis, nmcs)
-    block, unroll = b.autotune(None)
+    if args.c3_tuning:
+        v = [int(t) for t in args.c3_tuning.split(",")]
+        b.set_tuning(v[0], v[1:5])
+        block, unroll = b.tuning()
+    else:
+        block, unroll = b.autotune(None)
     for _ in range(args.warmup):
         b.run()
     clocks = Clocks()
@@ -694,6 +699,8 @@ def main():
                     help="skip the uneven-batch (C3) figures added to the default line")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "c2_parts"])
     ap.add_argument("--integrals", type=int, default=4096)
+    ap.add_argument("--c3-tuning", default=None,
+                    help="C3 without the autotuner: 'block,u8,u16,u32,u64' (threads per block, unroll per bucket)")
     ap.add_argument("--chains4", type=int, default=16384)
     ap.add_argument("--nmc4", type=int, default=65536)
     ap.add_argument("--chains5", type=int, default=16384)

@@ -106,6 +106,10 @@ int mcig_get_decision_stats(const mcig_mci *h, int64_t *checked, int64_t *revers
  * measured slower, hence off).  No counterpart in the reference, whose MCI::sample
  * (MCIntegrator.cpp:290-321) is one loop. */
 int mcig_set_sampling_chunks(mcig_mci *h, int n);
+/* 1: a single sampling launch of the register-resident kernel forms the Uncorrelated
+ * estimates of its float Full observables itself (float window sums of x and x^2 folded into
+ * Kahan sums), so the samples are not read back; 0: the estimator kernel reads them */
+int mcig_set_fused_estimates(mcig_mci *h, int on);
 
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
  * from counter (step, c).  */
@@ -245,6 +249,14 @@ int mcig_flow_create(int ndim, int nlayers, int hidden, uint64_t seed, int devic
 int mcig_flow_destroy(mcig_flow *f);
 int mcig_flow_get_params(const mcig_flow *f, float *theta, int64_t *n);
 int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n);
+/* Self-test of the flow's 5th-generation tensor-core path (tcgen05.mma from shared-memory
+ * descriptors, accumulator in tensor memory): d[128][n] = a[128][k] b[n][k]^T with bf16
+ * inputs (raw 16-bit patterns) and f32 accumulation, one CTA.  n, k multiples of 16 in
+ * [16, 256].  MCIG_ERR_TIMEOUT when the MMA's completion was not seen within the bounded wait. */
+int mcig_flow_tc_selftest(int device, const uint16_t *a, const uint16_t *b, int n, int k, float *d);
+/* the flow's passes (proposals, densities, training's density pass) on tcgen05 (1) or on
+ * mma.sync (0); both agree with the oracle at bf16 tolerance */
+int mcig_flow_set_tensor_path(mcig_flow *f, int tc);
 /* generative direction: x = f(z) and log q(x) for z[n][ndim] (host arrays) */
 int mcig_flow_forward(mcig_flow *f, const double *z, int64_t n, double *x, double *logq);
 /* density direction: z = f^-1(x) and log q(x) */

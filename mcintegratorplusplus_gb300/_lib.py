@@ -35,6 +35,7 @@ SIGNATURES = {
     "mcig_set_calibration_split": (c_int, [c_void_p, c_int]),
     "mcig_set_lanes": (c_int, [c_void_p, c_int]),
     "mcig_set_sampling_chunks": (c_int, [c_void_p, c_int]),
+    "mcig_set_fused_estimates": (c_int, [c_void_p, c_int]),
     "mcig_set_fp64_decision": (c_int, [c_void_p, c_int]),
     "mcig_get_decision_stats": (c_int, [c_void_p, P_int64, P_int64, P_double]),
     "mcig_set_seed": (c_int, [c_void_p, ctypes.c_uint64]),
@@ -96,6 +97,8 @@ SIGNATURES = {
     "mcig_flow_destroy": (c_int, [c_void_p]),
     "mcig_flow_get_params": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float), P_int64]),
     "mcig_flow_set_params": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float), c_int64]),
+    "mcig_flow_tc_selftest": (c_int, [c_int, c_void_p, c_void_p, c_int, c_int, ctypes.POINTER(ctypes.c_float)]),
+    "mcig_flow_set_tensor_path": (c_int, [c_void_p, c_int]),
     "mcig_flow_forward": (c_int, [c_void_p, P_double, c_int64, P_double, P_double]),
     "mcig_flow_inverse": (c_int, [c_void_p, P_double, c_int64, P_double, P_double]),
     "mcig_flow_loss_grad": (c_int, [c_void_p, P_double, c_int64, P_double, ctypes.POINTER(ctypes.c_float)]),

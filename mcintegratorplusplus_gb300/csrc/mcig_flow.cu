@@ -543,6 +543,389 @@ __global__ void __launch_bounds__(FLOW_PASS_THREADS, 1) flow_pass_kernel(FlowArg
 }
 
 // ------------------------------------------------------------------------
+// 5th-generation tensor cores (tcgen05): MMA issued by one thread from shared-memory
+// operand descriptors, accumulator in tensor memory (TMEM), read back with tcgen05.ld
+// ------------------------------------------------------------------------
+// Operands are bf16, K-major (k contiguous), in the no-swizzle canonical layout: 8 x 8
+// "core matrices" (8 rows of 16 bytes, 128 contiguous bytes), element (r, k) of an R x K
+// operand at core matrix (r / 8) * (K / 8) + k / 8, byte (r % 8) * 16 + (k % 8) * 2 within it.
+// So the descriptor's leading-dimension offset (next core matrix along K) is 128 bytes and
+// its stride-dimension offset (next 8 rows) K * 16 bytes; an MMA of K = 16 covers two core
+// matrices along K, and the next one starts 256 bytes further.
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) of an R x K canonical operand
+__host__ __device__ __forceinline__ uint32_t canon_off(int r, int k, int K)
+{
+    return (uint32_t)(((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start address, leading / stride byte offsets (16-byte
+// units), descriptor version 1 (bits 46-47), no swizzle (layout type 0)
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// instruction descriptor of kind::f16: f32 accumulator (bits 4-5 = 1), A and B bf16
+// (bits 7-9 and 10-12 = 1), both K-major, N / 8 at bit 17, M / 16 at bit 24
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A * B^T for one K = 16 slice (issued by one thread)
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+                 "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+// the issuing thread's MMAs so far arrive on the mbarrier when they complete
+__device__ __forceinline__ void umma_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// wait for the completion of the mbarrier phase with parity `parity`, at most `limit`
+// polls (about 2^24 x 64 ns = 1 s): false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t limit = 1u << 24)
+{
+    for (uint32_t i = 0; i < limit; ++i) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(parity)
+                     : "memory");
+        if (done) { return true; }
+        __nanosleep(32);
+    }
+    return false;
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// shared-memory writes of the generic proxy (st.shared, cp.async) visible to the tensor core
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// TMEM allocation by one whole warp: the address is written to shared memory at dst
+__device__ __forceinline__ void tmem_alloc(uint32_t dst, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(dst), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
+}
+// 16 consecutive f32 columns of the warp's 32 TMEM lanes (lane = the thread's row)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                 "%14, %15}, [%16];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) { v[i] = __uint_as_float(r[i]); }
+}
+
+// Self-test of the path: D[128][N] = A[128][K] B[N][K]^T, one CTA of 128 threads (thread t
+// reads row t of D from TMEM lane t).  N a multiple of 16 in [16, 256], K a multiple of 16 in
+// [16, 256]; status bit 0 set when the MMA's completion was not seen within the wait limit.
+__global__ void __launch_bounds__(128, 1) flow_tc_selftest_kernel(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *D,
+                                                                   int N, int K, int *status)
+{
+    extern __shared__ __align__(128) unsigned char sm[];
+    unsigned char *As = sm, *Bs = sm + 128 * K * 2;
+    uint64_t *mbar = (uint64_t *)(Bs + N * K * 2);
+    uint32_t *tslot = (uint32_t *)(mbar + 1);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int kc = K / 8;
+    for (int i = t; i < 128 * kc; i += 128) {
+        const int r = i / kc, c = i % kc;
+        *(uint4 *)(As + canon_off(r, 8 * c, K)) = *(const uint4 *)(A + (size_t)r * K + 8 * c);
+    }
+    for (int i = t; i < N * kc; i += 128) {
+        const int r = i / kc, c = i % kc;
+        *(uint4 *)(Bs + canon_off(r, 8 * c, K)) = *(const uint4 *)(B + (size_t)r * K + 8 * c);
+    }
+    uint32_t ncols = 32;
+    while (ncols < (uint32_t)N) { ncols <<= 1; }
+    if (t == 0) { mbar_init(smem_addr(mbar), 1); }
+    if (warp == 0) { tmem_alloc(smem_addr(tslot), ncols); }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = *tslot;
+    if (t == 0) {
+        const uint32_t idesc = umma_idesc_bf16(128, N);
+        for (int ks = 0; ks < K / 16; ++ks) {
+            const uint64_t ad = umma_desc(smem_addr(As) + 256 * ks, 128, 16 * K);
+            const uint64_t bd = umma_desc(smem_addr(Bs) + 256 * ks, 128, 16 * K);
+            umma_bf16(taddr, ad, bd, idesc, ks > 0 ? 1u : 0u);
+        }
+        umma_commit(smem_addr(mbar));
+    }
+    const bool ok = mbar_wait(smem_addr(mbar), 0);
+    tc_fence_after();
+    if (ok) {
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tmem_ld16(taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) { D[(size_t)t * N + c0 + j] = v[j]; }
+        }
+    } else if (lane == 0) {
+        atomicOr(status, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) { tmem_dealloc(taddr, ncols); }
+}
+
+// ------------------------------------------------------------------------
+// the pass on tcgen05: one CTA = 128 samples, thread t owns sample row t through all layers
+// ------------------------------------------------------------------------
+// Per layer (the flow definition above), in tensor memory columns [0, 256):
+//   MMA1  D[0,128)   = A1 [128 x 16]  * W1n^T   (one K = 16 slice)
+//   epilogue: h1 = relu(D + b1) -> bf16 -> A2 (canonical layout)
+//   MMA2  D[128,256) = A2 [128 x 128] * W2n^T   (eight slices)
+//   epilogue: h2 = relu(D + b2) -> bf16 -> A2 (MMA2 has completed)
+//   MMA3  D[0,32)    = A2 [128 x 128] * W3n^T   (N = 32: columns 2d.. of W3n are zero)
+//   epilogue: o = D + b3, the coupling of row t in registers and shared memory.
+// One thread issues the MMAs and commits them to an mbarrier that every thread waits on
+// (bounded); each thread reads its own TMEM lane (row) with tcgen05.ld.  The next layer's
+// weights arrive by cp.async into the second of two buffers while the layer computes.  The
+// dot products run in the tensor core's order rather than the mma.sync kernel's, so the two
+// kernels agree to f32 accumulation rounding (both against the oracle at bf16 tolerance).
+#define FTC_ROWS 128
+#define FTC_LDY (FLOW_MAXD + 1)
+struct FlowTcSmem {
+    __nv_bfloat16 W2[2][FLOW_H * FLOW_H]; // canonical [128][128]
+    __nv_bfloat16 A2[FTC_ROWS * FLOW_H];  // canonical [128][128]: h1, then h2
+    __nv_bfloat16 W3[2][32 * FLOW_H];     // canonical [32][128]
+    __nv_bfloat16 W1[2][FLOW_H * 16];     // canonical [128][16]
+    __nv_bfloat16 A1[FTC_ROWS * 16];      // canonical [128][16]
+    float Y[FTC_ROWS * FTC_LDY];          // the rows' coordinates
+    float O[FTC_ROWS * FTC_LDY];          // the rows' MLP outputs o = (s, t) of the layer
+    float bias[2][2 * FLOW_H + 32];
+    int perm[FLOW_MAXL * FLOW_MAXD];
+    uint64_t mbar;
+    uint32_t tslot;
+};
+
+// one layer's weights (canonical layouts) and biases into buffer buf, as one cp.async group
+__device__ __forceinline__ void tc_load_layer(FlowTcSmem &s, const __nv_bfloat16 *wl, const float *P, int d, int buf)
+{
+    for (int i = threadIdx.x; i < FLOW_H * 2; i += blockDim.x) { // W1n [128][16]: 2 chunks per row
+        const int r = i >> 1, c = i & 1;
+        cp_async16((unsigned char *)s.W1[buf] + canon_off(r, 8 * c, 16), wl + WB_W1N + r * 16 + 8 * c);
+    }
+    for (int i = threadIdx.x; i < FLOW_H * 16; i += blockDim.x) { // W2n [128][128]: 16 chunks per row
+        const int r = i >> 4, c = i & 15;
+        cp_async16((unsigned char *)s.W2[buf] + canon_off(r, 8 * c, FLOW_H), wl + WB_W2N + r * FLOW_H + 8 * c);
+    }
+    for (int i = threadIdx.x; i < 32 * 16; i += blockDim.x) { // W3n [32][128]
+        const int r = i >> 4, c = i & 15;
+        cp_async16((unsigned char *)s.W3[buf] + canon_off(r, 8 * c, FLOW_H), wl + WB_W3N + r * FLOW_H + 8 * c);
+    }
+    const bool aligned = ((reinterpret_cast<uintptr_t>(P + pl_b1(d)) | reinterpret_cast<uintptr_t>(P + pl_b2(d))) & 15) == 0;
+    if (aligned) {
+        for (int i = threadIdx.x; i < FLOW_H / 4; i += blockDim.x) {
+            cp_async16(s.bias[buf] + 4 * i, P + pl_b1(d) + 4 * i);
+            cp_async16(s.bias[buf] + FLOW_H + 4 * i, P + pl_b2(d) + 4 * i);
+        }
+    } else {
+        for (int i = threadIdx.x; i < FLOW_H; i += blockDim.x) {
+            s.bias[buf][i] = P[pl_b1(d) + i];
+            s.bias[buf][FLOW_H + i] = P[pl_b2(d) + i];
+        }
+    }
+    cp_async_commit();
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) { s.bias[buf][2 * FLOW_H + i] = (i < 2 * d) ? P[pl_b3(d) + i] : 0.f; }
+}
+
+// relu(D[cols c0..c0+127] + bias) of the thread's row into A2 as bf16
+__device__ __forceinline__ void tc_hidden_epilogue(FlowTcSmem &s, uint32_t tlane, uint32_t c0, const float *bias, int row)
+{
+    unsigned char *dst = (unsigned char *)s.A2;
+#pragma unroll 1
+    for (int c = 0; c < FLOW_H; c += 16) {
+        float v[16];
+        tmem_ld16(tlane + c0 + (uint32_t)c, v);
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float lo = fmaxf(v[2 * j] + bias[c + 2 * j], 0.f), hi = fmaxf(v[2 * j + 1] + bias[c + 2 * j + 1], 0.f);
+            w[j] = pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
+        }
+        *(uint4 *)(dst + canon_off(row, c, FLOW_H)) = make_uint4(w[0], w[1], w[2], w[3]);
+        *(uint4 *)(dst + canon_off(row, c + 8, FLOW_H)) = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+// every thread's shared-memory writes done and visible to the tensor core, and the previous
+// tensor-memory reads finished, before thread 0 issues the next MMAs
+__device__ __forceinline__ void tc_handoff()
+{
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+}
+
+__global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, int *status)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FlowTcSmem &s = *(FlowTcSmem *)smem_raw;
+    const int t = threadIdx.x, warp = t >> 5;
+    const int base = blockIdx.x * FTC_ROWS, row = base + t;
+    const bool live = row < f.n;
+    const int D = f.D, d = f.d;
+    float *Y = s.Y + t * FTC_LDY;
+    for (int c = 0; c < D; ++c) {
+        float v = live ? flow_input(f, row, c) : 0.f;
+        if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); } // density: undo the base affine first
+        Y[c] = v;
+    }
+    for (int i = t; i < f.L * D; i += blockDim.x) { s.perm[i] = f.perm[i]; }
+    const uint32_t mbar = smem_addr(&s.mbar);
+    if (t == 0) { mbar_init(mbar, 1); }
+    if (warp == 0) { tmem_alloc(smem_addr(&s.tslot), 256); }
+    auto layer_of = [&](int step) { return (f.dir == 0) ? step : f.L - 1 - step; };
+    auto params_of = [&](int step) { return f.theta + (int64_t)layer_of(step) * f.pstride; };
+    tc_load_layer(s, f.wb + (int64_t)layer_of(0) * f.wstride, params_of(0), d, 0);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = s.tslot;
+    const uint32_t tlane = taddr + ((uint32_t)(32 * warp) << 16); // this warp's 32 TMEM lanes
+    const uint32_t id_h = umma_idesc_bf16(128, FLOW_H), id_o = umma_idesc_bf16(128, 32);
+    uint32_t phase = 0;
+    bool ok = true;
+    float logdet = 0.f;
+    for (int step = 0; step < f.L && ok; ++step) {
+        const int l = layer_of(step);
+        const int buf = step & 1;
+        const int *perm = s.perm + l * D;
+        const float *bias = s.bias[buf];
+        cp_async_wait<0>(); // this layer's weights (issued during the previous layer) have arrived
+        // the a-half of the row as bf16 (columns d..15 zero)
+        {
+            uint32_t w[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float lo = (2 * j < d) ? Y[perm[2 * j]] : 0.f, hi = (2 * j + 1 < d) ? Y[perm[2 * j + 1]] : 0.f;
+                w[j] = pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
+            }
+            unsigned char *a1 = (unsigned char *)s.A1;
+            *(uint4 *)(a1 + canon_off(t, 0, 16)) = make_uint4(w[0], w[1], w[2], w[3]);
+            *(uint4 *)(a1 + canon_off(t, 8, 16)) = make_uint4(w[4], w[5], w[6], w[7]);
+        }
+        tc_handoff();
+        if (step + 1 < f.L) { // the other buffer was last read by the previous layer's MMAs, which have completed
+            tc_load_layer(s, f.wb + (int64_t)layer_of(step + 1) * f.wstride, params_of(step + 1), d, buf ^ 1);
+        }
+        // h1
+        if (t == 0) {
+            umma_bf16(taddr, umma_desc(smem_addr(s.A1), 128, 16 * 16), umma_desc(smem_addr(s.W1[buf]), 128, 16 * 16), id_h, 0u);
+            umma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        phase ^= 1;
+        if (!ok) { break; }
+        tc_fence_after();
+        tc_hidden_epilogue(s, tlane, 0, bias, t);
+        tc_handoff();
+        // h2
+        if (t == 0) {
+            for (int ks = 0; ks < FLOW_H / 16; ++ks) {
+                umma_bf16(taddr + 128, umma_desc(smem_addr(s.A2) + 256 * ks, 128, 16 * FLOW_H),
+                          umma_desc(smem_addr(s.W2[buf]) + 256 * ks, 128, 16 * FLOW_H), id_h, ks > 0 ? 1u : 0u);
+            }
+            umma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        phase ^= 1;
+        if (!ok) { break; }
+        tc_fence_after();
+        tc_hidden_epilogue(s, tlane, 128, bias + FLOW_H, t);
+        tc_handoff();
+        // o
+        if (t == 0) {
+            for (int ks = 0; ks < FLOW_H / 16; ++ks) {
+                umma_bf16(taddr, umma_desc(smem_addr(s.A2) + 256 * ks, 128, 16 * FLOW_H),
+                          umma_desc(smem_addr(s.W3[buf]) + 256 * ks, 128, 16 * FLOW_H), id_o, ks > 0 ? 1u : 0u);
+            }
+            umma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        phase ^= 1;
+        if (!ok) { break; }
+        tc_fence_after();
+        float *O = s.O + t * FTC_LDY; // o of the row (indexed by the runtime half width d)
+        for (int c = 0; c < 32; c += 16) {
+            float v[16];
+            tmem_ld16(tlane + (uint32_t)c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) { O[c + j] = v[j] + bias[2 * FLOW_H + c + j]; }
+        }
+        // coupling of the row
+        float *tp = (f.tape && live) ? f.tape + ((int64_t)l * f.n + row) * 4 * d : nullptr;
+        for (int j = 0; j < d; ++j) {
+            const float sj = soft_clamp(O[j]);
+            const float tv = O[d + j];
+            const int pb = perm[d + j];
+            const float bin = Y[pb];
+            const float bout = (f.dir == 0) ? fmaf(bin, __expf(sj), tv) : (bin - tv) * __expf(-sj);
+            if (tp) {
+                tp[j] = Y[perm[j]];
+                tp[d + j] = bout;
+                tp[2 * d + j] = sj;
+                tp[3 * d + j] = tv;
+            }
+            Y[pb] = bout;
+            logdet += sj;
+        }
+    }
+    if (!ok && t == 0) { atomicOr(status, 1); }
+    cp_async_wait<0>(); // a prefetch issued before a failed wait
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) { tmem_dealloc(taddr, 256); }
+    if (!ok || !live) { return; }
+    // output and log q of the row
+    float ls = 0.f;
+    for (int c = 0; c < D; ++c) { ls += f.logsig[c]; }
+    float zz = 0.f;
+    for (int c = 0; c < D; ++c) {
+        float z, o;
+        if (f.dir == 0) { // z was the input
+            z = flow_input(f, row, c);
+            o = f.mu[c] + __expf(f.logsig[c]) * Y[c];
+        } else {
+            z = Y[c];
+            o = z;
+        }
+        zz = fmaf(z, z, zz);
+        if (f.out) { f.out[(int64_t)row * D + c] = o; }
+        if (f.out_cm) { f.out_cm[(int64_t)c * f.cm_stride + row] = o; }
+    }
+    f.logq[row] = -0.5f * zz - 0.91893853320467274f * D - logdet - ls;
+}
+
+// ------------------------------------------------------------------------
 // backward: gradient of -mean log q through the density direction
 // ------------------------------------------------------------------------
 struct FlowBwdSmem {
@@ -853,6 +1236,10 @@ struct mcig_flow {
     // work buffers
     float *buf_in = nullptr, *buf_out = nullptr, *buf_logq = nullptr, *buf_tape = nullptr, *buf_batch = nullptr;
     int64_t cap = 0, tape_cap = 0, batch_cap = 0;
+    // passes on tcgen05 (flow_pass_tc_kernel) or on mma.sync (flow_pass_kernel); status bit 0:
+    // a tcgen05 pass did not see an MMA completion within its bounded wait
+    int tc = 0;
+    int *status = nullptr;
 };
 
 static int flow_err(int code, const std::string &m) { return mcig_set_last_error(code, m.c_str()); }
@@ -964,6 +1351,9 @@ extern "C" int mcig_flow_create(int ndim, int nlayers, int hidden, uint64_t seed
     int rc = flow_cast(f, f->st);
     if (rc) { return rc; }
     FCK(cudaFuncSetAttribute(flow_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowSmem)));
+    FCK(cudaFuncSetAttribute(flow_pass_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowTcSmem)));
+    FCK(cudaMalloc(&f->status, sizeof(int)));
+    FCK(cudaMemset(f->status, 0, sizeof(int)));
     FCK(cudaFuncSetAttribute(flow_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowBwdSmem)));
     FCK(cudaStreamSynchronize(f->st));
     *out = f;
@@ -976,9 +1366,40 @@ extern "C" int mcig_flow_destroy(mcig_flow *f)
     cudaSetDevice(f->device);
     cudaStreamSynchronize(f->st);
     cudaFree(f->theta); cudaFree(f->grad); cudaFree(f->m); cudaFree(f->v); cudaFree(f->wb); cudaFree(f->perm);
+    cudaFree(f->status);
     cudaFree(f->buf_in); cudaFree(f->buf_out); cudaFree(f->buf_logq); cudaFree(f->buf_tape); cudaFree(f->buf_batch);
     cudaStreamDestroy(f->st);
     delete f;
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_tc_selftest(int device, const uint16_t *a, const uint16_t *b, int n, int k, float *d)
+{
+    if (!a || !b || !d) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "tc self-test: NULL pointer"); }
+    if (n < 16 || n > 256 || n % 16 || k < 16 || k > 256 || k % 16) {
+        return flow_err(MCIG_ERR_INVALID_ARGUMENT, "tc self-test: N and K must be multiples of 16 in [16, 256]");
+    }
+    FCK(cudaSetDevice(device));
+    __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+    float *dD = nullptr;
+    int *dst = nullptr;
+    FCK(cudaMalloc(&dA, 128 * (size_t)k * 2));
+    FCK(cudaMalloc(&dB, (size_t)n * k * 2));
+    FCK(cudaMalloc(&dD, 128 * (size_t)n * 4));
+    FCK(cudaMalloc(&dst, sizeof(int)));
+    FCK(cudaMemcpy(dA, a, 128 * (size_t)k * 2, cudaMemcpyHostToDevice));
+    FCK(cudaMemcpy(dB, b, (size_t)n * k * 2, cudaMemcpyHostToDevice));
+    FCK(cudaMemset(dst, 0, sizeof(int)));
+    const size_t smem = (128 + (size_t)n) * k * 2 + 16;
+    FCK(cudaFuncSetAttribute(flow_tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    flow_tc_selftest_kernel<<<1, 128, smem>>>(dA, dB, dD, n, k, dst);
+    FCK(cudaGetLastError());
+    FCK(cudaDeviceSynchronize());
+    int st = 0;
+    FCK(cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost));
+    FCK(cudaMemcpy(d, dD, 128 * (size_t)n * 4, cudaMemcpyDeviceToHost));
+    cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(dst);
+    if (st) { return flow_err(MCIG_ERR_TIMEOUT, "tc self-test: the MMA completion was not seen within the wait limit"); }
     return MCIG_OK;
 }
 
@@ -1009,9 +1430,34 @@ extern "C" int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n)
 // one pass over device arrays (in [n][D] float -> out, logq); tape optional
 static int flow_pass_launch(mcig_flow *f, FlowArgs &a, int64_t n, cudaStream_t st)
 {
-    const int grid = (int)((n + FLOW_PASS_ROWS - 1) / FLOW_PASS_ROWS);
-    flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
+    if (f->tc) {
+        const int grid = (int)((n + FTC_ROWS - 1) / FTC_ROWS);
+        flow_pass_tc_kernel<<<grid, FTC_ROWS, sizeof(FlowTcSmem), st>>>(a, f->status);
+    } else {
+        const int grid = (int)((n + FLOW_PASS_ROWS - 1) / FLOW_PASS_ROWS);
+        flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
+    }
     FCK(cudaGetLastError());
+    return MCIG_OK;
+}
+
+// the status of the tcgen05 passes since the last check (then cleared)
+int mcig_flow_check_status(mcig_flow *f, cudaStream_t st)
+{
+    int h = 0;
+    FCK(cudaMemcpyAsync(&h, f->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FCK(cudaStreamSynchronize(st));
+    if (h) {
+        FCK(cudaMemsetAsync(f->status, 0, sizeof(int), st));
+        return flow_err(MCIG_ERR_TIMEOUT, "flow: a tensor-core pass did not see its MMA complete within the bounded wait");
+    }
+    return MCIG_OK;
+}
+
+extern "C" int mcig_flow_set_tensor_path(mcig_flow *f, int tc)
+{
+    if (!f) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow is NULL"); }
+    f->tc = tc ? 1 : 0;
     return MCIG_OK;
 }
 
@@ -1074,10 +1520,7 @@ int mcig_flow_pass_device(mcig_flow *f, int dir, const float *d_in, int64_t n, f
     a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
     a.perm = f->perm; a.tape = d_tape; a.wb = f->wb; a.theta = f->theta;
     a.wstride = WB_LAYER; a.pstride = f->pstride;
-    const int grid = (int)((n + FLOW_PASS_ROWS - 1) / FLOW_PASS_ROWS);
-    flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
-    FCK(cudaGetLastError());
-    return MCIG_OK;
+    return flow_pass_launch(f, a, n, st);
 }
 
 static int flow_host_pass(mcig_flow *f, int dir, const double *in, int64_t n, double *out, double *logq)
@@ -1095,6 +1538,7 @@ static int flow_host_pass(mcig_flow *f, int dir, const double *in, int64_t n, do
     FCK(cudaMemcpyAsync(h.data(), f->buf_out, h.size() * sizeof(float), cudaMemcpyDeviceToHost, f->st));
     FCK(cudaMemcpyAsync(lq.data(), f->buf_logq, n * sizeof(float), cudaMemcpyDeviceToHost, f->st));
     FCK(cudaStreamSynchronize(f->st));
+    if ((rc = mcig_flow_check_status(f, f->st))) { return rc; }
     if (out) { for (size_t i = 0; i < h.size(); ++i) { out[i] = h[i]; } }
     if (logq) { for (int64_t i = 0; i < n; ++i) { logq[i] = lq[i]; } }
     return MCIG_OK;

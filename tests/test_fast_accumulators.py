@@ -124,14 +124,27 @@ def test_split_calibration_equals_one_lane(ndim, pdf, nfind):
         np.testing.assert_array_equal(u, v)
 
 
+def _uncorr_ref(full, nv):
+    """MultiDimUncorrelatedEstimator (Estimators.cpp:125-155) per chain in double on the
+    float Full samples [nchains][naccu * nv]"""
+    x = full.reshape(full.shape[0], -1, nv).astype(np.float64)
+    n = x.shape[1]
+    avg = x.mean(axis=1)
+    var = (x * x).sum(axis=1) / n - avg * avg
+    err = np.where(var > 1e-300, np.sqrt(np.maximum(var, 0) / (n - 1.)), 0.)
+    return avg, err, np.sqrt(np.maximum(var, 0))
+
+
 @pytest.mark.parametrize("nskip", [1, 3])
 def test_chunked_sampling_equals_one_launch(nskip):
-    """Main sampling in chunks with the Full-sample estimator beside the next chunk
-    (mcig_set_sampling_chunks) against one launch: identical accumulator data, chain
-    estimates, averages, errors and counts."""
+    """Main sampling in one launch, with the Full observables' Uncorrelated estimates formed by
+    the sampling kernel itself (mcig_set_fused_estimates: windows of 128 float sums folded into
+    Kahan sums) or by the estimator kernel, and in chunks with the estimator beside the next
+    chunk (mcig_set_sampling_chunks): identical accumulator data, counts and Block estimates;
+    the Full estimates of all against the reference formula in double on the same samples."""
     import mcintegratorplusplus_gb300 as mcig
     res = []
-    for chunks in (1, 4, 3):  # 1: one launch (the default)
+    for chunks, fused in ((1, 1), (1, 0), (4, 0), (3, 0)):  # one launch with and without the fused estimates
         nc, nmc = 512, 2400
         m = mcig.MCI(16, nc, precision=mcig.PREC_FP32)
         m.setSeed(21)
@@ -144,9 +157,25 @@ def test_chunked_sampling_equals_one_launch(nskip):
         m.addObservable(mcig.OBS_XND, (), 1, nskip, False, mcig.EST_UNCORRELATED)              # Full
         m.addObservable(mcig.OBS_X2SUM, (), 1, 1, False, mcig.EST_UNCORRELATED)                # Full
         m.setSamplingChunks(chunks)
+        m.setFusedEstimates(fused)
         avg, err = m.integrate(nmc)
         ca, ce = m.getChainResults()
         res.append([avg, err, ca, ce, *m.getCounts()] + [m.getObsData(o) for o in range(3)])
+    nv_of = [1, 16, 1]
     for other in res[1:]:
-        for a, b in zip(res[0], other):
+        for a, b in zip(res[0][4:], other[4:]):  # counts and accumulator data
             assert np.array_equal(a, b)
+        # Block estimates (value 0) are formed by the same estimator kernel in both
+        assert np.array_equal(res[0][2][:, 0], other[2][:, 0]) and np.array_equal(res[0][3][:, 0], other[3][:, 0])
+    for r in res:
+        off = 1
+        for o in (1, 2):
+            avg, err, sd = _uncorr_ref(r[6 + o], nv_of[o])
+            ca, ce = r[2][:, off:off + nv_of[o]], r[3][:, off:off + nv_of[o]]
+            assert np.max(np.abs(ca - avg) / (np.abs(avg) + sd)) < 1e-6
+            np.testing.assert_allclose(ce, err, rtol=2e-5)
+            off += nv_of[o]
+    # the combined results: the same to the estimates' rounding
+    for other in res[1:]:
+        np.testing.assert_allclose(other[0], res[0][0], rtol=1e-6, atol=1e-6)
+        np.testing.assert_allclose(other[1], res[0][1], rtol=2e-5)

@@ -16,6 +16,39 @@ def random_params(seed, scale=0.02):
     return th.astype(np.float32)
 
 
+def _to_bf16_bits(x):
+    """float32 -> bf16 bit patterns, round to nearest even"""
+    b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    return ((b + 0x7FFF + ((b >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def _bf16_value(bits):
+    return (bits.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,k", [(128, 16), (128, 128), (32, 128), (256, 64)])
+def test_tcgen05_gemm_selftest(n, k):
+    """The 5th-generation tensor-core path (tcgen05.mma, shared-memory descriptors of the
+    no-swizzle K-major layout, f32 accumulator in tensor memory, tcgen05.ld) forms
+    D = A B^T of bf16 operands as the float64 product of the same bf16 values does, to f32
+    accumulation rounding."""
+    import ctypes
+    from mcintegratorplusplus_gb300 import _lib
+    L = _lib.load()
+    rng = np.random.default_rng(n * 1000 + k)
+    a = _to_bf16_bits(rng.standard_normal((128, k)))
+    b = _to_bf16_bits(rng.standard_normal((n, k)))
+    d = np.full((128, n), np.nan, dtype=np.float32)
+    rc = L.mcig_flow_tc_selftest(0, a.ctypes.data, b.ctypes.data, n, k,
+                                 d.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    assert rc == 0, L.mcig_last_error()
+    ref = _bf16_value(a) @ _bf16_value(b).T
+    scale = np.sqrt(k)
+    assert np.all(np.isfinite(d))
+    assert np.max(np.abs(d - ref)) < 1e-5 * scale * 8, np.max(np.abs(d - ref))
+
+
 def test_oracle_round_trip_and_gradient_by_finite_differences():
     perms = fo.permutations(D, 4, 7)
     rng = np.random.default_rng(0)
@@ -47,8 +80,11 @@ def mcig():
 
 
 @pytest.mark.gpu
-def test_flow_passes_match_oracle(mcig):
+@pytest.mark.parametrize("tc", [False, True])
+def test_flow_passes_match_oracle(mcig, tc):
+    """Both pass kernels (mma.sync; tcgen05 with TMEM accumulators) against the oracle."""
     f = mcig.Flow(D, L, H, seed=11)
+    f.set_tensor_path(tc)
     th = random_params(5)
     f.set_params(th)
     perms = fo.permutations(D, L, 11)
@@ -68,10 +104,12 @@ def test_flow_passes_match_oracle(mcig):
 
 
 @pytest.mark.gpu
-def test_flow_odd_half_dimension_matches_oracle(mcig):
+@pytest.mark.parametrize("tc", [False, True])
+def test_flow_odd_half_dimension_matches_oracle(mcig, tc):
     """D = 6 (d = 3): layer parameter blocks that do not start on 16-byte boundaries."""
     Dd, Ld = 6, 3
     f = mcig.Flow(Dd, Ld, H, seed=3)
+    f.set_tensor_path(tc)
     rng = np.random.default_rng(4)
     th = (fo.init_params(Dd, Ld, H, 3).astype(np.float64) + rng.standard_normal(fo.nparams(Dd, Ld, H)) * 0.02)
     f.set_params(th.astype(np.float32))

@@ -31,12 +31,14 @@ def test_noalloc_rejects_oversize_and_bad_n_without_device_work():
 
 
 @pytest.mark.gpu
-def test_noalloc_matches_allocating_estimator_twice():
+def test_noalloc_matches_allocating_estimator_call_after_call():
     import torch
     import mcintegratorplusplus_gb300 as mcig
     L = _lib()
-    for seed, n, nd in ((1337, 1 << 15, 2), (7, 1 << 12, 17)):  # two calls in a row, different data
-        x = orc.splitmix64_ar1(seed, n, nd, 0.9 if nd == 2 else 0.5)
+    # calls in a row on different data: two small shapes, then the largest accepted sizes
+    # (n * ndim == 2^21 values, the static scratch) with one coordinate and with four
+    for seed, n, nd in ((1337, 1 << 15, 2), (7, 1 << 12, 17), (11, 1 << 21, 1), (13, 1 << 19, 4)):
+        x = orc.splitmix64_ar1(seed, n, nd, 0.9 if nd <= 2 else 0.5)
         ref_avg, ref_err = mcig.estimate(mcig.EST_MJBLOCKER, x)  # allocating entry point
         dx = torch.from_numpy(x).cuda()
         davg = torch.full((nd,), float("nan"), dtype=torch.float64, device="cuda")

@@ -284,12 +284,12 @@ def run_gpu(args):
                            "e2e_integrals_per_s": c3["e2e"]["value"], "outer_steps_per_s": c3["outer_steps_per_s"],
                            "config": c3["config"], "accuracy": c3["accuracy"], "clocks": c3["clocks"]}
     if args.learned:
-        c5 = run_c5(argparse.Namespace(chains5=16384, nmc5=8192, warmup=1, steps=1))
+        c5 = run_c5(argparse.Namespace(chains5=16384, nmc5=8192, warmup=1, steps=1, c5_flow_gemm=args.c5_flow_gemm))
         line["learned_proposal"] = {
             "workload": "C5: 16,384 chains x 24-D 4-mode mixture, 8-layer affine-coupling flow every 5th step",
             "ess_per_s_flow": c5["value"], "ess_per_s_plain_mh": c5["plain_mh"]["value"],
             "ratio": c5["ess_per_s_ratio_flow_over_plain"], "flow_acceptance": c5["flow"]["acceptance"],
-            "ms_flow": c5["ms_per_step"], "ms_plain": c5["plain_mh"]["ms_per_step"]}
+            "ms_flow": c5["ms_per_step"], "ms_plain": c5["plain_mh"]["ms_per_step"], "flow_gemms": c5["flow_gemms"]}
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     return line
@@ -621,6 +621,7 @@ def run_c5(args):
             m.addObservable(mcig.OBS_XI, [0], 1, 1, False, mcig.EST_UNCORRELATED)
             if use_flow:
                 f = mcig.Flow(D, 8, 128, seed=6 + it)
+                f.set_tensor_path(args.c5_flow_gemm == "tcgen05")
                 _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=C5_ADAPT,
                                                 batch=nch, lr=3e-3)
                 accs.append(acc)
@@ -640,7 +641,7 @@ def run_c5(args):
     return {"metric": "effective samples/s of <x_1> (C5: 24-D 4-mode mixture, learned flow proposal)",
             "value": res[True][0], "unit": "effective samples/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res[True][1] * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 walker, bf16 flow GEMMs (f32 accumulate)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 walker, bf16 flow GEMMs (f32 accumulate)", "flow_gemms": args.c5_flow_gemm,
             "data": "synthetic (seeded mixture, random-init flow)",
             "config": {"workload": "C5 learned proposal", "chains": nch, "ndim": D, "nmc": nmc, "flow_layers": 8,
                        "hidden": 128, "period": 5, "adaptation_cycles": C5_ADAPT, "adam_batch": nch,
@@ -705,6 +706,8 @@ def main():
     ap.add_argument("--nmc4", type=int, default=65536)
     ap.add_argument("--chains5", type=int, default=16384)
     ap.add_argument("--nmc5", type=int, default=8192)
+    ap.add_argument("--c5-flow-gemm", default="tcgen05", choices=["tcgen05", "mma.sync"],
+                    help="tensor-core path of the flow's passes (the backward pass is mma.sync)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -106,10 +106,6 @@ int mcig_get_decision_stats(const mcig_mci *h, int64_t *checked, int64_t *revers
  * measured slower, hence off).  No counterpart in the reference, whose MCI::sample
  * (MCIntegrator.cpp:290-321) is one loop. */
 int mcig_set_sampling_chunks(mcig_mci *h, int n);
-/* 1: a single sampling launch of the register-resident kernel forms the Uncorrelated
- * estimates of its float Full observables itself (float window sums of x and x^2 folded into
- * Kahan sums), so the samples are not read back; 0: the estimator kernel reads them */
-int mcig_set_fused_estimates(mcig_mci *h, int on);
 
 /* MCI::setSeed (MCIntegrator.cpp:547-550).  Philox4x32-10 key; chain c draws
  * from counter (step, c).  */

@@ -35,7 +35,6 @@ SIGNATURES = {
     "mcig_set_calibration_split": (c_int, [c_void_p, c_int]),
     "mcig_set_lanes": (c_int, [c_void_p, c_int]),
     "mcig_set_sampling_chunks": (c_int, [c_void_p, c_int]),
-    "mcig_set_fused_estimates": (c_int, [c_void_p, c_int]),
     "mcig_set_fp64_decision": (c_int, [c_void_p, c_int]),
     "mcig_get_decision_stats": (c_int, [c_void_p, P_int64, P_int64, P_double]),
     "mcig_set_seed": (c_int, [c_void_p, ctypes.c_uint64]),

@@ -179,11 +179,6 @@ struct mcig_mci {
     // SMs' registers and the estimator ran mostly after it: 10.9 ms of estimation tail
     // against 8.1 ms for the one-pass estimator)
     int chunks = 1;
-    // mcig_set_fused_estimates: off by default.  Measured at C2 (65,536 chains x 10,000 steps,
-    // x.x and x_i Full): the estimator pass over the 44.6 GB of float samples took 7.6 ms at
-    // 5.9 TB/s, while forming the sums in the sampling launch added 8.6 ms to it (17 shared-
-    // memory window updates per step in a launch already bound by dependency latency)
-    int fused_est = 0;
     cudaStream_t est_stream = nullptr;
     cudaEvent_t cev[MCIG_MAX_CHUNKS + 1] = {};
     DBuf<float4> est_state;
@@ -1857,13 +1852,6 @@ extern "C" int mcig_set_sampling_chunks(mcig_mci *h, int n)
     return MCIG_OK;
 }
 
-extern "C" int mcig_set_fused_estimates(mcig_mci *h, int on)
-{
-    if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
-    h->fused_est = on ? 1 : 0;
-    return MCIG_OK;
-}
-
 static int64_t gcd64(int64_t a, int64_t b) { return b ? gcd64(b, a % b) : a; }
 
 // MCI::sample of the main run (MCIntegrator.cpp:290-321) as one launch, or, where the
@@ -1895,32 +1883,6 @@ static int sample_chunked(mcig_mci *h, const KParams &kp, int64_t nmc, std::vect
     int rc;
     if (!chunk) {
         s.nsteps = nmc;
-        // one sampling launch of the register-resident kernel forms the Uncorrelated estimates
-        // of its float Full observables itself (FastSampler::fuse_add): the samples are
-        // written once and not read back
-        if (h->fused_est && kernel_family(h, s) == 1 && h->full32 && any_full) {
-            int nod = 0;
-            size_t nstate = 0;
-            for (size_t o = 0; o < h->obs.size(); ++o) {
-                const ObsDef &d = h->obs[o];
-                if (d.acc == MCIG_ACC_FULL && d.estimator == MCIG_EST_UNCORRELATED && h->obs_nstore[o] >= 2) {
-                    s.obs[o].fuse = 1;
-                    s.obs[o].foff = (int)nstate;
-                    nstate += (size_t)d.nv;
-                    est_done[o] = 2;
-                }
-                nod += d.nv;
-            }
-            const size_t nc = (size_t)h->nchains;
-            if ((rc = h->est_avg.alloc(nc * std::max(nod, 1))) || (rc = h->est_err.alloc(nc * std::max(nod, 1))) ||
-                (rc = h->est_state.alloc(std::max(nstate, (size_t)1) * nc))) {
-                return rc;
-            }
-            s.fuse_state = h->est_state.p;
-            s.est_avg = h->est_avg.p;
-            s.est_err = h->est_err.p;
-            s.est_ldo = nod;
-        }
         return launch(h, s);
     }
     if (!h->est_stream) {

@@ -31,7 +31,6 @@
 #define MCIG_MAXTYPES 4
 #define MCIG_PERIODIC_MAXWRAP 64
 #define MCIG_MAXDIM 64
-#define MCIG_FUSE_W 128 // accumulations per float window of a fused Uncorrelated estimate
 #define MCIG_FAST_BLOCK 64 // threads per block of the register-resident kernel (slot stride)
 #define MCIG_FCONST 2080 // floats of sampling-function data in the parameter block (register-resident kernel)
 
@@ -66,9 +65,6 @@ struct ObsDesc {
     uint32_t bs_magic, bs_shift, sk_magic, sk_shift;
     double inv_bs; // 1. / bs (Block normalisation, BlockAccumulator.cpp)
     int lslot;     // multi-lane kernel (mcig_lanes.cuh): first accumulator slot of a lane
-    // register-resident kernel, float Full data with the Uncorrelated estimator: 1 when the
-    // sampling launch forms the estimate itself (KParams::fuse_state from value foff on)
-    int fuse, foff;
 };
 
 struct KParams {
@@ -111,12 +107,6 @@ struct KParams {
     int64_t r0;             // register-resident kernel, chunked sampling: step index of this launch's
                             // first step in the whole sampling run (accumulation and block indices)
     int acc_counts;         // 1: add this launch's counts to nacc/nrej (later chunks of a run)
-    // Uncorrelated estimates formed in the sampling launch (ObsDesc::fuse): Kahan float sums
-    // (s_x, c_x, s_x2, c_x2) of each series at fuse_state[(foff + j) * nchains + chain], and
-    // the estimates written to est_avg/est_err[chain * est_ldo + voff + j]
-    float4 *fuse_state;
-    double *est_avg, *est_err;
-    int est_ldo;
     const uint8_t *active;  // optional: chains with active[c] == 0 skip this launch
     // file output (storeObservablesOnFile / storeWalkerPositionsOnFile): chain 0 records
     // its walker after the steps dump_steps[0..ndump) (ascending) into dump_x[ndump][ndim]

@@ -293,7 +293,6 @@ struct FastSampler {
                     if (all || j < nv) { dst[j * nc] = (double)v[j]; }
                 }
             }
-            if (od.fuse) { fuse_add<NV>(od, k, v, nv, all); }
             return;
         }
         ST *sl = slots + od.voff * MCIG_FAST_BLOCK + threadIdx.x;
@@ -315,71 +314,6 @@ struct FastSampler {
                     Slot::zero(sl[j * MCIG_FAST_BLOCK]);
                 }
             }
-        }
-    }
-
-    // The Uncorrelated estimator of a float Full observable formed while sampling, so the
-    // samples are not read back (MultiDimUncorrelatedEstimator, Estimators.cpp:125-155):
-    // plain float sums of x and x^2 over windows of MCIG_FUSE_W accumulations in the
-    // observable's accumulator slots (a Full observable has slots it does not otherwise use),
-    // folded at each window's end into Kahan float sums per series in fuse_state
-    // (chain-minor, coalesced), and the estimate formed from those at the end of the launch.
-    __device__ __forceinline__ float2 *fuse_window(const ObsDesc &od) const
-    {
-        return reinterpret_cast<float2 *>(slots + od.voff * MCIG_FAST_BLOCK + threadIdx.x);
-    }
-    __device__ __forceinline__ static void kahan_add(float &s, float &cc, float v)
-    {
-        const float y = v - cc, t = s + y;
-        cc = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ void fuse_fold1(const ObsDesc &od, int j)
-    {
-        float2 *w = fuse_window(od) + j * MCIG_FAST_BLOCK;
-        const float2 a = *w;
-        float4 *sp = p.fuse_state + (size_t)(od.foff + j) * p.nchains + c;
-        float4 t = *sp;
-        kahan_add(t.x, t.y, a.x);
-        kahan_add(t.z, t.w, a.y);
-        *sp = t;
-        *w = make_float2(0.f, 0.f);
-    }
-    template <int NV>
-    __device__ __forceinline__ void fuse_add(const ObsDesc &od, uint32_t k, const float *v, int nv, bool all)
-    {
-        float2 *w = fuse_window(od);
-#pragma unroll
-        for (int j = 0; j < NV; ++j) {
-            if (all || j < nv) {
-                float2 a = w[j * MCIG_FAST_BLOCK];
-                a.x += v[j];
-                a.y = fmaf(v[j], v[j], a.y);
-                w[j * MCIG_FAST_BLOCK] = a;
-            }
-        }
-        if (((k + 1) & (MCIG_FUSE_W - 1)) == 0) {
-#pragma unroll
-            for (int j = 0; j < NV; ++j) {
-                if (all || j < nv) { fuse_fold1(od, j); }
-            }
-        }
-    }
-    // after the last step: the open window, then the estimate of every value (the reference
-    // formula in double, the 1-D wrapper's rounding for one value, as est_uncorr_f32_kernel)
-    __device__ void fuse_finish(const ObsDesc &od, int64_t nacc)
-    {
-        const double SMALLEST_ERROR = 1.e-300;
-        const double norm = 1. / nacc;
-        for (int j = 0; j < od.nv; ++j) {
-            if (nacc % MCIG_FUSE_W != 0) { fuse_fold1(od, j); }
-            const float4 t = p.fuse_state[(size_t)(od.foff + j) * p.nchains + c];
-            const double average = ((double)t.x - (double)t.y) * norm;
-            double e = ((double)t.z - (double)t.w) * norm - average * average;
-            if (od.nv == 1) { e = (e > SMALLEST_ERROR) ? sqrt(e / (nacc - 1.)) : 0.; }
-            else { e = (e > SMALLEST_ERROR) ? sqrt(e * (1. / (nacc - 1.))) : 0.; }
-            p.est_avg[(size_t)c * p.est_ldo + od.voff + j] = average;
-            p.est_err[(size_t)c * p.est_ldo + od.voff + j] = e;
         }
     }
 
@@ -472,12 +406,6 @@ struct FastSampler {
     {
         lp = fast_logp<MAXD, PK>(p, fc, x);
         for (int j = 0; j < p.nobsdim && sample; ++j) { Slot::zero(slot(j)); }
-        for (int o = 0; o < p.nobs && sample; ++o) {
-            if (!p.obs[o].fuse) { continue; }
-            for (int j = 0; j < p.obs[o].nv; ++j) {
-                p.fuse_state[(size_t)(p.obs[o].foff + j) * p.nchains + c] = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        }
         const uint32_t n32 = (uint32_t)n;
         const uint32_t r0 = (uint32_t)p.r0; // chunked sampling: global index of the first step
         uint32_t na = 0;
@@ -491,9 +419,6 @@ struct FastSampler {
             for (int o = MCIG_FAST_UNROLLED_OBS; o < p.nobs; ++o) { obs_step(p.obs[o], r0 + r); }
         }
         if (sample) {
-            for (int o = 0; o < p.nobs; ++o) {
-                if (p.obs[o].fuse) { fuse_finish(p.obs[o], 1 + (n - 1) / p.obs[o].nskip); }
-            }
             for (int o = 0; o < p.nobs; ++o) { // SimpleAccumulator::_finalize
                 const ObsDesc &od = p.obs[o];
                 if (od.acc != MCIG_ACC_SIMPLE) { continue; }

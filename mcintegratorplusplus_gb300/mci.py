@@ -125,11 +125,6 @@ class MCI:
         """Main sampling in n launches with the Full-sample estimator overlapped (1: one launch)."""
         _raise(self.L.mcig_set_sampling_chunks(self._h, int(n)))
 
-    def setFusedEstimates(self, on):
-        """Uncorrelated estimates of float Full observables formed in the sampling launch (1)
-        or by the estimator kernel reading the samples back (0)."""
-        _raise(self.L.mcig_set_fused_estimates(self._h, int(bool(on))))
-
     def setFP64Decision(self, mode=1):
         """Metropolis decision certified in double near the float threshold (1), on every step (2), off (0)."""
         _raise(self.L.mcig_set_fp64_decision(self._h, int(mode)))

@@ -105,7 +105,7 @@ def ess_report(chain_means, var, nchains, nmc, series=None, mj=None, block_err=N
     if series is not None:
         s = np.asarray(series, dtype=np.float64)
         out["tau_int_sokal"] = sokal_tau(s)
-        out["tau_series"] = "Full x.x of %d chains x %d samples" % s.shape
+        out["tau_series"] = "Full samples of the observable, %d chains x %d" % s.shape
         if mj is not None:
             n2 = 1 << int(np.floor(np.log2(s.shape[1])))
             tail = np.ascontiguousarray(s[:, -n2:].T)  # [n2][chains]: one MJBlocker series per chain
@@ -706,7 +706,7 @@ def main():
     ap.add_argument("--nmc4", type=int, default=65536)
     ap.add_argument("--chains5", type=int, default=16384)
     ap.add_argument("--nmc5", type=int, default=8192)
-    ap.add_argument("--c5-flow-gemm", default="tcgen05", choices=["tcgen05", "mma.sync"],
+    ap.add_argument("--c5-flow-gemm", default="mma.sync", choices=["tcgen05", "mma.sync"],
                     help="tensor-core path of the flow's passes (the backward pass is mma.sync)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -639,6 +639,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; ++i) { v[i] = __uint_as_float(r[i]); }
 }
 
+// 32 consecutive f32 columns of the warp's 32 TMEM lanes, without the wait (tmem_ld_wait)
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                 "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                   "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
 // Self-test of the path: D[128][N] = A[128][K] B[N][K]^T, one CTA of 128 threads (thread t
 // reads row t of D from TMEM lane t).  N a multiple of 16 in [16, 256], K a multiple of 16 in
 // [16, 256]; status bit 0 set when the MMA's completion was not seen within the wait limit.
@@ -695,21 +709,24 @@ __global__ void __launch_bounds__(128, 1) flow_tc_selftest_kernel(const __nv_bfl
 }
 
 // ------------------------------------------------------------------------
-// the pass on tcgen05: one CTA = 128 samples, thread t owns sample row t through all layers
+// the pass on tcgen05: one CTA = 128 samples (the MMA tile's M), 8 warps
 // ------------------------------------------------------------------------
 // Per layer (the flow definition above), in tensor memory columns [0, 256):
 //   MMA1  D[0,128)   = A1 [128 x 16]  * W1n^T   (one K = 16 slice)
 //   epilogue: h1 = relu(D + b1) -> bf16 -> A2 (canonical layout)
 //   MMA2  D[128,256) = A2 [128 x 128] * W2n^T   (eight slices)
 //   epilogue: h2 = relu(D + b2) -> bf16 -> A2 (MMA2 has completed)
-//   MMA3  D[0,32)    = A2 [128 x 128] * W3n^T   (N = 32: columns 2d.. of W3n are zero)
-//   epilogue: o = D + b3, the coupling of row t in registers and shared memory.
-// One thread issues the MMAs and commits them to an mbarrier that every thread waits on
-// (bounded); each thread reads its own TMEM lane (row) with tcgen05.ld.  The next layer's
+//   MMA3  D[0,32)    = A2 [128 x 128] * W3n^T   (N = 32: rows 2d.. of W3n are zero)
+//   epilogue: o = D + b3, the coupling of each row in shared memory.
+// Warp w reads TMEM lanes 32 (w % 4) .. + 31, i.e. the rows of its quarter, and in the hidden
+// epilogues the column half w / 4 of them (two 32-column loads, one wait); the row's
+// coupling and output belong to the thread of warp w < 4.  One thread issues the MMAs and
+// commits them to an mbarrier that every thread waits on (bounded).  The next layer's
 // weights arrive by cp.async into the second of two buffers while the layer computes.  The
 // dot products run in the tensor core's order rather than the mma.sync kernel's, so the two
 // kernels agree to f32 accumulation rounding (both against the oracle at bf16 tolerance).
 #define FTC_ROWS 128
+#define FTC_THREADS 256
 #define FTC_LDY (FLOW_MAXD + 1)
 struct FlowTcSmem {
     __nv_bfloat16 W2[2][FLOW_H * FLOW_H]; // canonical [128][128]
@@ -756,22 +773,27 @@ __device__ __forceinline__ void tc_load_layer(FlowTcSmem &s, const __nv_bfloat16
     for (int i = threadIdx.x; i < 32; i += blockDim.x) { s.bias[buf][2 * FLOW_H + i] = (i < 2 * d) ? P[pl_b3(d) + i] : 0.f; }
 }
 
-// relu(D[cols c0..c0+127] + bias) of the thread's row into A2 as bf16
-__device__ __forceinline__ void tc_hidden_epilogue(FlowTcSmem &s, uint32_t tlane, uint32_t c0, const float *bias, int row)
+// relu(D + bias) of 64 columns [c0, c0 + 64) of the thread's row (TMEM lane) into A2 as bf16
+__device__ __forceinline__ void tc_hidden_epilogue(FlowTcSmem &s, uint32_t tlane, uint32_t tcol, int c0, const float *bias,
+                                                   int row)
 {
     unsigned char *dst = (unsigned char *)s.A2;
-#pragma unroll 1
-    for (int c = 0; c < FLOW_H; c += 16) {
-        float v[16];
-        tmem_ld16(tlane + c0 + (uint32_t)c, v);
-        uint32_t w[8];
+    uint32_t r0[32], r1[32];
+    tmem_ld32_nowait(tlane + tcol + (uint32_t)c0, r0);
+    tmem_ld32_nowait(tlane + tcol + (uint32_t)c0 + 32, r1);
+    tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const float lo = fmaxf(v[2 * j] + bias[c + 2 * j], 0.f), hi = fmaxf(v[2 * j + 1] + bias[c + 2 * j + 1], 0.f);
+    for (int q = 0; q < 8; ++q) { // 8 columns (16 bytes of bf16) per store
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int k = 8 * q + 2 * j; // column c0 + k within the 64
+            const float v0 = __uint_as_float(k < 32 ? r0[k] : r1[k - 32]);
+            const float v1 = __uint_as_float(k + 1 < 32 ? r0[k + 1] : r1[k + 1 - 32]);
+            const float lo = fmaxf(v0 + bias[c0 + k], 0.f), hi = fmaxf(v1 + bias[c0 + k + 1], 0.f);
             w[j] = pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
         }
-        *(uint4 *)(dst + canon_off(row, c, FLOW_H)) = make_uint4(w[0], w[1], w[2], w[3]);
-        *(uint4 *)(dst + canon_off(row, c + 8, FLOW_H)) = make_uint4(w[4], w[5], w[6], w[7]);
+        *(uint4 *)(dst + canon_off(row, c0 + 8 * q, FLOW_H)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 
@@ -785,20 +807,24 @@ __device__ __forceinline__ void tc_handoff()
     tc_fence_after();
 }
 
-__global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, int *status)
+__global__ void __launch_bounds__(FTC_THREADS, 1) flow_pass_tc_kernel(FlowArgs f, int *status)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FlowTcSmem &s = *(FlowTcSmem *)smem_raw;
-    const int t = threadIdx.x, warp = t >> 5;
-    const int base = blockIdx.x * FTC_ROWS, row = base + t;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int quad = warp & 3, half = warp >> 2;
+    const int rl = 32 * quad + lane; // the thread's row in the tile = its TMEM lane
+    const int base = blockIdx.x * FTC_ROWS, row = base + rl;
     const bool live = row < f.n;
+    const bool owner = half == 0; // the row's coupling and output
     const int D = f.D, d = f.d;
-    float *Y = s.Y + t * FTC_LDY;
-    for (int c = 0; c < D; ++c) {
-        float v = live ? flow_input(f, row, c) : 0.f;
+    for (int i = t; i < D * FTC_ROWS; i += blockDim.x) { // coordinate-major: coalesced chain-minor reads
+        const int c = i / FTC_ROWS, r = i % FTC_ROWS;
+        float v = (base + r < f.n) ? flow_input(f, base + r, c) : 0.f;
         if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); } // density: undo the base affine first
-        Y[c] = v;
+        s.Y[r * FTC_LDY + c] = v;
     }
+    float *Y = s.Y + rl * FTC_LDY;
     for (int i = t; i < f.L * D; i += blockDim.x) { s.perm[i] = f.perm[i]; }
     const uint32_t mbar = smem_addr(&s.mbar);
     if (t == 0) { mbar_init(mbar, 1); }
@@ -810,7 +836,7 @@ __global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, i
     __syncthreads();
     tc_fence_after();
     const uint32_t taddr = s.tslot;
-    const uint32_t tlane = taddr + ((uint32_t)(32 * warp) << 16); // this warp's 32 TMEM lanes
+    const uint32_t tlane = taddr + ((uint32_t)(32 * quad) << 16); // this warp's 32 TMEM lanes
     const uint32_t id_h = umma_idesc_bf16(128, FLOW_H), id_o = umma_idesc_bf16(128, 32);
     uint32_t phase = 0;
     bool ok = true;
@@ -821,17 +847,16 @@ __global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, i
         const int *perm = s.perm + l * D;
         const float *bias = s.bias[buf];
         cp_async_wait<0>(); // this layer's weights (issued during the previous layer) have arrived
-        // the a-half of the row as bf16 (columns d..15 zero)
-        {
-            uint32_t w[8];
+        __syncthreads();    // and the previous layer's coupling (the row owners' Y) is complete
+        { // the a-half of the row as bf16 (columns d..15 zero): columns 8 half .. 8 half + 7
+            uint32_t w[4];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const float lo = (2 * j < d) ? Y[perm[2 * j]] : 0.f, hi = (2 * j + 1 < d) ? Y[perm[2 * j + 1]] : 0.f;
+            for (int j = 0; j < 4; ++j) {
+                const int k = 8 * half + 2 * j;
+                const float lo = (k < d) ? Y[perm[k]] : 0.f, hi = (k + 1 < d) ? Y[perm[k + 1]] : 0.f;
                 w[j] = pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
             }
-            unsigned char *a1 = (unsigned char *)s.A1;
-            *(uint4 *)(a1 + canon_off(t, 0, 16)) = make_uint4(w[0], w[1], w[2], w[3]);
-            *(uint4 *)(a1 + canon_off(t, 8, 16)) = make_uint4(w[4], w[5], w[6], w[7]);
+            *(uint4 *)((unsigned char *)s.A1 + canon_off(rl, 8 * half, 16)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
         tc_handoff();
         if (step + 1 < f.L) { // the other buffer was last read by the previous layer's MMAs, which have completed
@@ -846,7 +871,7 @@ __global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, i
         phase ^= 1;
         if (!ok) { break; }
         tc_fence_after();
-        tc_hidden_epilogue(s, tlane, 0, bias, t);
+        tc_hidden_epilogue(s, tlane, 0, 64 * half, bias, rl);
         tc_handoff();
         // h2
         if (t == 0) {
@@ -860,7 +885,7 @@ __global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, i
         phase ^= 1;
         if (!ok) { break; }
         tc_fence_after();
-        tc_hidden_epilogue(s, tlane, 128, bias + FLOW_H, t);
+        tc_hidden_epilogue(s, tlane, 128, 64 * half, bias + FLOW_H, rl);
         tc_handoff();
         // o
         if (t == 0) {
@@ -874,29 +899,32 @@ __global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, i
         phase ^= 1;
         if (!ok) { break; }
         tc_fence_after();
-        float *O = s.O + t * FTC_LDY; // o of the row (indexed by the runtime half width d)
-        for (int c = 0; c < 32; c += 16) {
-            float v[16];
-            tmem_ld16(tlane + (uint32_t)c, v);
+        if (owner) {
+            float *O = s.O + rl * FTC_LDY; // o of the row (indexed by the runtime half width d)
+            {
+                uint32_t r[32];
+                tmem_ld32_nowait(tlane, r);
+                tmem_ld_wait();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) { O[c + j] = v[j] + bias[2 * FLOW_H + c + j]; }
-        }
-        // coupling of the row
-        float *tp = (f.tape && live) ? f.tape + ((int64_t)l * f.n + row) * 4 * d : nullptr;
-        for (int j = 0; j < d; ++j) {
-            const float sj = soft_clamp(O[j]);
-            const float tv = O[d + j];
-            const int pb = perm[d + j];
-            const float bin = Y[pb];
-            const float bout = (f.dir == 0) ? fmaf(bin, __expf(sj), tv) : (bin - tv) * __expf(-sj);
-            if (tp) {
-                tp[j] = Y[perm[j]];
-                tp[d + j] = bout;
-                tp[2 * d + j] = sj;
-                tp[3 * d + j] = tv;
+                for (int j = 0; j < 32; ++j) { O[j] = __uint_as_float(r[j]) + bias[2 * FLOW_H + j]; }
             }
-            Y[pb] = bout;
-            logdet += sj;
+            // coupling of the row
+            float *tp = (f.tape && live) ? f.tape + ((int64_t)l * f.n + row) * 4 * d : nullptr;
+            for (int j = 0; j < d; ++j) {
+                const float sj = soft_clamp(O[j]);
+                const float tv = O[d + j];
+                const int pb = perm[d + j];
+                const float bin = Y[pb];
+                const float bout = (f.dir == 0) ? fmaf(bin, __expf(sj), tv) : (bin - tv) * __expf(-sj);
+                if (tp) {
+                    tp[j] = Y[perm[j]];
+                    tp[d + j] = bout;
+                    tp[2 * d + j] = sj;
+                    tp[3 * d + j] = tv;
+                }
+                Y[pb] = bout;
+                logdet += sj;
+            }
         }
     }
     if (!ok && t == 0) { atomicOr(status, 1); }
@@ -904,7 +932,7 @@ __global__ void __launch_bounds__(FTC_ROWS, 1) flow_pass_tc_kernel(FlowArgs f, i
     tc_fence_before();
     __syncthreads();
     if (warp == 0) { tmem_dealloc(taddr, 256); }
-    if (!ok || !live) { return; }
+    if (!ok || !live || !owner) { return; }
     // output and log q of the row
     float ls = 0.f;
     for (int c = 0; c < D; ++c) { ls += f.logsig[c]; }
@@ -1432,7 +1460,7 @@ static int flow_pass_launch(mcig_flow *f, FlowArgs &a, int64_t n, cudaStream_t s
 {
     if (f->tc) {
         const int grid = (int)((n + FTC_ROWS - 1) / FTC_ROWS);
-        flow_pass_tc_kernel<<<grid, FTC_ROWS, sizeof(FlowTcSmem), st>>>(a, f->status);
+        flow_pass_tc_kernel<<<grid, FTC_THREADS, sizeof(FlowTcSmem), st>>>(a, f->status);
     } else {
         const int grid = (int)((n + FLOW_PASS_ROWS - 1) / FLOW_PASS_ROWS);
         flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);

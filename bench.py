@@ -279,7 +279,7 @@ def run_gpu(args):
         "clocks": ck,
     }
     if args.batched:
-        c3 = run_c3(argparse.Namespace(integrals=4096, warmup=1, steps=3))
+        c3 = run_c3(argparse.Namespace(integrals=4096, warmup=1, steps=3, c3_tuning=getattr(args, "c3_tuning", None)))
         line["batched"] = {"workload": c3["metric"], "integrals_per_s": c3["value"], "ms_per_batch": c3["ms_per_step"],
                            "e2e_integrals_per_s": c3["e2e"]["value"], "outer_steps_per_s": c3["outer_steps_per_s"],
                            "config": c3["config"], "accuracy": c3["accuracy"], "clocks": c3["clocks"]}
@@ -409,7 +409,7 @@ def run_c3(args):
         nmcs.append(nmc)
         chains.append(nch)
     b = mcig.Batch(mcis, nmcs)
-    if args.c3_tuning:
+    if getattr(args, "c3_tuning", None):
         v = [int(t) for t in args.c3_tuning.split(",")]
         b.set_tuning(v[0], v[1:5])
         block, unroll = b.tuning()
@@ -621,7 +621,7 @@ def run_c5(args):
             m.addObservable(mcig.OBS_XI, [0], 1, 1, False, mcig.EST_UNCORRELATED)
             if use_flow:
                 f = mcig.Flow(D, 8, 128, seed=6 + it)
-                f.set_tensor_path(args.c5_flow_gemm == "tcgen05")
+                f.set_tensor_path(getattr(args, "c5_flow_gemm", "mma.sync") == "tcgen05")
                 _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=C5_ADAPT,
                                                 batch=nch, lr=3e-3)
                 accs.append(acc)
@@ -641,7 +641,7 @@ def run_c5(args):
     return {"metric": "effective samples/s of <x_1> (C5: 24-D 4-mode mixture, learned flow proposal)",
             "value": res[True][0], "unit": "effective samples/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res[True][1] * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 walker, bf16 flow GEMMs (f32 accumulate)", "flow_gemms": args.c5_flow_gemm,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 walker, bf16 flow GEMMs (f32 accumulate)", "flow_gemms": getattr(args, "c5_flow_gemm", "mma.sync"),
             "data": "synthetic (seeded mixture, random-init flow)",
             "config": {"workload": "C5 learned proposal", "chains": nch, "ndim": D, "nmc": nmc, "flow_layers": 8,
                        "hidden": 128, "period": 5, "adaptation_cycles": C5_ADAPT, "adam_batch": nch,

@@ -594,8 +594,9 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
-// wait for the completion of the mbarrier phase with parity `parity`, at most `limit`
-// polls (about 2^24 x 64 ns = 1 s): false when the limit ran out
+// wait for the completion of the mbarrier phase with parity `parity`: 4,096 polls back to
+// back (an MMA round trip completes within them), then polls 64 ns apart, at most `limit` in
+// all (about 2^24 x 64 ns = 1 s); false when the limit ran out
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t limit = 1u << 24)
 {
     for (uint32_t i = 0; i < limit; ++i) {
@@ -606,7 +607,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32
                      : "r"(mbar), "r"(parity)
                      : "memory");
         if (done) { return true; }
-        __nanosleep(32);
+        if (i >= 4096) { __nanosleep(64); }
     }
     return false;
 }

@@ -1317,8 +1317,7 @@ static int run_estimator(mcig_mci *h, int est, const void *data, int is_float, i
     case MCIG_EST_NOOP: est_noop_kernel<<<grid, block, 0, st>>>(a); break;
     case MCIG_EST_UNCORRELATED:
         if (n < 2) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "[UncorrelatedEstimator] n must be larger than 1"); }
-        if (is_float && S % 4 == 0) { est_uncorr_f32x4_kernel<<<(int)((S / 4 + block - 1) / block), block, 0, st>>>(a); }
-        else if (is_float) { est_uncorr_f32_kernel<<<grid, block, 0, st>>>(a); }
+        if (is_float) { est_uncorr_f32_kernel<<<grid, block, 0, st>>>(a); }
         else { est_uncorr_kernel<<<grid, block, 0, st>>>(a); }
         break;
     case MCIG_EST_FCBLOCKER:

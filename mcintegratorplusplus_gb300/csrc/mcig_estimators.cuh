@@ -101,50 +101,6 @@ static __global__ void est_uncorr_f32_kernel(EstArgs a)
     est_store(a, s, average, e);
 }
 
-// The same estimator, four consecutive series per thread (a.nv * a.nchains a multiple of 4):
-// one 16-byte load per row, 8 rows in flight, the four series' Kahan sums each in sample
-// order, so every series gets est_uncorr_f32_kernel's result bit for bit.
-static __global__ void est_uncorr_f32x4_kernel(EstArgs a)
-{
-    const int64_t S = (int64_t)a.nv * a.nchains;
-    const int64_t s4 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (4 * s4 >= S) { return; }
-    const float4 *d = (const float4 *)a.data + s4;
-    const int64_t stride = S / 4;
-    float s1[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f}, s2[4] = {0.f, 0.f, 0.f, 0.f},
-          c2[4] = {0.f, 0.f, 0.f, 0.f};
-    int64_t i = 0;
-    for (; i + 8 <= a.n; i += 8) {
-        float4 x[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) { x[k] = d[(i + k) * stride]; }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            kahan2(s1[0], c1[0], s2[0], c2[0], x[k].x);
-            kahan2(s1[1], c1[1], s2[1], c2[1], x[k].y);
-            kahan2(s1[2], c1[2], s2[2], c2[2], x[k].z);
-            kahan2(s1[3], c1[3], s2[3], c2[3], x[k].w);
-        }
-    }
-    for (; i < a.n; ++i) {
-        const float4 x = d[i * stride];
-        kahan2(s1[0], c1[0], s2[0], c2[0], x.x);
-        kahan2(s1[1], c1[1], s2[1], c2[1], x.y);
-        kahan2(s1[2], c1[2], s2[2], c2[2], x.z);
-        kahan2(s1[3], c1[3], s2[3], c2[3], x.w);
-    }
-    const double SMALLEST_ERROR = 1.e-300;
-    const double norm = 1. / a.n;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const double average = ((double)s1[q] - (double)c1[q]) * norm;
-        double e = ((double)s2[q] - (double)c2[q]) * norm - average * average;
-        if (a.one_d) { e = (e > SMALLEST_ERROR) ? sqrt(e / (a.n - 1.)) : 0.; }
-        else { e = (e > SMALLEST_ERROR) ? sqrt(e * (1. / (a.n - 1.))) : 0.; }
-        est_store(a, 4 * s4 + q, average, e);
-    }
-}
-
 // The same estimator over rows [i0, i1) of the data, for sampling that runs in chunks:
 // the Kahan sums of each series continue from `state` (zero for i0 == 0) and are saved
 // there, and the chunk that ends at row a.n forms the result.  Every series sees the add

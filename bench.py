@@ -186,6 +186,10 @@ def run_gpu(args):
     m.setSeed(20241203)
     m.setFullStorage(32)
     configure(m, P, args.nmc, args.blocks)
+    if args.c2_kernel == "one-lane":
+        m.setKernel(2)
+    elif args.c2_kernel == "pair":
+        m.setLanes(2)
     nod = m.getNObsDim()
     # pinned host buffers: initial walkers in, averages / errors out
     x0 = torch.zeros((nchains, NDIM), dtype=torch.float64).pin_memory()
@@ -606,6 +610,9 @@ def run_c5(args):
     x_1 from MJBlocker and Sokal's window on 256 chains' series.  Metric: ESS/s with the flow."""
     import mcintegratorplusplus_gb300 as mcig
     D, nch, nmc = 24, args.chains5, args.nmc5
+    adapt = getattr(args, "c5_adapt", None) or C5_ADAPT
+    batch = getattr(args, "c5_batch", None) or nch
+    lanes = getattr(args, "c5_lanes", 0) or 0
     params, means, var_x1 = c5_target()
     res = {}
     for use_flow in (False, True):
@@ -618,12 +625,14 @@ def run_c5(args):
             m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
             m.setNdecorrelationSteps(1000)
             m.setFullStorage(32)
+            if lanes:
+                m.setLanes(lanes)
             m.addObservable(mcig.OBS_XI, [0], 1, 1, False, mcig.EST_UNCORRELATED)
             if use_flow:
                 f = mcig.Flow(D, 8, 128, seed=6 + it)
                 f.set_tensor_path(getattr(args, "c5_flow_gemm", "mma.sync") == "tcgen05")
-                _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=C5_ADAPT,
-                                                batch=nch, lr=3e-3)
+                _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=adapt,
+                                                batch=batch, lr=3e-3)
                 accs.append(acc)
             else:
                 m.integrate(nmc)
@@ -644,7 +653,7 @@ def run_c5(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 walker, bf16 flow GEMMs (f32 accumulate)", "flow_gemms": getattr(args, "c5_flow_gemm", "mma.sync"),
             "data": "synthetic (seeded mixture, random-init flow)",
             "config": {"workload": "C5 learned proposal", "chains": nch, "ndim": D, "nmc": nmc, "flow_layers": 8,
-                       "hidden": 128, "period": 5, "adaptation_cycles": C5_ADAPT, "adam_batch": nch,
+                       "hidden": 128, "period": 5, "adaptation_cycles": adapt, "adam_batch": batch,
                        "adam_lr": 3e-3, "refresh": 4096},
             "plain_mh": {"value": res[False][0], "ms_per_step": res[False][1] * 1e3, "ess": res[False][2],
                          "phases": res[False][4], "ess_detail": res[False][5]},
@@ -698,6 +707,8 @@ def main():
                     help="skip the learned-proposal comparison added to the default line")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the uneven-batch (C3) figures added to the default line")
+    ap.add_argument("--c2-kernel", default="auto", choices=["auto", "one-lane", "pair"],
+                    help="C2 burn-in and sampling kernel: the library's choice, one lane or two lanes per chain")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "c2_parts"])
     ap.add_argument("--integrals", type=int, default=4096)
     ap.add_argument("--c3-tuning", default=None,
@@ -706,6 +717,10 @@ def main():
     ap.add_argument("--nmc4", type=int, default=65536)
     ap.add_argument("--chains5", type=int, default=16384)
     ap.add_argument("--nmc5", type=int, default=8192)
+    ap.add_argument("--c5-adapt", type=int, default=None, help="adaptation cycles of the flow (default C5_ADAPT)")
+    ap.add_argument("--c5-batch", type=int, default=None, help="rows per Adam step of the flow (default: all chains)")
+    ap.add_argument("--c5-lanes", type=int, default=0, choices=[0, 4, 8],
+                    help="lanes per chain of the local Metropolis steps in both C5 arms (0: one lane)")
     ap.add_argument("--c5-flow-gemm", default="mma.sync", choices=["tcgen05", "mma.sync"],
                     help="tensor-core path of the flow's passes (the backward pass is mma.sync)")
     args = ap.parse_args()

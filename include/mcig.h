@@ -76,7 +76,19 @@ int mcig_set_phase_fusion(mcig_mci *h, int on);
  * whose MCI::findMRT2Step (src/MCIntegrator.cpp:87-168) calibrates one chain. */
 int mcig_set_calibration_split(mcig_mci *h, int on);
 
-/* Multi-lane mixture kernel (default 0: off): with lpc = 4 or 8, a float handle whose single
+/* Multi-lane kernels.  lpc = 0 (default): automatic, i.e. two lanes per chain for the
+ * configurations of lpc = 2 with at most 32,768 chains, else one; lpc = 1: one lane per chain.
+ * lpc = 2: a float handle with one exp(-x.x) or precision-matrix sampling function in 9..16
+ * coordinates (all-coordinate uniform or Gaussian move, one step type, unbound domain,
+ * observables without exp() or coordinate blocks) runs burn-in and sampling (and the
+ * calibration when its split tail is off) with 2 lanes per chain: lane group l draws and
+ * moves coordinates [8l, 8l+8), the proposal is gathered with warp shuffles and each lane
+ * forms 8 rows of U x (mcig_pair.cuh).  Results are bit-identical to the one-lane kernel;
+ * the point is latency hiding where one lane per chain leaves few warps per SM (16,384
+ * chains: 3.4 warps per SM with one lane at 124 registers, 6.7 with two at 72 registers;
+ * measured sampling launch 18.9 against 23.9 ms; at 65,536 chains the one-lane kernel is
+ * faster, 35.8 against 41.5 ms).
+ * lpc = 4 or 8: a float handle whose single
  * sampling function is a mixture of at most 8 Gaussians (17..32 coordinates, all-coordinate
  * uniform or Gaussian move, one step type, unbound domain) runs its calibration, burn-in and
  * sampling with lpc lanes per chain: lane group l draws and moves coordinates [l*ndim/lpc,

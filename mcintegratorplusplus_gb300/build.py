@@ -33,6 +33,8 @@ UNITS = {
     "mcig_flow": [],
     "sample_batch": [],
     "sample_lanes": [],
+    "sample_pair": [],
+    "flow_accept": [],
 }
 
 

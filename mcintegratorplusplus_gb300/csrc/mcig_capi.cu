@@ -1152,15 +1152,47 @@ static bool lanes_eligible(const mcig_mci *h)
     return true;
 }
 
-// the kernel family a launch of kp runs: 2 the multi-lane mixture kernel, 1 the
-// register-resident one-lane kernel, 0 the general kernel (or a plugin's)
+// Chain counts up to which the two-lane kernel serves its configurations by default.  One lane
+// per chain fills an SM with nchains / 152 / 32 warps (3.4 at 16,384 chains, 13.5 at 65,536):
+// measured on a 16-D precision-matrix target with x.x and x_i in Block and Full accumulators,
+// the two-lane sampling launch took 18.9 ms against 23.9 ms at 16,384 chains and 41.5 ms
+// against 35.8 ms at 65,536 chains.
+#define MCIG_PAIR_AUTO_CHAINS 32768
+
+// the two-lane kernel (mcig_pair.cuh) serves float walkers with an all-coordinate uniform or
+// Gaussian move, one step type, the unbound domain, one exp(-x.x) or precision-matrix
+// sampling function, 9..16 coordinates and observables without exp() or coordinate blocks
+static bool pair_eligible(const mcig_mci *h)
+{
+    if (uses_plugin(h) || h->prec == MCIG_PREC_FP64 || h->replay || h->periodic) { return false; }
+    if (h->ndim < 9 || h->ndim > 16 || h->movetype != MCIG_MOVE_ALL || h->ntypes != 1) { return false; }
+    if (h->srrd != MCIG_SRRD_UNIFORM && h->srrd != MCIG_SRRD_GAUSSIAN) { return false; }
+    if (h->pdfs.size() != 1) { return false; }
+    const int k = h->pdfs[0].kind;
+    if (k != MCIG_PDF_GAUSS && k != MCIG_PDF_GAUSS_SUM && k != MCIG_PDF_GAUSS_PREC) { return false; }
+    for (auto &o : h->obs) {
+        if (o.kind == MCIG_OBS_GAUSSX2 || o.kind == MCIG_OBS_X2BLOCK || o.kind >= MCIG_OBS_USER) { return false; }
+    }
+    return true;
+}
+
+// the kernel family a launch of kp runs: 3 the two-lane kernel, 2 the multi-lane mixture
+// kernel, 1 the register-resident one-lane kernel, 0 the general kernel (or a plugin's)
 static int kernel_family(const mcig_mci *h, const KParams &kp)
 {
     const bool small_n = kp.nsteps < ((int64_t)1 << 31); // 32-bit step counters in the register-resident kernels
+    // two lanes per chain for burn-in and sampling (and calibration when its split tail is
+    // off): mcig_set_lanes(h, 2), or automatically below MCIG_PAIR_AUTO_CHAINS chains, where
+    // one lane per chain leaves the SMs with too few warps to hide latency
+    const bool want_pair = h->lanes == 2 || (h->lanes == 0 && h->nchains <= MCIG_PAIR_AUTO_CHAINS);
+    if (kp.ndump == 0 && kp.mode != KMODE_FUSED && h->kernel_policy == 0 && want_pair && small_n &&
+        pair_eligible(h) && !(kp.mode == KMODE_CALIB && h->calib_split)) {
+        return 3;
+    }
     // several lanes per chain: the calibration, burn-in and sampling launches of the mixture
     // configurations it serves, when asked for (mcig_set_lanes, or kernel policy 3)
     const bool want_lanes = kp.ndump == 0 && kp.mode != KMODE_FUSED &&
-                            (h->kernel_policy == 3 || (h->kernel_policy == 0 && h->lanes > 0));
+                            (h->kernel_policy == 3 || (h->kernel_policy == 0 && (h->lanes == 4 || h->lanes == 8)));
     if (want_lanes && small_n && lanes_eligible(h)) { return 2; }
     // file output is recorded by the general kernel
     const bool fast = kp.ndump == 0 && (h->kernel_policy == 2 || (h->kernel_policy == 0 && fast_eligible(h) && small_n));
@@ -1170,6 +1202,16 @@ static int kernel_family(const mcig_mci *h, const KParams &kp)
 static int launch(mcig_mci *h, const KParams &kp)
 {
     const int family = kernel_family(h, kp);
+    if (family == 3) {
+        if (h->f64_decide) { return set_err(MCIG_ERR_UNSUPPORTED, "the FP64-certified decision runs in the multi-lane mixture kernel only (mcig_set_lanes)"); }
+        const int k = h->pdfs[0].kind;
+        mcig_launch_fn pf = mcig_pair_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, k == MCIG_PDF_GAUSS_PREC ? 2 : 1);
+        if (!pf) { return set_err(MCIG_ERR_UNSUPPORTED, "no two-lane kernel for this configuration"); }
+        pf(kp, &h->fc, h->movetype, 0, 0, 0, h->stream);
+        ++h->launches;
+        CK(cudaGetLastError());
+        return MCIG_OK;
+    }
     if (family == 2) {
         mcig_launch_fn lf = mcig_lanes_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, 32, h->lanes > 0 ? h->lanes : 8);
         if (!lf) { return set_err(MCIG_ERR_UNSUPPORTED, "no multi-lane kernel for %d lanes per chain", h->lanes); }
@@ -1237,7 +1279,9 @@ extern "C" int mcig_set_calibration_split(mcig_mci *h, int on)
 extern "C" int mcig_set_lanes(mcig_mci *h, int lpc)
 {
     if (!h) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "handle is NULL"); }
-    if (lpc != 0 && lpc != 4 && lpc != 8) { return set_err(MCIG_ERR_INVALID_ARGUMENT, "lanes per chain must be 0, 4 or 8"); }
+    if (lpc < 0 || lpc > 8 || (lpc > 2 && lpc != 4 && lpc != 8)) {
+        return set_err(MCIG_ERR_INVALID_ARGUMENT, "lanes per chain must be 0, 1, 2, 4 or 8");
+    }
     h->lanes = lpc;
     return MCIG_OK;
 }
@@ -2213,7 +2257,6 @@ int mcig_flow_density_cmf_device(mcig_flow *f, const float *in_cmf, int64_t nstr
                                  cudaStream_t st);
 int mcig_flow_check_status(mcig_flow *f, cudaStream_t st);
 
-enum { TAG_FLOW_ACCEPT = 4 }; // (the proposal's z uses tag 3 in the generative pass)
 
 // walkers [ndim][nchains] (double) -> rows [nchains][ndim] (float)
 __global__ void walkers_to_rows_kernel(const double *x, int ndim, int nc, float *out)
@@ -2316,6 +2359,15 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
         sp.obs[o].nstore = h->obs_nstore[o];
     }
     uint64_t cycle = 0;
+    // the test with the sampling function's log density as straight-line code where the
+    // register-resident kernel has it (one exp(-x.x), precision-matrix or mixture function)
+    mcig_flow_accept_fn fast_accept = nullptr;
+    if (h->pdfs.size() == 1) {
+        const PdfDef &d = h->pdfs[0];
+        const int pk = (d.kind == MCIG_PDF_GAUSS || d.kind == MCIG_PDF_GAUSS_SUM) ? 1 :
+                       (d.kind == MCIG_PDF_GAUSS_PREC ? 2 : ((d.kind == MCIG_PDF_GAUSS_MIX && (int)d.params[0] <= 8) ? 3 : 0));
+        if (pk && h->ndim <= 32) { fast_accept = mcig_flow_accept_launcher(maxd_bucket(h->ndim), pk); }
+    }
     // one independence proposal for every chain; krow = Full row to record, -1 none
     // log q of the current walkers and of the proposals both come from the density pass, one
     // deterministic function, so the Metropolis-Hastings ratio uses the same q on both sides
@@ -2329,7 +2381,11 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
             (r = mcig_flow_density_cmf_device(f, xprop.p, (int64_t)nc, (int64_t)nc, lq_prop.p, h->stream))) {
             return r;
         }
-        flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p);
+        if (fast_accept) {
+            fast_accept(sp, &h->fc, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p, h->stream);
+        } else {
+            flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p);
+        }
         h->launches += 4;
         CK(cudaGetLastError());
         ++cycle;

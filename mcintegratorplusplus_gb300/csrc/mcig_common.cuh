@@ -21,7 +21,10 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
 #include <cuda_runtime.h>
 
 #include "../../include/mcig_types.h"
@@ -33,6 +36,29 @@
 #define MCIG_MAXDIM 64
 #define MCIG_FAST_BLOCK 64 // threads per block of the register-resident kernel (slot stride)
 #define MCIG_FCONST 2080 // floats of sampling-function data in the parameter block (register-resident kernel)
+
+// Shared-memory attributes of kernel k on the current device, set through the runtime once
+// per kernel and device (they persist for the process): the carveout at its maximum, and the
+// dynamic shared-memory limit raised whenever a launch asks for more than any before it.
+// Loops of short launches (the learned proposal's local steps) would otherwise spend host
+// time on attribute calls at every launch.
+inline void mcig_smem_attrs(const void *k, size_t smem)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> limit; // (kernel, device) -> dynamic limit set
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(mu);
+    auto it = limit.find(std::make_pair(k, dev));
+    if (it == limit.end()) {
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        it = limit.emplace(std::make_pair(k, dev), (size_t)48 * 1024).first;
+    }
+    if (smem > it->second) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        it->second = smem;
+    }
+}
 
 enum { RNG_PHILOX = 0, RNG_TAPE = 1 };
 // KMODE_FUSED (register-resident kernel): calibration (MIN_STAT fuse_calib, none if 0), burn-in

@@ -516,7 +516,6 @@ void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, i
 {
     auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK>;
     // shared memory as large as possible, so the accumulator slots never limit residency
-    cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-    if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
+    mcig_smem_attrs((const void *)k, smem);
     k<<<grid, block, smem, st>>>(p, *fc);
 }

@@ -511,8 +511,7 @@ void mcig_lanes_launch(const KParams &p0, const FastConst *fc, int /*movetype*/,
         ns += (p.obs[o].kind == MCIG_OBS_XND || p.obs[o].kind == MCIG_OBS_X2) ? MAXD / LPC : 1;
     }
     const size_t smem = mcig_lanes_smem<MAXD, LPC>(p, KAHAN);
-    cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-    if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
+    mcig_smem_attrs((const void *)k, smem);
     const int64_t threads = (int64_t)p.nchains * LPC;
     const int grid = (int)((threads + MCIG_FAST_BLOCK - 1) / MCIG_FAST_BLOCK);
     k<<<grid, MCIG_FAST_BLOCK, smem, st>>>(p, *fc);

@@ -25,6 +25,19 @@ mcig_launch_fn mcig_calib_launcher_pk16(int pk);
 // lanes per chain; NULL otherwise
 mcig_launch_fn mcig_lanes_launcher(int kahan, int maxd, int lpc);
 
+// float kernel with two lanes per chain for one sampling function of kind pk (PK_GAUSS or
+// PK_PREC) in 9..16 coordinates (mcig_pair.cuh): all-coordinate move, one step type,
+// unbound domain; NULL otherwise
+mcig_launch_fn mcig_pair_launcher(int kahan, int pk);
+
+// Metropolis-Hastings test of the learned proposal for one sampling function of kind pk
+// (PK_GAUSS, PK_PREC or PK_MIX) at maxd 8, 16 or 32 (flow_accept.cu); NULL otherwise
+typedef void (*mcig_flow_accept_fn)(const KParams &p, const FastConst *fc, const float *xprop, const float *lq_prop,
+                                    const float *lq_cur, uint64_t cycle, int64_t krow, int64_t *nacc_flow, cudaStream_t st);
+mcig_flow_accept_fn mcig_flow_accept_launcher(int maxd, int pk);
+// Philox tag of the flow's accept draw (tag 3: the proposal's z in the generative pass)
+enum { TAG_FLOW_ACCEPT = 4 };
+
 // general kernel of a plugin (include/mcig/plugin.cuh) over its user functors: launches and
 // returns the launch's cudaError_t of the plugin's own CUDA runtime
 typedef int (*mcig_plugin_launch_fn)(const KParams &p, int movetype, int grid, int block, size_t smem, cudaStream_t st);

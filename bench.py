@@ -630,7 +630,7 @@ def run_c5(args):
             m.addObservable(mcig.OBS_XI, [0], 1, 1, False, mcig.EST_UNCORRELATED)
             if use_flow:
                 f = mcig.Flow(D, 8, 128, seed=6 + it)
-                f.set_tensor_path(getattr(args, "c5_flow_gemm", "mma.sync") == "tcgen05")
+                f.set_tensor_path({"mma.sync": 0, "tcgen05": 1, "mma.sync-smem": 2}[getattr(args, "c5_flow_gemm", "mma.sync")])
                 _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=adapt,
                                                 batch=batch, lr=3e-3)
                 accs.append(acc)
@@ -721,7 +721,7 @@ def main():
     ap.add_argument("--c5-batch", type=int, default=None, help="rows per Adam step of the flow (default: all chains)")
     ap.add_argument("--c5-lanes", type=int, default=0, choices=[0, 4, 8],
                     help="lanes per chain of the local Metropolis steps in both C5 arms (0: one lane)")
-    ap.add_argument("--c5-flow-gemm", default="mma.sync", choices=["tcgen05", "mma.sync"],
+    ap.add_argument("--c5-flow-gemm", default="mma.sync", choices=["tcgen05", "mma.sync", "mma.sync-smem"],
                     help="tensor-core path of the flow's passes (the backward pass is mma.sync)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -262,8 +262,11 @@ int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n);
  * inputs (raw 16-bit patterns) and f32 accumulation, one CTA.  n, k multiples of 16 in
  * [16, 256].  MCIG_ERR_TIMEOUT when the MMA's completion was not seen within the bounded wait. */
 int mcig_flow_tc_selftest(int device, const uint16_t *a, const uint16_t *b, int n, int k, float *d);
-/* the flow's passes (proposals, densities, training's density pass) on tcgen05 (1) or on
- * mma.sync (0); both agree with the oracle at bf16 tolerance */
+/* the kernel of the flow's passes (proposals, densities, training's density pass): 0 (default)
+ * register-fused mma.sync (one warp carries 16 rows through every layer with the hidden
+ * activations in registers; two row sets per launch for the learned proposal's densities),
+ * 1 tcgen05 with TMEM accumulators, 2 mma.sync with the hidden activations in shared memory.
+ * 0 and 2 give the same numbers bit for bit; all three agree with the oracle at bf16 tolerance */
 int mcig_flow_set_tensor_path(mcig_flow *f, int tc);
 /* generative direction: x = f(z) and log q(x) for z[n][ndim] (host arrays) */
 int mcig_flow_forward(mcig_flow *f, const double *z, int64_t n, double *x, double *logq);

@@ -2256,6 +2256,8 @@ int mcig_flow_propose_device(mcig_flow *f, uint64_t cycle, uint32_t key0, uint32
 int mcig_flow_density_cmf_device(mcig_flow *f, const float *in_cmf, int64_t nstride, int64_t n, float *d_logq,
                                  cudaStream_t st);
 int mcig_flow_check_status(mcig_flow *f, cudaStream_t st);
+int mcig_flow_density2_device(mcig_flow *f, const double *in_cm, const float *in_cmf_b, int64_t nstride, int64_t n,
+                              float *logq_a, float *logq_b, cudaStream_t st);
 
 
 // walkers [ndim][nchains] (double) -> rows [nchains][ndim] (float)
@@ -2373,12 +2375,13 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     // deterministic function, so the Metropolis-Hastings ratio uses the same q on both sides
     // (the generative pass's own log q of x' differs from it by the bf16 rounding of its MLP
     // inputs); the proposal's z is drawn inside the generative pass
+    // (the density of the walkers and of the proposals in one launch where the pass kernel
+    // takes two row sets)
     auto flow_cycle = [&](int64_t krow) -> int {
         int r;
-        if ((r = mcig_flow_pass_device_cm(f, 1, nullptr, h->x.p, (int64_t)nc, (int64_t)nc, nullptr, lq_cur.p, h->stream)) ||
-            (r = mcig_flow_propose_device(f, cycle, kp.key0 ^ 0x6A09E667u, kp.key1 ^ 0xBB67AE85u, (int64_t)nc, (int64_t)nc,
+        if ((r = mcig_flow_propose_device(f, cycle, kp.key0 ^ 0x6A09E667u, kp.key1 ^ 0xBB67AE85u, (int64_t)nc, (int64_t)nc,
                                           xprop.p, lq_prop.p, h->stream)) ||
-            (r = mcig_flow_density_cmf_device(f, xprop.p, (int64_t)nc, (int64_t)nc, lq_prop.p, h->stream))) {
+            (r = mcig_flow_density2_device(f, h->x.p, xprop.p, (int64_t)nc, (int64_t)nc, lq_cur.p, lq_prop.p, h->stream))) {
             return r;
         }
         if (fast_accept) {

@@ -85,6 +85,11 @@ struct FlowArgs {
     float *out_cm;
     int64_t cm_stride;
     const float *in_cmf;      // chain-minor float input in_cmf[c * cm_stride + row] (replaces in)
+    // a second set of nb rows after the n rows above (register-fused pass, density direction,
+    // no out / tape): row n + r reads in_cmf_b[c * cm_stride + r], its log q goes to logq_b[r]
+    int nb;
+    const float *in_cmf_b;
+    float *logq_b;
     // generative direction: z drawn in the kernel (replaces in): coordinate i of row r is
     // Box-Muller normal i % 4 of Philox block (zcycle lo, zcycle hi, r, FLOW_TAG_Z << 12 | i / 4)
     // with key (zk0, zk1)
@@ -109,6 +114,7 @@ __device__ __forceinline__ float flow_z_value(const FlowArgs &f, int row, int i)
 // input value of row r (in the whole set), coordinate c, from whichever source the pass reads
 __device__ __forceinline__ float flow_input(const FlowArgs &f, int r, int c)
 {
+    if (r >= f.n) { return f.in_cmf_b[(int64_t)c * f.cm_stride + (r - f.n)]; }
     if (f.zgen) { return flow_z_value(f, r, c); }
     if (f.in_cm) { return (float)f.in_cm[(int64_t)c * f.cm_stride + r]; }
     if (f.in_cmf) { return f.in_cmf[(int64_t)c * f.cm_stride + r]; }
@@ -390,7 +396,8 @@ __device__ __forceinline__ void load_tile_async(__nv_bfloat16 *dst, int ld, cons
 // the generative-direction weights of one layer and its biases b1, b2 (float, 16-byte
 // aligned in the parameter vector) into buffer buf, as one copy group; b3 (2d floats)
 // is copied with plain loads
-__device__ __forceinline__ void load_layer_weights_async(FlowSmem &s, const __nv_bfloat16 *wl, const float *P, int d, int buf)
+template <class S>
+__device__ __forceinline__ void load_layer_weights_async(S &s, const __nv_bfloat16 *wl, const float *P, int d, int buf)
 {
     load_tile_async<16>(s.W1n[buf], LDA_S, wl + WB_W1N, FLOW_H);
     load_tile_async<FLOW_H>(s.W2n[buf], LDH_S, wl + WB_W2N, FLOW_H);
@@ -538,6 +545,204 @@ __global__ void __launch_bounds__(FLOW_PASS_THREADS, 1) flow_pass_kernel(FlowArg
         for (int i = threadIdx.x; i < D * FLOW_PASS_ROWS; i += blockDim.x) {
             const int c = i / FLOW_PASS_ROWS, r = i % FLOW_PASS_ROWS;
             if (r < rows) { f.out_cm[(int64_t)c * f.cm_stride + base + r] = s.Y[r][c]; }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// register-fused pass: one warp carries 16 rows through every layer, activations in registers
+// ------------------------------------------------------------------------
+// The m16n8k16 accumulator fragment of two adjacent 8-column tiles (thread: rows g, g + 8,
+// columns 2t, 2t + 1 of each) is, converted to bf16, the A fragment of one 16-wide k slice of
+// the next product (rows g, g + 8, k 2t, 2t + 1 and 8 + 2t, 9 + 2t).  So a warp forms
+// h1 = relu(a W1 + b1) for its 16 rows in all 128 columns, turns it into the A fragments of
+// the second product without a shared-memory round trip, does the same with h2 for the
+// third, and only the layer output o = (s, t) (16 x 32 floats) passes through shared memory
+// for the coupling.  Warps never wait on one another inside a layer: the block meets once per
+// layer to switch the double-buffered weights (prefetched with cp.async, as in
+// flow_pass_kernel).  Without the hidden tiles in shared memory a CTA holds up to 16 warps
+// (256 rows), so two row sets (the density of the walkers and of the proposals) run in one
+// launch with the SMs' warps doubled.  The products and their roundings are those of
+// flow_pass_kernel (same bf16 operands, same k order per output), element for element.
+#define FLOW_FUSED_MAXW 16
+struct FlowFusedSmem {
+    __nv_bfloat16 W1n[2][FLOW_H * LDA_S];
+    __nv_bfloat16 W2n[2][FLOW_H * LDH_S];
+    __nv_bfloat16 W3n[2][32 * LDH_S];
+    float bias[2][2 * FLOW_H + 32];
+    int perm[FLOW_MAXL * FLOW_MAXD];
+    float Y[FLOW_FUSED_MAXW * 16][FLOW_MAXD + 1]; // the rows' coordinates
+    float O[FLOW_FUSED_MAXW][16][FLOW_MAXD + 1];  // each warp's layer output, then s
+    float logdet[FLOW_FUSED_MAXW * 16];
+};
+
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi)
+{
+    return pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
+}
+
+// C[16 x 8 NT] += A[16 x 16 KS] B: A as register fragments (one x4 per k slice), B "n-major"
+// in shared memory (element (k, n) at Bn[n * ldb + k]) through ldmatrix, as warp_gemm
+template <int KS, int NT>
+__device__ __forceinline__ void frag_gemm(const uint32_t (&a)[KS][4], const __nv_bfloat16 *Bn, int ldb, float (&acc)[NT][4])
+{
+    const int lane = threadIdx.x & 31, mi = lane >> 3, rr = lane & 7;
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks) {
+#pragma unroll
+        for (int nt = 0; nt < NT; nt += 2) {
+            uint32_t b0, b1, b2, b3;
+            ldmatrix_x4(b0, b1, b2, b3, Bn + ((nt + (mi >> 1)) * 8 + rr) * ldb + ks * 16 + (mi & 1) * 8);
+            mma_bf16(acc[nt], a[ks][0], a[ks][1], a[ks][2], a[ks][3], b0, b1);
+            mma_bf16(acc[nt + 1], a[ks][0], a[ks][1], a[ks][2], a[ks][3], b2, b3);
+        }
+    }
+}
+
+// relu(acc + bias) of the 128 columns as bf16 A fragments of the next product (8 k slices)
+__device__ __forceinline__ void frag_relu_to_a(const float (&acc)[16][4], const float *bias, uint32_t (&h)[8][4])
+{
+    const int t = threadIdx.x & 3;
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+        const int c0 = 16 * kk + 2 * t, c1 = c0 + 8;
+        const float *x0 = acc[2 * kk], *x1 = acc[2 * kk + 1];
+        h[kk][0] = pack_bf2(fmaxf(x0[0] + bias[c0], 0.f), fmaxf(x0[1] + bias[c0 + 1], 0.f));
+        h[kk][1] = pack_bf2(fmaxf(x0[2] + bias[c0], 0.f), fmaxf(x0[3] + bias[c0 + 1], 0.f));
+        h[kk][2] = pack_bf2(fmaxf(x1[0] + bias[c1], 0.f), fmaxf(x1[1] + bias[c1 + 1], 0.f));
+        h[kk][3] = pack_bf2(fmaxf(x1[2] + bias[c1], 0.f), fmaxf(x1[3] + bias[c1 + 1], 0.f));
+    }
+}
+
+__global__ void __launch_bounds__(FLOW_FUSED_MAXW * 32, 1) flow_pass_fused_kernel(FlowArgs f)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FlowFusedSmem &s = *(FlowFusedSmem *)smem_raw;
+    const int rows_cta = 16 * (int)(blockDim.x >> 5);
+    const int base = blockIdx.x * rows_cta;
+    const int ntot = f.n + f.nb;
+    const int D = f.D, d = f.d;
+    const int rows = min(rows_cta, ntot - base);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3, r0 = warp * 16;
+    const float invd = 1.f / (float)d;
+    for (int i = threadIdx.x; i < D * rows_cta; i += blockDim.x) { // coordinate-major: coalesced over the rows
+        const int c = i / rows_cta, r = i % rows_cta;
+        float v = 0.f;
+        if (r < rows) {
+            if (f.in_cm || f.in_cmf || f.zgen || base + r >= f.n) { v = flow_input(f, base + r, c); }
+            else { v = f.in[(int64_t)(base + r) * D + c]; }
+        }
+        if (f.dir == 1) { v = (v - f.mu[c]) * __expf(-f.logsig[c]); } // density: undo the base affine first
+        s.Y[r][c] = v;
+    }
+    for (int i = threadIdx.x; i < rows_cta; i += blockDim.x) { s.logdet[i] = 0.f; }
+    for (int i = threadIdx.x; i < f.L * D; i += blockDim.x) { s.perm[i] = f.perm[i]; }
+    auto layer_of = [&](int step) { return (f.dir == 0) ? step : f.L - 1 - step; };
+    auto params_of = [&](int step) { return f.theta + (int64_t)layer_of(step) * f.pstride; };
+    load_layer_weights_async(s, f.wb + (int64_t)layer_of(0) * f.wstride, params_of(0), d, 0);
+    float (*O)[FLOW_MAXD + 1] = s.O[warp];
+    for (int step = 0; step < f.L; ++step) {
+        const int l = layer_of(step);
+        const int buf = step & 1;
+        const int *perm = s.perm + l * D;
+        cp_async_wait<0>(); // this layer's weights and biases (issued during the previous layer) have arrived
+        __syncthreads();    // ... for every thread; and every warp has left the previous layer
+        if (step + 1 < f.L) {
+            load_layer_weights_async(s, f.wb + (int64_t)layer_of(step + 1) * f.wstride, params_of(step + 1), d, buf ^ 1);
+        }
+        const float *bias = s.bias[buf];
+        uint32_t h[8][4];
+        { // h1: the a-half (columns d..15 zero) as the A fragment of one k slice
+            uint32_t a[1][4];
+            const int ca = 2 * t4, cb = 8 + 2 * t4;
+            const float *ya = s.Y[r0 + g], *yb = s.Y[r0 + g + 8];
+            auto av = [&](const float *y, int c) { return c < d ? y[perm[c]] : 0.f; };
+            a[0][0] = pack_bf2(av(ya, ca), av(ya, ca + 1));
+            a[0][1] = pack_bf2(av(yb, ca), av(yb, ca + 1));
+            a[0][2] = pack_bf2(av(ya, cb), av(ya, cb + 1));
+            a[0][3] = pack_bf2(av(yb, cb), av(yb, cb + 1));
+            float acc[16][4];
+            zero_acc(acc);
+            frag_gemm<1, 16>(a, s.W1n[buf], LDA_S, acc);
+            frag_relu_to_a(acc, bias, h);
+        }
+        { // h2
+            float acc[16][4];
+            zero_acc(acc);
+            frag_gemm<8, 16>(h, s.W2n[buf], LDH_S, acc);
+            frag_relu_to_a(acc, bias + FLOW_H, h);
+        }
+        { // o = h2 W3 + b3 (32 columns; 2d used)
+            float acc[4][4];
+            zero_acc(acc);
+            frag_gemm<8, 4>(h, s.W3n[buf], LDH_S, acc);
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int c = nt * 8 + 2 * t4;
+                O[g][c] = acc[nt][0] + bias[2 * FLOW_H + c];
+                O[g][c + 1] = acc[nt][1] + bias[2 * FLOW_H + c + 1];
+                O[g + 8][c] = acc[nt][2] + bias[2 * FLOW_H + c];
+                O[g + 8][c + 1] = acc[nt][3] + bias[2 * FLOW_H + c + 1];
+            }
+        }
+        __syncwarp();
+        // coupling of the warp's 16 rows x d columns, (row, column) pairs spread over its lanes
+        for (int i = lane; i < 16 * d; i += 32) {
+            const int q = (int)(((float)i + 0.5f) * invd);
+            const int r = r0 + q, j = i - q * d;
+            const float sj = soft_clamp(O[q][j]);
+            const float tj = O[q][d + j];
+            const int pb = perm[d + j];
+            const float bin = s.Y[r][pb];
+            const float bout = (f.dir == 0) ? fmaf(bin, __expf(sj), tj) : (bin - tj) * __expf(-sj);
+            if (f.tape && r < rows) {
+                float *tp = f.tape + ((int64_t)l * f.n + base + r) * 4 * d;
+                tp[j] = s.Y[r][perm[j]];  // a
+                tp[d + j] = bout;         // b (density direction: the layer's output half)
+                tp[2 * d + j] = sj;
+                tp[3 * d + j] = tj;
+            }
+            s.Y[r][pb] = bout;
+            O[q][j] = sj; // kept for the row's log-determinant below
+        }
+        __syncwarp();
+        if (lane < 16) {
+            float ld = 0.f;
+            for (int j = 0; j < d; ++j) { ld += O[lane][j]; }
+            s.logdet[r0 + lane] += ld;
+        }
+        __syncwarp();
+    }
+    // output and log q of the warp's rows
+    float ls = 0.f;
+    for (int c = 0; c < D; ++c) { ls += f.logsig[c]; }
+    for (int r = r0; r < min(r0 + 16, rows); ++r) {
+        float zz = 0.f;
+        const int row = base + r;
+        if (lane < D) {
+            float z, o;
+            if (f.dir == 0) { // z was the input
+                z = (f.in_cm || f.in_cmf || f.zgen || row >= f.n) ? flow_input(f, row, lane) : f.in[(int64_t)row * D + lane];
+                o = f.mu[lane] + __expf(f.logsig[lane]) * s.Y[r][lane];
+            } else {
+                z = s.Y[r][lane];
+                o = z;
+            }
+            zz = z * z;
+            if (f.out && row < f.n) { f.out[(int64_t)row * D + lane] = o; }
+            if (f.out_cm) { s.Y[r][lane] = o; } // stored chain-minor below
+        }
+        zz = warp_sum(zz);
+        if (lane == 0) {
+            const float lq = -0.5f * zz - 0.91893853320467274f * D - s.logdet[r] - ls;
+            if (row < f.n) { f.logq[row] = lq; } else { f.logq_b[row - f.n] = lq; }
+        }
+    }
+    if (f.out_cm) { // coalesced over the rows, one coordinate at a time (first set only)
+        __syncthreads();
+        for (int i = threadIdx.x; i < D * rows_cta; i += blockDim.x) {
+            const int c = i / rows_cta, r = i % rows_cta;
+            if (r < rows && base + r < f.n) { f.out_cm[(int64_t)c * f.cm_stride + base + r] = s.Y[r][c]; }
         }
     }
 }
@@ -1267,7 +1472,8 @@ struct mcig_flow {
     int64_t cap = 0, tape_cap = 0, batch_cap = 0;
     // passes on tcgen05 (flow_pass_tc_kernel) or on mma.sync (flow_pass_kernel); status bit 0:
     // a tcgen05 pass did not see an MMA completion within its bounded wait
-    int tc = 0;
+    int tc = 0;      // pass kernel: 0 register-fused mma.sync, 1 tcgen05, 2 shared-memory mma.sync
+    int nsm = 152;   // SMs of the device
     int *status = nullptr;
 };
 
@@ -1380,6 +1586,8 @@ extern "C" int mcig_flow_create(int ndim, int nlayers, int hidden, uint64_t seed
     int rc = flow_cast(f, f->st);
     if (rc) { return rc; }
     FCK(cudaFuncSetAttribute(flow_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowSmem)));
+    FCK(cudaFuncSetAttribute(flow_pass_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowFusedSmem)));
+    FCK(cudaDeviceGetAttribute(&f->nsm, cudaDevAttrMultiProcessorCount, device));
     FCK(cudaFuncSetAttribute(flow_pass_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FlowTcSmem)));
     FCK(cudaMalloc(&f->status, sizeof(int)));
     FCK(cudaMemset(f->status, 0, sizeof(int)));
@@ -1456,15 +1664,23 @@ extern "C" int mcig_flow_set_params(mcig_flow *f, const float *theta, int64_t n)
     return MCIG_OK;
 }
 
-// one pass over device arrays (in [n][D] float -> out, logq); tape optional
+// one pass over device arrays (in [n][D] float -> out, logq); tape optional.  The
+// register-fused kernel takes as many warps per CTA (16 rows each, at most 16) as spread the
+// rows of both sets over every SM once.
 static int flow_pass_launch(mcig_flow *f, FlowArgs &a, int64_t n, cudaStream_t st)
 {
-    if (f->tc) {
+    const int64_t total = n + a.nb;
+    if (f->tc == 1) {
         const int grid = (int)((n + FTC_ROWS - 1) / FTC_ROWS);
         flow_pass_tc_kernel<<<grid, FTC_THREADS, sizeof(FlowTcSmem), st>>>(a, f->status);
-    } else {
+    } else if (f->tc == 2) {
         const int grid = (int)((n + FLOW_PASS_ROWS - 1) / FLOW_PASS_ROWS);
         flow_pass_kernel<<<grid, FLOW_PASS_THREADS, sizeof(FlowSmem), st>>>(a);
+    } else {
+        const int64_t per_sm = (total + 16 * (int64_t)f->nsm - 1) / (16 * (int64_t)f->nsm);
+        const int w = (int)std::min<int64_t>(FLOW_FUSED_MAXW, std::max<int64_t>(1, per_sm));
+        const int grid = (int)((total + 16 * w - 1) / (16 * w));
+        flow_pass_fused_kernel<<<grid, 32 * w, sizeof(FlowFusedSmem), st>>>(a);
     }
     FCK(cudaGetLastError());
     return MCIG_OK;
@@ -1486,8 +1702,33 @@ int mcig_flow_check_status(mcig_flow *f, cudaStream_t st)
 extern "C" int mcig_flow_set_tensor_path(mcig_flow *f, int tc)
 {
     if (!f) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "flow is NULL"); }
-    f->tc = tc ? 1 : 0;
+    if (tc < 0 || tc > 2) { return flow_err(MCIG_ERR_INVALID_ARGUMENT, "pass kernel must be 0 (register-fused mma.sync), 1 (tcgen05) or 2 (shared-memory mma.sync)"); }
+    f->tc = tc;
     return MCIG_OK;
+}
+
+// the density passes (log q) of two chain-minor walker sets in one launch of the register-fused
+// kernel: in_cm (double) -> logq_a and in_cmf_b (float) -> logq_b, n walkers each (stride
+// nstride); with another pass kernel selected, two launches
+int mcig_flow_density2_device(mcig_flow *f, const double *in_cm, const float *in_cmf_b, int64_t nstride, int64_t n,
+                              float *logq_a, float *logq_b, cudaStream_t st)
+{
+    FlowArgs a;
+    memset(&a, 0, sizeof(a));
+    a.D = f->D; a.d = f->d; a.L = f->L; a.n = (int)n; a.dir = 1;
+    a.logq = logq_a;
+    a.mu = f->theta + f->base_off; a.logsig = f->theta + f->base_off + f->D;
+    a.perm = f->perm; a.wb = f->wb; a.theta = f->theta;
+    a.wstride = WB_LAYER; a.pstride = f->pstride;
+    a.in_cm = in_cm; a.cm_stride = nstride;
+    if (f->tc == 0) {
+        a.nb = (int)n; a.in_cmf_b = in_cmf_b; a.logq_b = logq_b;
+        return flow_pass_launch(f, a, n, st);
+    }
+    int rc = flow_pass_launch(f, a, n, st);
+    if (rc) { return rc; }
+    a.in_cm = nullptr; a.in_cmf = in_cmf_b; a.logq = logq_b;
+    return flow_pass_launch(f, a, n, st);
 }
 
 // one pass with chain-minor walkers: input in_cm (double, NULL: rows d_in) and output

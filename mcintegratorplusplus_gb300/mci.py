@@ -411,8 +411,9 @@ class Flow:
             pass
 
     def set_tensor_path(self, tc):
-        """passes on tcgen05 (True) or on mma.sync (False)"""
-        _raise(self.L.mcig_flow_set_tensor_path(self._h, int(bool(tc))))
+        """pass kernel: 0 (or False) register-fused mma.sync, 1 (or True) tcgen05 with TMEM
+        accumulators, 2 mma.sync with the hidden activations in shared memory"""
+        _raise(self.L.mcig_flow_set_tensor_path(self._h, int(tc)))
 
     def params(self):
         n = ctypes.c_int64()

@@ -80,9 +80,10 @@ def mcig():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tc", [False, True])
+@pytest.mark.parametrize("tc", [0, 1, 2])
 def test_flow_passes_match_oracle(mcig, tc):
-    """Both pass kernels (mma.sync; tcgen05 with TMEM accumulators) against the oracle."""
+    """The three pass kernels (register-fused mma.sync; tcgen05 with TMEM accumulators;
+    mma.sync with shared-memory activations) against the oracle."""
     f = mcig.Flow(D, L, H, seed=11)
     f.set_tensor_path(tc)
     th = random_params(5)
@@ -104,7 +105,27 @@ def test_flow_passes_match_oracle(mcig, tc):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tc", [False, True])
+@pytest.mark.parametrize("Dd,Ld,n", [(D, L, 300), (6, 3, 200), (32, 4, 1000)])
+def test_flow_fused_pass_equals_shared_memory_pass(mcig, Dd, Ld, n):
+    """The register-fused pass (activations in registers) and the shared-memory pass form the
+    same bf16 products in the same order: outputs and log q equal bit for bit, both ways."""
+    rng = np.random.default_rng(8)
+    th = (fo.init_params(Dd, Ld, H, 5).astype(np.float64) + rng.standard_normal(fo.nparams(Dd, Ld, H)) * 0.05)
+    z = rng.standard_normal((n, Dd))
+    out = []
+    for tc in (0, 2):
+        f = mcig.Flow(Dd, Ld, H, seed=5)
+        f.set_tensor_path(tc)
+        f.set_params(th.astype(np.float32))
+        x, lq = f.forward(z)
+        zi, lqi = f.inverse(x)
+        out.append((x, lq, zi, lqi))
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b), np.abs(a - b).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tc", [0, 1, 2])
 def test_flow_odd_half_dimension_matches_oracle(mcig, tc):
     """D = 6 (d = 3): layer parameter blocks that do not start on 16-byte boundaries."""
     Dd, Ld = 6, 3

@@ -611,6 +611,7 @@ def run_c5(args):
     import mcintegratorplusplus_gb300 as mcig
     D, nch, nmc = 24, args.chains5, args.nmc5
     adapt = getattr(args, "c5_adapt", None) or C5_ADAPT
+    lr = getattr(args, "c5_lr", None) or 3e-3
     batch = getattr(args, "c5_batch", None) or nch
     lanes = getattr(args, "c5_lanes", 0) or 0
     params, means, var_x1 = c5_target()
@@ -632,7 +633,7 @@ def run_c5(args):
                 f = mcig.Flow(D, 8, 128, seed=6 + it)
                 f.set_tensor_path({"mma.sync": 0, "tcgen05": 1, "mma.sync-smem": 2}[getattr(args, "c5_flow_gemm", "mma.sync")])
                 _, _, acc = mcig.integrate_flow(m, f, nmc, period=5, refresh=4096, train_steps=adapt,
-                                                batch=batch, lr=3e-3)
+                                                batch=batch, lr=lr)
                 accs.append(acc)
             else:
                 m.integrate(nmc)
@@ -654,7 +655,7 @@ def run_c5(args):
             "data": "synthetic (seeded mixture, random-init flow)",
             "config": {"workload": "C5 learned proposal", "chains": nch, "ndim": D, "nmc": nmc, "flow_layers": 8,
                        "hidden": 128, "period": 5, "adaptation_cycles": adapt, "adam_batch": batch,
-                       "adam_lr": 3e-3, "refresh": 4096},
+                       "adam_lr": lr, "refresh": 4096, "local_lanes_per_chain": lanes or 1},
             "plain_mh": {"value": res[False][0], "ms_per_step": res[False][1] * 1e3, "ess": res[False][2],
                          "phases": res[False][4], "ess_detail": res[False][5]},
             "flow": {"ess": res[True][2], "acceptance": res[True][3], "phases": res[True][4],
@@ -719,6 +720,7 @@ def main():
     ap.add_argument("--nmc5", type=int, default=8192)
     ap.add_argument("--c5-adapt", type=int, default=None, help="adaptation cycles of the flow (default C5_ADAPT)")
     ap.add_argument("--c5-batch", type=int, default=None, help="rows per Adam step of the flow (default: all chains)")
+    ap.add_argument("--c5-lr", type=float, default=None, help="Adam learning rate of the flow (default 3e-3)")
     ap.add_argument("--c5-lanes", type=int, default=0, choices=[0, 4, 8],
                     help="lanes per chain of the local Metropolis steps in both C5 arms (0: one lane)")
     ap.add_argument("--c5-flow-gemm", default="mma.sync", choices=["tcgen05", "mma.sync", "mma.sync-smem"],

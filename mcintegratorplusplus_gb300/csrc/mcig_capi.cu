@@ -2333,12 +2333,30 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     if ((rc = alloc_obs_data(h, h->obs, nmc, h->obsdata, h->obs_nstore, h->full32))) { return rc; }
     const size_t nc = (size_t)h->nchains;
     const int D = h->ndim;
-    DBuf<float> xf, xprop, lq_cur, lq_prop;
+    DBuf<float> xf, xprop, xprop2, lq_cur, lq_prop, lq_prop2;
     DBuf<int64_t> nflow;
-    if ((rc = xf.alloc(nc * D)) || (rc = xprop.alloc(nc * D)) || (rc = lq_cur.alloc(nc)) ||
-        (rc = lq_prop.alloc(nc)) || (rc = nflow.alloc(nc))) {
+    if ((rc = xf.alloc(nc * D)) || (rc = xprop.alloc(nc * D)) || (rc = xprop2.alloc(nc * D)) || (rc = lq_cur.alloc(nc)) ||
+        (rc = lq_prop.alloc(nc)) || (rc = lq_prop2.alloc(nc)) || (rc = nflow.alloc(nc))) {
         return rc;
     }
+    // the second stream of the sampling phase: the next cycle's generative pass (it depends on
+    // the flow's weights and the cycle's z only, not on the walkers) runs there beside this
+    // cycle's test and the next local steps, into the other of two proposal buffers
+    struct Overlap {
+        cudaStream_t st = nullptr;
+        cudaEvent_t d2 = nullptr, gen[2] = {nullptr, nullptr}, done = nullptr;
+        ~Overlap()
+        {
+            if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+            for (cudaEvent_t e : {d2, gen[0], gen[1], done}) { if (e) { cudaEventDestroy(e); } }
+        }
+    } ov;
+    CK(cudaStreamCreateWithFlags(&ov.st, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ov.d2, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ov.gen[0], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ov.gen[1], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ov.done, cudaEventDisableTiming));
+    float *xp[2] = {xprop.p, xprop2.p}, *lqp[2] = {lq_prop.p, lq_prop2.p};
     CK(cudaEventRecord(h->ev[0], h->stream));
     if (do_find && h->nfind != 0) {
         KParams c = kp;
@@ -2376,18 +2394,37 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
     // (the generative pass's own log q of x' differs from it by the bf16 rounding of its MLP
     // inputs); the proposal's z is drawn inside the generative pass
     // (the density of the walkers and of the proposals in one launch where the pass kernel
-    // takes two row sets)
-    auto flow_cycle = [&](int64_t krow) -> int {
+    // takes two row sets).  prefetch: the next cycle follows without a training step in
+    // between, so its generative pass is issued now on the second stream, after this cycle's
+    // density pass (every earlier write of the weights and read of its buffer is then done)
+    int64_t pending = -1; // cycle whose proposal the second stream is forming
+    auto gen = [&](uint64_t cyc, cudaStream_t st) {
+        return mcig_flow_propose_device(f, cyc, kp.key0 ^ 0x6A09E667u, kp.key1 ^ 0xBB67AE85u, (int64_t)nc, (int64_t)nc,
+                                        xp[cyc & 1], lqp[cyc & 1], st);
+    };
+    auto flow_cycle = [&](int64_t krow, bool prefetch) -> int {
         int r;
-        if ((r = mcig_flow_propose_device(f, cycle, kp.key0 ^ 0x6A09E667u, kp.key1 ^ 0xBB67AE85u, (int64_t)nc, (int64_t)nc,
-                                          xprop.p, lq_prop.p, h->stream)) ||
-            (r = mcig_flow_density2_device(f, h->x.p, xprop.p, (int64_t)nc, (int64_t)nc, lq_cur.p, lq_prop.p, h->stream))) {
+        const int b = (int)(cycle & 1);
+        if (pending == (int64_t)cycle) {
+            CK(cudaStreamWaitEvent(h->stream, ov.gen[b], 0));
+        } else if ((r = gen(cycle, h->stream))) {
             return r;
         }
+        pending = -1;
+        if ((r = mcig_flow_density2_device(f, h->x.p, xp[b], (int64_t)nc, (int64_t)nc, lq_cur.p, lqp[b], h->stream))) {
+            return r;
+        }
+        if (prefetch) {
+            CK(cudaEventRecord(ov.d2, h->stream));
+            CK(cudaStreamWaitEvent(ov.st, ov.d2, 0));
+            if ((r = gen(cycle + 1, ov.st))) { return r; }
+            CK(cudaEventRecord(ov.gen[b ^ 1], ov.st));
+            pending = (int64_t)cycle + 1;
+        }
         if (fast_accept) {
-            fast_accept(sp, &h->fc, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p, h->stream);
+            fast_accept(sp, &h->fc, xp[b], lqp[b], lq_cur.p, cycle, krow, nflow.p, h->stream);
         } else {
-            flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xprop.p, lq_prop.p, lq_cur.p, cycle, krow, nflow.p);
+            flow_accept_kernel<<<tg, tb, 0, h->stream>>>(sp, xp[b], lqp[b], lq_cur.p, cycle, krow, nflow.p);
         }
         h->launches += 4;
         CK(cudaGetLastError());
@@ -2409,7 +2446,7 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
         ++h->launches;
         if ((rc = mcig_flow_train_device(f, xf.p, (int64_t)nc, 1, batch, lr, nullptr, h->stream))) { return rc; }
         h->launches += 5;
-        if (4 * t >= train_steps && (rc = flow_cycle(-1))) { return rc; }
+        if (4 * t >= train_steps && (rc = flow_cycle(-1, false))) { return rc; }
     }
     CK(cudaMemsetAsync(nflow.p, 0, nc * sizeof(int64_t), h->stream));
     const uint64_t cycle0 = cycle;
@@ -2428,7 +2465,8 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
             step += nloc;
         }
         if (step < nmc) {
-            if ((rc = flow_cycle(step))) { return rc; }
+            const bool trains_next = train_steps > 0 && batch > 0 && step + 1 >= next_refresh && step + 1 < nmc;
+            if ((rc = flow_cycle(step, step + period < nmc && !trains_next))) { return rc; }
             ++step;
         }
         if (step >= next_refresh && step < nmc) {
@@ -2440,6 +2478,8 @@ extern "C" int mcig_integrate_flow(mcig_mci *h, mcig_flow *f, int64_t nmc, int p
             next_refresh += refresh;
         }
     }
+    CK(cudaEventRecord(ov.done, ov.st)); // the second stream has nothing left (a pending pass is never unused)
+    CK(cudaStreamWaitEvent(h->stream, ov.done, 0));
     CK(cudaEventRecord(h->ev[3], h->stream));
     if ((rc = estimate_all(h, h->obs, h->obsdata, h->obs_nstore, h->full32, h->chain_avg, h->chain_err))) { return rc; }
     CK(cudaEventRecord(h->ev[4], h->stream));

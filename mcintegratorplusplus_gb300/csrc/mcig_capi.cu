@@ -1238,7 +1238,12 @@ static int launch(mcig_mci *h, const KParams &kp)
             const int k = h->pdfs[0].kind;
             pk = (k == MCIG_PDF_GAUSS || k == MCIG_PDF_GAUSS_SUM) ? 1 : (k == MCIG_PDF_GAUSS_PREC ? 2 : (k == MCIG_PDF_GAUSS_MIX ? 3 : 0));
         }
-        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk);
+        int moments = 1; // observables x and x.x only, float Full data
+        for (size_t o = 0; o < h->obs.size(); ++o) {
+            const ObsDesc &od = kp.obs[o];
+            if ((od.kind != MCIG_OBS_XND && od.kind != MCIG_OBS_X2SUM) || (od.acc == MCIG_ACC_FULL && !od.full32)) { moments = 0; }
+        }
+        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk, moments);
         smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
         if (kp.mode == KMODE_CALIB && h->calib_split && h->movetype == MCIG_MOVE_ALL && maxd_bucket(h->ndim) == 16 &&
             h->ntypes == 1 && !h->periodic && (pk == 1 || pk == 2)) { // PK_GAUSS, PK_PREC

@@ -160,7 +160,11 @@ template <> struct FastSlot<false> {
     __device__ __forceinline__ static double get(const T &v) { return v; }
 };
 
-template <int MAXD, int MOVE, bool KAHAN, int PK>
+// MOMENTS: every observable is x (XND) or x.x (X2SUM), Full data in float or a Simple/Block
+// accumulator.  The kernel then holds only those paths: the general observable code is a
+// runtime choice among every kind and accumulator, which the compiler turns into predicated
+// code that issues the arithmetic of all of them on every step; x.x is formed once a step.
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false>
 struct FastSampler {
     using Slot = FastSlot<KAHAN>;
     using ST = typename Slot::T;
@@ -171,6 +175,7 @@ struct FastSampler {
     float x[MAXD];
     float st[MCIG_MAXTYPES];
     float lp;
+    float xx;   // MOMENTS: x.x of the walker at the current step
     uint32_t s0, s1;
     uint64_t ctr;
 
@@ -286,7 +291,7 @@ struct FastSampler {
                         if (j < nv) { dst[j * nc] = v[j]; }
                     }
                 }
-            } else {
+            } else if constexpr (!MOMENTS) {
                 double *dst = (double *)od.data + row * (size_t)nv * nc + c;
 #pragma unroll
                 for (int j = 0; j < NV; ++j) {
@@ -322,6 +327,11 @@ struct FastSampler {
     __device__ __forceinline__ void observe_put(const ObsDesc &od, uint32_t k, bool flush, uint32_t blk)
     {
         const int kind = od.kind;
+        if constexpr (MOMENTS) {
+            if (kind == MCIG_OBS_XND) { put<MAXD>(od, k, flush, blk, x, p.ndim); }
+            else { put<1>(od, k, flush, blk, &xx, 1); }
+            return;
+        }
         if (kind == MCIG_OBS_XND || kind == MCIG_OBS_X2 || kind == MCIG_OBS_X2BLOCK) {
             float v[MAXD];
             int nv = p.ndim;
@@ -412,6 +422,12 @@ struct FastSampler {
         for (uint32_t r = 0; r < n32; ++r) {
             na += step() ? 1u : 0u;
             if (!sample) { continue; }
+            if constexpr (MOMENTS) { // the X2SUM value of the general path, formed once
+                float s = 0.f;
+#pragma unroll
+                for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); }
+                xx = s;
+            }
 #pragma unroll
             for (int o = 0; o < MCIG_FAST_UNROLLED_OBS; ++o) {
                 if (o < p.nobs) { obs_step(p.obs[o], r0 + r); }
@@ -487,7 +503,7 @@ struct FastSampler {
 // Up to 16 dimensions the kernel is held to 128 registers per thread: registers are
 // allocated in steps that make 136 or 144 per thread fit only six 64-thread blocks
 // per SM (912 of the 1,024 blocks of 65,536 chains, so a second wave), 128 fits eight.
-template <int MAXD, int MOVE, bool KAHAN, int PK>
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -496,7 +512,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    FastSampler<MAXD, MOVE, KAHAN, PK> s(p, fc, c, slots);
+    FastSampler<MAXD, MOVE, KAHAN, PK, MOMENTS> s(p, fc, c, slots);
     if (p.mode == KMODE_CALIB) { s.calibrate(p.nsteps); }
     else if (p.mode == KMODE_FUSED) {
         // MCI::integrate's phases for this chain alone: a chain whose calibration converges
@@ -510,11 +526,11 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     s.store_state();
 }
 
-template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY>
+template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY, bool MOMENTS = false>
 void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, int grid, int block, size_t smem,
                       cudaStream_t st)
 {
-    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK>;
+    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS>;
     // shared memory as large as possible, so the accumulator slots never limit residency
     mcig_smem_attrs((const void *)k, smem);
     k<<<grid, block, smem, st>>>(p, *fc);

@@ -12,8 +12,10 @@ mcig_launch_fn mcig_generic_launcher(int precision, int rng);
 
 // register-resident float kernel (mcig_fast.cuh): move MCIG_MOVE_ALL / MCIG_MOVE_VEC,
 // maxd 4, 8, 16 or 32, pdf set pk (PK_ANY, or PK_GAUSS / PK_PREC / PK_MIX for a single
-// sampling function of that kind); NULL otherwise
-mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk);
+// sampling function of that kind); moments: every observable is x or x.x with float Full
+// data or a Simple/Block accumulator (a kernel holding only those paths where one exists);
+// NULL otherwise
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments = 0);
 
 // step-size calibration (KMODE_CALIB) with the calibration's tail split over lanes
 // (mcig_calib.cuh): all-coordinate move, one step type, no periodic domain, ndim 9..16,

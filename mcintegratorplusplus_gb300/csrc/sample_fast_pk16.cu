@@ -4,8 +4,17 @@
 #include "mcig_calib.cuh"
 #include "mcig_launchers.h"
 
-mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk)
+mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk, int moments)
 {
+    if (moments) { // observables x and x.x only (FastSampler's MOMENTS)
+        switch (pk) {
+        case PK_GAUSS:
+            return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_GAUSS, true> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_GAUSS, true>;
+        case PK_PREC:
+            return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_PREC, true> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_PREC, true>;
+        default: break;
+        }
+    }
     switch (pk) {
     case PK_GAUSS: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_GAUSS> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_GAUSS>;
     case PK_PREC: return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK_PREC> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK_PREC>;

@@ -171,3 +171,49 @@ def test_chunked_sampling_equals_one_launch(nskip):
             assert np.max(np.abs(ca - avg) / (np.abs(avg) + sd)) < 1e-6
             np.testing.assert_allclose(ce, err, rtol=2e-5)
             off += nv_of[o]
+
+
+def _moments_run(mcig, prec, pdf, ndim, extra):
+    """Observables x.x and x_i in Block and float Full accumulators (the kernel variant that
+    holds only those paths); extra: one more observable (a constant, Simple) that makes the
+    launch take the general observable code instead."""
+    nc, nmc, nb = 300, 1200, 12
+    m = mcig.MCI(ndim, nc, precision=prec)
+    m.setSeed(21)
+    m.setFullStorage(32)
+    if pdf == "prec":
+        rng = np.random.default_rng(3)
+        q, _ = np.linalg.qr(rng.standard_normal((ndim, ndim)))
+        m.addSamplingFunction(mcig.PDF_GAUSS_PREC, (q @ np.diag(10.0 ** rng.uniform(-1, 1, ndim)) @ q.T).ravel())
+    else:
+        m.addSamplingFunction(mcig.PDF_GAUSS)
+    m.setTrialMove(mcig.MOVE_ALL, mcig.SRRD_GAUSSIAN)
+    m.setNdecorrelationSteps(200)
+    m.setKernel(2)
+    m.addObservable(mcig.OBS_X2SUM, (), nmc // nb, 1, False, mcig.EST_UNCORRELATED)
+    m.addObservable(mcig.OBS_XND, (), nmc // nb, 1, False, mcig.EST_UNCORRELATED)
+    m.addObservable(mcig.OBS_X2SUM, (), 1, 1, False, mcig.EST_UNCORRELATED)
+    m.addObservable(mcig.OBS_XND, (), 1, 1, False, mcig.EST_UNCORRELATED)
+    if extra:
+        m.addObservable(mcig.OBS_CONST, (2.5,), 0, 1, False, mcig.EST_NOOP)
+    avg, err = m.integrate(nmc)
+    ca, ce = m.getChainResults()
+    nv = 2 + 2 * ndim
+    out = {"avg": avg[:nv], "err": err[:nv], "ca": ca[:, :nv], "ce": ce[:, :nv], "x": m.getX(),
+           "steps": m.getMRT2Steps(), "ctr": m.getStepCounters(), "counts": np.stack(m.getCounts())}
+    for o in range(4):
+        out["data%d" % o] = m.getObsData(o)
+    return out
+
+
+@pytest.mark.parametrize("prec_name,pdf,ndim", [("PREC_FP32", "prec", 16), ("PREC_FP32_ACC64", "prec", 16),
+                                                ("PREC_FP32", "gauss", 11)])
+def test_moments_kernel_equals_general_observable_code(prec_name, pdf, ndim):
+    """The register-resident kernel holding only the x and x.x observable paths gives the
+    general observable code's values bit for bit (same float products and sums)."""
+    import mcintegratorplusplus_gb300 as mcig
+    prec = getattr(mcig, prec_name)
+    a = _moments_run(mcig, prec, pdf, ndim, False)
+    b = _moments_run(mcig, prec, pdf, ndim, True)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k

@@ -77,7 +77,8 @@ int mcig_set_phase_fusion(mcig_mci *h, int on);
 int mcig_set_calibration_split(mcig_mci *h, int on);
 
 /* Multi-lane kernels.  lpc = 0 (default): automatic, i.e. two lanes per chain for the
- * configurations of lpc = 2 with at most 32,768 chains, else one; lpc = 1: one lane per chain.
+ * configurations of lpc = 2 with at most 32,768 chains unless every observable is x or x.x
+ * (whose one-lane variant is as fast), else one; lpc = 1: one lane per chain.
  * lpc = 2: a float handle with one exp(-x.x) or precision-matrix sampling function in 9..16
  * coordinates (all-coordinate uniform or Gaussian move, one step type, unbound domain,
  * observables without exp() or coordinate blocks) runs burn-in and sampling (and the

@@ -1152,11 +1152,24 @@ static bool lanes_eligible(const mcig_mci *h)
     return true;
 }
 
-// Chain counts up to which the two-lane kernel serves its configurations by default.  One lane
-// per chain fills an SM with nchains / 152 / 32 warps (3.4 at 16,384 chains, 13.5 at 65,536):
-// measured on a 16-D precision-matrix target with x.x and x_i in Block and Full accumulators,
-// the two-lane sampling launch took 18.9 ms against 23.9 ms at 16,384 chains and 41.5 ms
-// against 35.8 ms at 65,536 chains.
+// every observable of the launch is x or x.x with float Full data or a Simple/Block
+// accumulator: the register-resident kernels have variants holding only those paths
+static int moments_only(const mcig_mci *h, const KParams &kp)
+{
+    for (size_t o = 0; o < h->obs.size(); ++o) {
+        const ObsDesc &od = kp.obs[o];
+        if ((od.kind != MCIG_OBS_XND && od.kind != MCIG_OBS_X2SUM) || (od.acc == MCIG_ACC_FULL && !od.full32)) { return 0; }
+    }
+    return 1;
+}
+
+// Chain counts up to which the two-lane kernel serves its configurations by default, unless
+// every observable is x or x.x (then the one-lane kernel's variant for them is as fast).  One
+// lane per chain fills an SM with nchains / 152 / 32 warps (3.4 at 16,384 chains, 13.5 at
+// 65,536).  Measured sampling launches, 16-D precision-matrix target, 10,000 steps:
+//   observables x, x.x, x_i, log p, sum x_i (general code): two lanes 18.9 against 23.9 ms at
+//   16,384 chains, 25.5 against 26.8 ms at 32,768, 41.5 against 35.8 ms at 65,536;
+//   x and x.x only: 18.6 / 17.9 ms at 16,384, 19.8 / 21.0 ms at 24,576, 23.4 / 21.5 ms at 32,768.
 #define MCIG_PAIR_AUTO_CHAINS 32768
 
 // the two-lane kernel (mcig_pair.cuh) serves float walkers with an all-coordinate uniform or
@@ -1184,7 +1197,7 @@ static int kernel_family(const mcig_mci *h, const KParams &kp)
     // two lanes per chain for burn-in and sampling (and calibration when its split tail is
     // off): mcig_set_lanes(h, 2), or automatically below MCIG_PAIR_AUTO_CHAINS chains, where
     // one lane per chain leaves the SMs with too few warps to hide latency
-    const bool want_pair = h->lanes == 2 || (h->lanes == 0 && h->nchains <= MCIG_PAIR_AUTO_CHAINS);
+    const bool want_pair = h->lanes == 2 || (h->lanes == 0 && h->nchains <= MCIG_PAIR_AUTO_CHAINS && !moments_only(h, kp));
     if (kp.ndump == 0 && kp.mode != KMODE_FUSED && h->kernel_policy == 0 && want_pair && small_n &&
         pair_eligible(h) && !(kp.mode == KMODE_CALIB && h->calib_split)) {
         return 3;
@@ -1205,7 +1218,8 @@ static int launch(mcig_mci *h, const KParams &kp)
     if (family == 3) {
         if (h->f64_decide) { return set_err(MCIG_ERR_UNSUPPORTED, "the FP64-certified decision runs in the multi-lane mixture kernel only (mcig_set_lanes)"); }
         const int k = h->pdfs[0].kind;
-        mcig_launch_fn pf = mcig_pair_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, k == MCIG_PDF_GAUSS_PREC ? 2 : 1);
+        mcig_launch_fn pf = mcig_pair_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, k == MCIG_PDF_GAUSS_PREC ? 2 : 1,
+                                               moments_only(h, kp));
         if (!pf) { return set_err(MCIG_ERR_UNSUPPORTED, "no two-lane kernel for this configuration"); }
         pf(kp, &h->fc, h->movetype, 0, 0, 0, h->stream);
         ++h->launches;
@@ -1238,12 +1252,7 @@ static int launch(mcig_mci *h, const KParams &kp)
             const int k = h->pdfs[0].kind;
             pk = (k == MCIG_PDF_GAUSS || k == MCIG_PDF_GAUSS_SUM) ? 1 : (k == MCIG_PDF_GAUSS_PREC ? 2 : (k == MCIG_PDF_GAUSS_MIX ? 3 : 0));
         }
-        int moments = 1; // observables x and x.x only, float Full data
-        for (size_t o = 0; o < h->obs.size(); ++o) {
-            const ObsDesc &od = kp.obs[o];
-            if ((od.kind != MCIG_OBS_XND && od.kind != MCIG_OBS_X2SUM) || (od.acc == MCIG_ACC_FULL && !od.full32)) { moments = 0; }
-        }
-        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk, moments);
+        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk, moments_only(h, kp));
         smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
         if (kp.mode == KMODE_CALIB && h->calib_split && h->movetype == MCIG_MOVE_ALL && maxd_bucket(h->ndim) == 16 &&
             h->ntypes == 1 && !h->periodic && (pk == 1 || pk == 2)) { // PK_GAUSS, PK_PREC

@@ -29,8 +29,8 @@ mcig_launch_fn mcig_lanes_launcher(int kahan, int maxd, int lpc);
 
 // float kernel with two lanes per chain for one sampling function of kind pk (PK_GAUSS or
 // PK_PREC) in 9..16 coordinates (mcig_pair.cuh): all-coordinate move, one step type,
-// unbound domain; NULL otherwise
-mcig_launch_fn mcig_pair_launcher(int kahan, int pk);
+// unbound domain; moments as for mcig_fast_launcher; NULL otherwise
+mcig_launch_fn mcig_pair_launcher(int kahan, int pk, int moments = 0);
 
 // Metropolis-Hastings test of the learned proposal for one sampling function of kind pk
 // (PK_GAUSS, PK_PREC or PK_MIX) at maxd 8, 16 or 32 (flow_accept.cu); NULL otherwise

@@ -34,7 +34,9 @@ __host__ __device__ __forceinline__ constexpr int pair_coef_off(int j)
     return (j % 2 == 0) ? (j / 2) * (j / 2 + 1) : (j / 2 + 1) * (j / 2 + 1);
 }
 
-template <int PK, bool KAHAN>
+// MOMENTS: every observable is x (XND) or x.x (X2SUM) with float Full data or a Simple/Block
+// accumulator, so only those paths are compiled (FastSampler's MOMENTS)
+template <int PK, bool KAHAN, bool MOMENTS = false>
 struct PairSampler {
     static_assert(PK == PK_PREC || PK == PK_GAUSS, "the pair kernel serves one precision matrix or exp(-x.x)");
     static constexpr int MAXD = 16;            // coordinates (padded with zero steps)
@@ -202,7 +204,7 @@ struct PairSampler {
                 for (int m = 0; m < NV; ++m) {
                     if (all || j0 + m < od.nv) { dst[m * ncs] = v[m]; }
                 }
-            } else {
+            } else if constexpr (!MOMENTS) {
                 double *dst = (double *)od.data + (row * (size_t)od.nv + j0) * ncs + c;
 #pragma unroll
                 for (int m = 0; m < NV; ++m) {
@@ -232,6 +234,14 @@ struct PairSampler {
     __device__ __forceinline__ void observe(const ObsDesc &od, uint32_t kk, bool flush, uint32_t blk)
     {
         const int kind = od.kind;
+        if constexpr (MOMENTS) {
+            if (kind == MCIG_OBS_XND) {
+                if (valid) { put<CPL>(od, l * CPL, kk, flush, blk, x); }
+            } else if (valid && l == 0) {
+                put<1>(od, 0, kk, flush, blk, &xx);
+            }
+            return;
+        }
         if (vec_kind(kind)) {
             float v[CPL];
 #pragma unroll
@@ -378,10 +388,10 @@ struct PairSampler {
 
 // 64 threads (two warps, 32 chains) per block; at most 72 registers per thread keep 14
 // blocks on an SM, so 65,536 chains (131,072 lanes) run in one wave of 27 warps per SM
-template <int PK, bool KAHAN>
+template <int PK, bool KAHAN, bool MOMENTS>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 14) mcig_pair_kernel(const KParams p, const FastConst fc)
 {
-    using PS = PairSampler<PK, KAHAN>;
+    using PS = PairSampler<PK, KAHAN, MOMENTS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *tab = (float *)smem_raw; // [2][72]: lane group l's coefficients, column-major
     typename PS::ST *slots = (typename PS::ST *)(smem_raw + PS::TAB_BYTES);
@@ -405,12 +415,12 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 14) mcig_pair_kernel(const KP
     s.store_state();
 }
 
-template <int PK, bool KAHAN>
+template <int PK, bool KAHAN, bool MOMENTS = false>
 void mcig_pair_launch(const KParams &p0, const FastConst *fc, int /*movetype*/, int /*grid*/, int /*block*/,
                       size_t /*smem*/, cudaStream_t st)
 {
-    using PS = PairSampler<PK, KAHAN>;
-    auto k = mcig_pair_kernel<PK, KAHAN>;
+    using PS = PairSampler<PK, KAHAN, MOMENTS>;
+    auto k = mcig_pair_kernel<PK, KAHAN, MOMENTS>;
     KParams p = p0;
     int ns = 0; // per-lane accumulator slot of each observable
     for (int o = 0; o < p.nobs; ++o) {

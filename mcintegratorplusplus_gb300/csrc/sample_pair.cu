@@ -3,8 +3,15 @@
 #include "mcig_pair.cuh"
 #include "mcig_launchers.h"
 
-mcig_launch_fn mcig_pair_launcher(int kahan, int pk)
+mcig_launch_fn mcig_pair_launcher(int kahan, int pk, int moments)
 {
+    if (moments) { // observables x and x.x only
+        switch (pk) {
+        case PK_GAUSS: return kahan ? mcig_pair_launch<PK_GAUSS, true, true> : mcig_pair_launch<PK_GAUSS, false, true>;
+        case PK_PREC: return kahan ? mcig_pair_launch<PK_PREC, true, true> : mcig_pair_launch<PK_PREC, false, true>;
+        default: return nullptr;
+        }
+    }
     switch (pk) {
     case PK_GAUSS: return kahan ? mcig_pair_launch<PK_GAUSS, true> : mcig_pair_launch<PK_GAUSS, false>;
     case PK_PREC: return kahan ? mcig_pair_launch<PK_PREC, true> : mcig_pair_launch<PK_PREC, false>;

@@ -119,7 +119,8 @@ class MCI:
 
     def setLanes(self, lpc):
         """Lanes per chain of the multi-lane kernels: 0 automatic (two lanes where they serve the
-        configuration and there are at most 32,768 chains), 1 one lane, 2 (one exp(-x.x) or
+        configuration, there are at most 32,768 chains and an observable other than x or x.x),
+        1 one lane, 2 (one exp(-x.x) or
         precision-matrix sampling function in 9..16 coordinates), 4 or 8 (one mixture in 17..32
         coordinates)."""
         _raise(self.L.mcig_set_lanes(self._h, int(lpc)))

@@ -27,7 +27,7 @@ def target(ndim, seed=2024):
     return Sigma, 0.5 * (P + P.T)
 
 
-def configure(m, ndim, pdf, srrd, nmc, nblocks):
+def configure(m, ndim, pdf, srrd, nmc, nblocks, obsset="all"):
     if pdf == "prec":
         m.add_sampling_function(3, target(ndim)[1])   # GAUSS_PREC
     else:
@@ -39,6 +39,9 @@ def configure(m, ndim, pdf, srrd, nmc, nblocks):
     m.add_observable(0, (), bs, 1, False, 1)   # x.x Block
     m.add_observable(1, (), bs, 1, False, 1)   # x_i Block
     m.add_observable(0, (), 1, 1, False, 1)    # x.x Full
+    if obsset == "moments":                    # x and x.x only: the kernels' variants for them
+        m.add_observable(1, (), 1, 1, False, 1)
+        return
     if pdf == "prec":
         m.add_observable(1, (), 1, 1, False, 1)    # x_i Full
     else:
@@ -48,11 +51,11 @@ def configure(m, ndim, pdf, srrd, nmc, nblocks):
     m.add_observable(5, (), bs, 1, False, 1)   # sum x_i Block
 
 
-def run(mcig, prec, lanes, ndim, pdf, srrd, nc, nmc=1200, nblocks=12, seed=77, split=True):
+def run(mcig, prec, lanes, ndim, pdf, srrd, nc, nmc=1200, nblocks=12, seed=77, split=True, obsset="all"):
     m = mcig.MCI(ndim, nc, device=0, precision=prec)
     m.setSeed(seed)
     m.setFullStorage(32)
-    configure(m, ndim, pdf, srrd, nmc, nblocks)
+    configure(m, ndim, pdf, srrd, nmc, nblocks, obsset)
     m.setCalibrationSplit(split)
     if lanes:
         m.setLanes(lanes)
@@ -67,18 +70,20 @@ def run(mcig, prec, lanes, ndim, pdf, srrd, nc, nmc=1200, nblocks=12, seed=77, s
     return out
 
 
-@pytest.mark.parametrize("prec_name,ndim,pdf,srrd,nc,split", [
-    ("fp32", 16, "prec", 1, 1000, True),         # the benchmark's form, partial last warp
-    ("fp32_acc64", 16, "prec", 1, 1000, True),   # double block sums
-    ("fp32", 11, "prec", 0, 520, True),          # padded coordinates, uniform move
-    ("fp32", 13, "gauss", 1, 777, True),         # exp(-x.x)
-    ("fp32", 16, "prec", 1, 600, False),         # calibration on two lanes as well
+@pytest.mark.parametrize("prec_name,ndim,pdf,srrd,nc,split,obsset", [
+    ("fp32", 16, "prec", 1, 1000, True, "all"),         # partial last warp, every served observable kind
+    ("fp32_acc64", 16, "prec", 1, 1000, True, "all"),   # double block sums
+    ("fp32", 11, "prec", 0, 520, True, "all"),          # padded coordinates, uniform move
+    ("fp32", 13, "gauss", 1, 777, True, "all"),         # exp(-x.x)
+    ("fp32", 16, "prec", 1, 600, False, "all"),         # calibration on two lanes as well
+    ("fp32", 16, "prec", 1, 1000, True, "moments"),     # the benchmark's observables (x, x.x variants)
+    ("fp32_acc64", 13, "gauss", 1, 520, True, "moments"),
 ])
-def test_pair_bit_identical_to_one_lane(prec_name, ndim, pdf, srrd, nc, split):
+def test_pair_bit_identical_to_one_lane(prec_name, ndim, pdf, srrd, nc, split, obsset):
     import mcintegratorplusplus_gb300 as mcig
     prec = {"fp32": mcig.PREC_FP32, "fp32_acc64": mcig.PREC_FP32_ACC64}[prec_name]
-    a = run(mcig, prec, 0, ndim, pdf, srrd, nc, split=split)
-    b = run(mcig, prec, 2, ndim, pdf, srrd, nc, split=split)
+    a = run(mcig, prec, 0, ndim, pdf, srrd, nc, split=split, obsset=obsset)
+    b = run(mcig, prec, 2, ndim, pdf, srrd, nc, split=split, obsset=obsset)
     for k in a:
         assert np.array_equal(a[k], b[k]), (k, np.max(np.abs(np.asarray(a[k], float) - np.asarray(b[k], float))))
 

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 8) mcig_calib_kernel(const KP
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = c < p.nchains && !(p.active && !p.active[c]);
     const int64_t MIN_STAT = p.nsteps;
-    FastSampler<MAXD, MCIG_MOVE_ALL, true, PK> s(p, fc, live ? c : 0, nullptr);
+    FastSampler<MAXD, MCIG_MOVE_ALL, true, PK, false, true> s(p, fc, live ? c : 0, nullptr); // one step type
     int cons = 0, counter = 0;
     int64_t na = 0;
     bool done = !live || !calib_more(p, cons, counter);

@@ -1252,7 +1252,8 @@ static int launch(mcig_mci *h, const KParams &kp)
             const int k = h->pdfs[0].kind;
             pk = (k == MCIG_PDF_GAUSS || k == MCIG_PDF_GAUSS_SUM) ? 1 : (k == MCIG_PDF_GAUSS_PREC ? 2 : (k == MCIG_PDF_GAUSS_MIX ? 3 : 0));
         }
-        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk, moments_only(h, kp));
+        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk, moments_only(h, kp),
+                                h->ntypes == 1);
         smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
         if (kp.mode == KMODE_CALIB && h->calib_split && h->movetype == MCIG_MOVE_ALL && maxd_bucket(h->ndim) == 16 &&
             h->ntypes == 1 && !h->periodic && (pk == 1 || pk == 2)) { // PK_GAUSS, PK_PREC

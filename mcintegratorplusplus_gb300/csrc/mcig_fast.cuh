@@ -164,7 +164,10 @@ template <> struct FastSlot<false> {
 // accumulator.  The kernel then holds only those paths: the general observable code is a
 // runtime choice among every kind and accumulator, which the compiler turns into predicated
 // code that issues the arithmetic of all of them on every step; x.x is formed once a step.
-template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false>
+// ONET: one step-size type, so the step of coordinate i is st[0] (times its 0 / 1 table
+// entry) without the code of the other types (20 registers and 8 % of the sampling time at
+// the 16-D precision-matrix configuration)
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, bool ONET = false>
 struct FastSampler {
     using Slot = FastSlot<KAHAN>;
     using ST = typename Slot::T;
@@ -193,6 +196,7 @@ struct FastSampler {
     __device__ __forceinline__ float step_i(int i) const
     {
         float s = st[0] * fc.tw[0][i];
+        if constexpr (ONET) { return s; }
         if (p.ntypes > 1) {
 #pragma unroll
             for (int t = 1; t < MCIG_MAXTYPES; ++t) { s = fmaf(st[t], fc.tw[t][i], s); }
@@ -503,7 +507,7 @@ struct FastSampler {
 // Up to 16 dimensions the kernel is held to 128 registers per thread: registers are
 // allocated in steps that make 136 or 144 per thread fit only six 64-thread blocks
 // per SM (912 of the 1,024 blocks of 65,536 chains, so a second wave), 128 fits eight.
-template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false>
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, bool ONET = false>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -512,7 +516,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    FastSampler<MAXD, MOVE, KAHAN, PK, MOMENTS> s(p, fc, c, slots);
+    FastSampler<MAXD, MOVE, KAHAN, PK, MOMENTS, ONET> s(p, fc, c, slots);
     if (p.mode == KMODE_CALIB) { s.calibrate(p.nsteps); }
     else if (p.mode == KMODE_FUSED) {
         // MCI::integrate's phases for this chain alone: a chain whose calibration converges
@@ -526,11 +530,11 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     s.store_state();
 }
 
-template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY, bool MOMENTS = false>
+template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY, bool MOMENTS = false, bool ONET = false>
 void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, int grid, int block, size_t smem,
                       cudaStream_t st)
 {
-    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS>;
+    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS, ONET>;
     // shared memory as large as possible, so the accumulator slots never limit residency
     mcig_smem_attrs((const void *)k, smem);
     k<<<grid, block, smem, st>>>(p, *fc);

@@ -14,8 +14,9 @@ mcig_launch_fn mcig_generic_launcher(int precision, int rng);
 // maxd 4, 8, 16 or 32, pdf set pk (PK_ANY, or PK_GAUSS / PK_PREC / PK_MIX for a single
 // sampling function of that kind); moments: every observable is x or x.x with float Full
 // data or a Simple/Block accumulator (a kernel holding only those paths where one exists);
+// onetype: one step-size type (a kernel without the other types' code where one exists);
 // NULL otherwise
-mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments = 0);
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments = 0, int onetype = 0);
 
 // step-size calibration (KMODE_CALIB) with the calibration's tail split over lanes
 // (mcig_calib.cuh): all-coordinate move, one step type, no periodic domain, ndim 9..16,

@@ -8,6 +8,7 @@
 
 mcig_launch_fn mcig_fast_launcher_vec(int kahan, int maxd);
 mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk, int moments);
+mcig_launch_fn mcig_fast_launcher_pk16_onetype(int kahan, int pk, int moments);
 mcig_launch_fn mcig_fast_launcher_pk32(int kahan, int pk);
 
 static mcig_launch_fn launcher_all(int kahan, int maxd)
@@ -20,8 +21,12 @@ static mcig_launch_fn launcher_all(int kahan, int maxd)
     }
 }
 
-mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments)
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments, int onetype)
 {
+    if (move == MCIG_MOVE_ALL && maxd == 16 && onetype) { // one step-size type
+        mcig_launch_fn f = mcig_fast_launcher_pk16_onetype(kahan, pk, moments);
+        if (f) { return f; }
+    }
     if (move == MCIG_MOVE_ALL && pk != PK_ANY) { // one-pdf kernels where they exist
         mcig_launch_fn f = maxd == 16 ? mcig_fast_launcher_pk16(kahan, pk, moments) : (maxd == 32 ? mcig_fast_launcher_pk32(kahan, pk) : nullptr);
         if (f) { return f; }

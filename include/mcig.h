@@ -86,7 +86,7 @@ int mcig_set_calibration_split(mcig_mci *h, int on);
  * moves coordinates [8l, 8l+8), the proposal is gathered with warp shuffles and each lane
  * forms 8 rows of U x (mcig_pair.cuh).  Results are bit-identical to the one-lane kernel;
  * the point is latency hiding where one lane per chain leaves few warps per SM (16,384
- * chains: 3.4 warps per SM with one lane at 124 registers, 6.7 with two at 72 registers;
+ * chains: 3.4 warps per SM with one lane at 124 registers, 6.7 with two at 80 registers;
  * measured sampling launch 18.9 against 23.9 ms; at 65,536 chains the one-lane kernel is
  * faster, 35.8 against 41.5 ms).
  * lpc = 4 or 8: a float handle whose single

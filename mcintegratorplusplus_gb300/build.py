@@ -27,6 +27,7 @@ UNITS = {
     "sample_fast_vec": [],
     "sample_fast_pk16": [],
     "sample_fast_pk16o": [],
+    "sample_fast_pk16u": [],
     "sample_fast_pk32": [],
     "sample_fast_pk32d": [],
     "sample_fast_pk32p": [],

@@ -112,8 +112,9 @@ __device__ __forceinline__ bool calib_more(const KParams &p, int cons, int count
 // periodic domain, a single exp(-x.x) or precision-matrix sampling function.  Results (step
 // sizes, walkers, Philox counters, counts of the last iteration) are those of
 // FastSampler::calibrate.  Every lane of a warp stays to the end (the warp's shuffles and
-// ballots name all 32 lanes); lanes without a chain take no part in the sampling.
-template <int MAXD, int PK>
+// ballots name all 32 lanes); lanes without a chain take no part in the sampling.  LEAN: the
+// move's distribution, 1 uniform, 2 Gaussian (FastSampler's LEAN).
+template <int MAXD, int PK, int LEAN>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 8) mcig_calib_kernel(const KParams p, const FastConst fc)
 {
     using CS = CalibSplit<MAXD, PK>;
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 8) mcig_calib_kernel(const KP
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = c < p.nchains && !(p.active && !p.active[c]);
     const int64_t MIN_STAT = p.nsteps;
-    FastSampler<MAXD, MCIG_MOVE_ALL, true, PK, false, true> s(p, fc, live ? c : 0, nullptr); // one step type
+    FastSampler<MAXD, MCIG_MOVE_ALL, true, PK, false, LEAN> s(p, fc, live ? c : 0, nullptr); // one step type
     int cons = 0, counter = 0;
     int64_t na = 0;
     bool done = !live || !calib_more(p, cons, counter);
@@ -182,7 +183,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 8) mcig_calib_kernel(const KP
     float sc[4]; // step sizes of the lane's coordinates (one type: st[0], 0 beyond ndim)
 #pragma unroll
     for (int k = 0; k < 4; ++k) { sc[k] = (4 * l + k < p.ndim) ? st[0] : 0.f; }
-    const bool gauss = p.srrd == MCIG_SRRD_GAUSSIAN;
+    constexpr bool gauss = LEAN == 2;
     bool gdone = !gact;
     while (__any_sync(FULL, !gdone)) {
         float xf[MAXD];
@@ -230,9 +231,9 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 8) mcig_calib_kernel(const KP
     }
 }
 
-template <int MAXD, int PK>
+template <int MAXD, int PK, int LEAN>
 void mcig_calib_launch(const KParams &p, const FastConst *fc, int /*movetype*/, int grid, int block, size_t /*smem*/,
                        cudaStream_t st)
 {
-    mcig_calib_kernel<MAXD, PK><<<grid, block, 0, st>>>(p, *fc);
+    mcig_calib_kernel<MAXD, PK, LEAN><<<grid, block, 0, st>>>(p, *fc);
 }

@@ -1219,7 +1219,7 @@ static int launch(mcig_mci *h, const KParams &kp)
         if (h->f64_decide) { return set_err(MCIG_ERR_UNSUPPORTED, "the FP64-certified decision runs in the multi-lane mixture kernel only (mcig_set_lanes)"); }
         const int k = h->pdfs[0].kind;
         mcig_launch_fn pf = mcig_pair_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, k == MCIG_PDF_GAUSS_PREC ? 2 : 1,
-                                               moments_only(h, kp));
+                                               moments_only(h, kp), h->srrd == MCIG_SRRD_GAUSSIAN);
         if (!pf) { return set_err(MCIG_ERR_UNSUPPORTED, "no two-lane kernel for this configuration"); }
         pf(kp, &h->fc, h->movetype, 0, 0, 0, h->stream);
         ++h->launches;
@@ -1227,7 +1227,8 @@ static int launch(mcig_mci *h, const KParams &kp)
         return MCIG_OK;
     }
     if (family == 2) {
-        mcig_launch_fn lf = mcig_lanes_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, 32, h->lanes > 0 ? h->lanes : 8);
+        mcig_launch_fn lf = mcig_lanes_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, 32, h->lanes > 0 ? h->lanes : 8,
+                                                h->srrd == MCIG_SRRD_GAUSSIAN);
         if (!lf) { return set_err(MCIG_ERR_UNSUPPORTED, "no multi-lane kernel for %d lanes per chain", h->lanes); }
         lf(kp, &h->fc, h->movetype, 0, 0, 0, h->stream);
         ++h->launches;
@@ -1252,12 +1253,12 @@ static int launch(mcig_mci *h, const KParams &kp)
             const int k = h->pdfs[0].kind;
             pk = (k == MCIG_PDF_GAUSS || k == MCIG_PDF_GAUSS_SUM) ? 1 : (k == MCIG_PDF_GAUSS_PREC ? 2 : (k == MCIG_PDF_GAUSS_MIX ? 3 : 0));
         }
-        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk, moments_only(h, kp),
-                                h->ntypes == 1);
+        const int lean = (h->ntypes == 1 && !h->periodic) ? (h->srrd == MCIG_SRRD_GAUSSIAN ? 2 : 1) : 0; // srrd: uniform or Gaussian here
+        fn = mcig_fast_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, h->movetype, maxd_bucket(h->ndim), pk, moments_only(h, kp), lean);
         smem = (size_t)kp.nobsdim * block * 8; // accumulator slots (float2 or double)
         if (kp.mode == KMODE_CALIB && h->calib_split && h->movetype == MCIG_MOVE_ALL && maxd_bucket(h->ndim) == 16 &&
             h->ntypes == 1 && !h->periodic && (pk == 1 || pk == 2)) { // PK_GAUSS, PK_PREC
-            fn = mcig_calib_launcher_pk16(pk); // same results, the tail's chains on four lanes each
+            fn = mcig_calib_launcher_pk16(pk, h->srrd == MCIG_SRRD_GAUSSIAN); // same results, the tail's chains on four lanes each
             smem = 0;
         }
     } else if (uses_plugin(h)) { // the plugin's general kernel over its functors

@@ -164,10 +164,13 @@ template <> struct FastSlot<false> {
 // accumulator.  The kernel then holds only those paths: the general observable code is a
 // runtime choice among every kind and accumulator, which the compiler turns into predicated
 // code that issues the arithmetic of all of them on every step; x.x is formed once a step.
-// ONET: one step-size type, so the step of coordinate i is st[0] (times its 0 / 1 table
-// entry) without the code of the other types (20 registers and 8 % of the sampling time at
-// the 16-D precision-matrix configuration)
-template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, bool ONET = false>
+// LEAN (1: uniform draws, 2: Gaussian draws): one step-size type and the unbound domain, so
+// the step of coordinate i is st[0] (times its 0 / 1 table entry) and the move's distribution
+// is known, without the code of the other types, of the other distribution and of the
+// periodic wrap (at the 16-D precision-matrix configuration 115 -> 95 -> 108 registers with
+// the compile-time distribution, and 13 % of the sampling time: the runtime choices are
+// compiled into predicated code that issues part of every alternative); 0: general
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, int LEAN = 0>
 struct FastSampler {
     using Slot = FastSlot<KAHAN>;
     using ST = typename Slot::T;
@@ -196,7 +199,7 @@ struct FastSampler {
     __device__ __forceinline__ float step_i(int i) const
     {
         float s = st[0] * fc.tw[0][i];
-        if constexpr (ONET) { return s; }
+        if constexpr (LEAN != 0) { return s; }
         if (p.ntypes > 1) {
 #pragma unroll
             for (int t = 1; t < MCIG_MAXTYPES; ++t) { s = fmaf(st[t], fc.tw[t][i], s); }
@@ -214,7 +217,7 @@ struct FastSampler {
     {
         s0 = (uint32_t)ctr;
         s1 = (uint32_t)(ctr >> 32);
-        const bool gauss = p.srrd == MCIG_SRRD_GAUSSIAN;
+        const bool gauss = LEAN == 2 ? true : (LEAN == 1 ? false : p.srrd == MCIG_SRRD_GAUSSIAN);
         float xn[MAXD];
         int lo = 0, hi = p.ndim;
         if constexpr (MOVE == MCIG_MOVE_ALL) { // SRRDAllMove::trialMove
@@ -244,7 +247,7 @@ struct FastSampler {
                 }
             }
         }
-        if (p.periodic) {
+        if (LEAN == 0 && p.periodic) {
 #pragma unroll
             for (int i = 0; i < MAXD; ++i) {
                 if (i >= lo && i < hi) {
@@ -507,7 +510,7 @@ struct FastSampler {
 // Up to 16 dimensions the kernel is held to 128 registers per thread: registers are
 // allocated in steps that make 136 or 144 per thread fit only six 64-thread blocks
 // per SM (912 of the 1,024 blocks of 65,536 chains, so a second wave), 128 fits eight.
-template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, bool ONET = false>
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, int LEAN = 0>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -516,7 +519,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    FastSampler<MAXD, MOVE, KAHAN, PK, MOMENTS, ONET> s(p, fc, c, slots);
+    FastSampler<MAXD, MOVE, KAHAN, PK, MOMENTS, LEAN> s(p, fc, c, slots);
     if (p.mode == KMODE_CALIB) { s.calibrate(p.nsteps); }
     else if (p.mode == KMODE_FUSED) {
         // MCI::integrate's phases for this chain alone: a chain whose calibration converges
@@ -530,11 +533,11 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     s.store_state();
 }
 
-template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY, bool MOMENTS = false, bool ONET = false>
+template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY, bool MOMENTS = false, int LEAN = 0>
 void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, int grid, int block, size_t smem,
                       cudaStream_t st)
 {
-    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS, ONET>;
+    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS, LEAN>;
     // shared memory as large as possible, so the accumulator slots never limit residency
     mcig_smem_attrs((const void *)k, smem);
     k<<<grid, block, smem, st>>>(p, *fc);

@@ -110,7 +110,7 @@ __device__ __noinline__ bool lanes_decide_d(const double *pp, int nd, int nc, in
     return log((double)u) <= (mn + log(sn)) - (mo + log(so));
 }
 
-template <int MAXD, int LPC, bool KAHAN>
+template <int MAXD, int LPC, bool KAHAN, bool GAUSS = true> // GAUSS: Gaussian (else uniform) move draws
 struct LaneMixSampler {
     static_assert(MAXD % (4 * LPC) == 0 && 32 % LPC == 0 && LPC >= 2 && LPC <= 8, "lanes own whole Philox blocks");
     static constexpr int CPL = MAXD / LPC;         // coordinates per lane
@@ -264,7 +264,7 @@ struct LaneMixSampler {
     __device__ __forceinline__ bool step(bool upd)
     {
         const uint32_t s0 = (uint32_t)ctr, s1 = (uint32_t)(ctr >> 32);
-        const bool gauss = p.srrd == MCIG_SRRD_GAUSSIAN;
+        constexpr bool gauss = GAUSS;
         float xn[CPL];
 #pragma unroll
         for (int j = 0; j < BPL; ++j) {
@@ -454,10 +454,10 @@ struct LaneMixSampler {
 template <int MAXD>
 struct LanesTable { static constexpr size_t bytes = (size_t)8 * (MAXD / 2 + 1) * sizeof(float4) + 8 * sizeof(float); };
 
-template <int MAXD, int LPC, bool KAHAN>
+template <int MAXD, int LPC, bool KAHAN, bool GAUSS>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, LPC >= 8 ? 14 : 8) mcig_lanes_kernel(const KParams p, const FastConst fc)
 {
-    using LS = LaneMixSampler<MAXD, LPC, KAHAN>;
+    using LS = LaneMixSampler<MAXD, LPC, KAHAN, GAUSS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4 *tab = (float4 *)smem_raw;
     float *lcn = (float *)(tab + 8 * LS::TS);
@@ -499,11 +499,11 @@ size_t mcig_lanes_smem(const KParams &p, bool kahan)
     return LanesTable<MAXD>::bytes + ns * MCIG_FAST_BLOCK * (kahan ? sizeof(float2) : sizeof(double));
 }
 
-template <int MAXD, int LPC, bool KAHAN>
+template <int MAXD, int LPC, bool KAHAN, bool GAUSS>
 void mcig_lanes_launch(const KParams &p0, const FastConst *fc, int /*movetype*/, int /*grid*/, int /*block*/,
                        size_t /*smem*/, cudaStream_t st)
 {
-    auto k = mcig_lanes_kernel<MAXD, LPC, KAHAN>;
+    auto k = mcig_lanes_kernel<MAXD, LPC, KAHAN, GAUSS>;
     KParams p = p0;
     int ns = 0; // per-lane accumulator slot of each observable
     for (int o = 0; o < p.nobs; ++o) {

@@ -14,24 +14,26 @@ mcig_launch_fn mcig_generic_launcher(int precision, int rng);
 // maxd 4, 8, 16 or 32, pdf set pk (PK_ANY, or PK_GAUSS / PK_PREC / PK_MIX for a single
 // sampling function of that kind); moments: every observable is x or x.x with float Full
 // data or a Simple/Block accumulator (a kernel holding only those paths where one exists);
-// onetype: one step-size type (a kernel without the other types' code where one exists);
-// NULL otherwise
-mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments = 0, int onetype = 0);
+// lean: one step-size type, unbound domain and uniform (1) or Gaussian (2) draws (a kernel
+// without the code of the alternatives where one exists), 0 otherwise; NULL otherwise
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments = 0, int lean = 0);
 
 // step-size calibration (KMODE_CALIB) with the calibration's tail split over lanes
-// (mcig_calib.cuh): all-coordinate move, one step type, no periodic domain, ndim 9..16,
-// one sampling function of kind pk (PK_GAUSS or PK_PREC); NULL otherwise
-mcig_launch_fn mcig_calib_launcher_pk16(int pk);
+// (mcig_calib.cuh): all-coordinate move with uniform (gauss 0) or Gaussian (1) draws, one
+// step type, no periodic domain, ndim 9..16, one sampling function of kind pk (PK_GAUSS or
+// PK_PREC); NULL otherwise
+mcig_launch_fn mcig_calib_launcher_pk16(int pk, int gauss);
 
 // float kernel with several lanes per chain for one mixture sampling function
-// (mcig_lanes.cuh): all-coordinate move, one step type, unbound domain, maxd 32, lpc 4 or 8
-// lanes per chain; NULL otherwise
-mcig_launch_fn mcig_lanes_launcher(int kahan, int maxd, int lpc);
+// (mcig_lanes.cuh): all-coordinate move with uniform (gauss 0) or Gaussian (1) draws, one
+// step type, unbound domain, maxd 32, lpc 4 or 8 lanes per chain; NULL otherwise
+mcig_launch_fn mcig_lanes_launcher(int kahan, int maxd, int lpc, int gauss);
 
 // float kernel with two lanes per chain for one sampling function of kind pk (PK_GAUSS or
 // PK_PREC) in 9..16 coordinates (mcig_pair.cuh): all-coordinate move, one step type,
-// unbound domain; moments as for mcig_fast_launcher; NULL otherwise
-mcig_launch_fn mcig_pair_launcher(int kahan, int pk, int moments = 0);
+// unbound domain; moments as for mcig_fast_launcher; gauss: Gaussian (1) or uniform (0) move
+// draws; NULL otherwise
+mcig_launch_fn mcig_pair_launcher(int kahan, int pk, int moments, int gauss);
 
 // Metropolis-Hastings test of the learned proposal for one sampling function of kind pk
 // (PK_GAUSS, PK_PREC or PK_MIX) at maxd 8, 16 or 32 (flow_accept.cu); NULL otherwise

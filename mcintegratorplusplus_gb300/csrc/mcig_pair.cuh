@@ -6,7 +6,7 @@
 // so 65,536 chains are 12 warps per SM; with three warps per scheduler it issues in little
 // more than half of the cycles, the rest being dependency latency (Philox rounds, the
 // quadratic form's FMA chains, the MUFU of Box-Muller).  Here the two lanes of a chain
-// share its step, so the same chains are twice the warps at about half the registers:
+// share its step, so the same chains are twice the warps at two thirds of the registers:
 //   * lane group l (lanes 16 l .. 16 l + 15, one chain each) owns coordinates [8 l, 8 l + 8),
 //     i.e. the Philox move blocks 2 l and 2 l + 1 of the step, and draws and moves only those;
 //   * the proposal's coordinates reach both lanes by shuffles as U x consumes them; lane
@@ -35,8 +35,9 @@ __host__ __device__ __forceinline__ constexpr int pair_coef_off(int j)
 }
 
 // MOMENTS: every observable is x (XND) or x.x (X2SUM) with float Full data or a Simple/Block
-// accumulator, so only those paths are compiled (FastSampler's MOMENTS)
-template <int PK, bool KAHAN, bool MOMENTS = false>
+// accumulator, so only those paths are compiled (FastSampler's MOMENTS); GAUSS: Gaussian
+// (else uniform) move draws, known at compile time
+template <int PK, bool KAHAN, bool MOMENTS = false, bool GAUSS = true>
 struct PairSampler {
     static_assert(PK == PK_PREC || PK == PK_GAUSS, "the pair kernel serves one precision matrix or exp(-x.x)");
     static constexpr int MAXD = 16;            // coordinates (padded with zero steps)
@@ -155,7 +156,7 @@ struct PairSampler {
             ua = accept_draw<float>(philox4x32_10_rk((uint32_t)ca, (uint32_t)(ca >> 32), (uint32_t)c, TAG_ACCEPT << 12, fc.rk));
         }
         const float u = __shfl_sync(FULL, ua, (int)(r & 1u) * G + k);
-        const bool gauss = p.srrd == MCIG_SRRD_GAUSSIAN;
+        constexpr bool gauss = GAUSS;
         float xn[CPL];
 #pragma unroll
         for (int b = 0; b < CPL / 4; ++b) {
@@ -386,12 +387,13 @@ struct PairSampler {
     }
 };
 
-// 64 threads (two warps, 32 chains) per block; at most 72 registers per thread keep 14
-// blocks on an SM, so 65,536 chains (131,072 lanes) run in one wave of 27 warps per SM
-template <int PK, bool KAHAN, bool MOMENTS>
-__global__ void __launch_bounds__(MCIG_FAST_BLOCK, 14) mcig_pair_kernel(const KParams p, const FastConst fc)
+// 64 threads (two warps, 32 chains) per block; at most 80 registers per thread (no spills)
+// keep 12 blocks on an SM: the chain counts the kernel serves by default (at most 32,768, 6.7
+// blocks per SM) run in one wave
+template <int PK, bool KAHAN, bool MOMENTS, bool GAUSS>
+__global__ void __launch_bounds__(MCIG_FAST_BLOCK, 12) mcig_pair_kernel(const KParams p, const FastConst fc)
 {
-    using PS = PairSampler<PK, KAHAN, MOMENTS>;
+    using PS = PairSampler<PK, KAHAN, MOMENTS, GAUSS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *tab = (float *)smem_raw; // [2][72]: lane group l's coefficients, column-major
     typename PS::ST *slots = (typename PS::ST *)(smem_raw + PS::TAB_BYTES);
@@ -415,12 +417,12 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, 14) mcig_pair_kernel(const KP
     s.store_state();
 }
 
-template <int PK, bool KAHAN, bool MOMENTS = false>
+template <int PK, bool KAHAN, bool MOMENTS, bool GAUSS>
 void mcig_pair_launch(const KParams &p0, const FastConst *fc, int /*movetype*/, int /*grid*/, int /*block*/,
                       size_t /*smem*/, cudaStream_t st)
 {
-    using PS = PairSampler<PK, KAHAN, MOMENTS>;
-    auto k = mcig_pair_kernel<PK, KAHAN, MOMENTS>;
+    using PS = PairSampler<PK, KAHAN, MOMENTS, GAUSS>;
+    auto k = mcig_pair_kernel<PK, KAHAN, MOMENTS, GAUSS>;
     KParams p = p0;
     int ns = 0; // per-lane accumulator slot of each observable
     for (int o = 0; o < p.nobs; ++o) {

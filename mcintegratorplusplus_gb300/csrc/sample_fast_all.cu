@@ -8,7 +8,8 @@
 
 mcig_launch_fn mcig_fast_launcher_vec(int kahan, int maxd);
 mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk, int moments);
-mcig_launch_fn mcig_fast_launcher_pk16_onetype(int kahan, int pk, int moments);
+mcig_launch_fn mcig_fast_launcher_pk16_lean1(int kahan, int pk, int moments);
+mcig_launch_fn mcig_fast_launcher_pk16_lean2(int kahan, int pk, int moments);
 mcig_launch_fn mcig_fast_launcher_pk32(int kahan, int pk);
 
 static mcig_launch_fn launcher_all(int kahan, int maxd)
@@ -21,10 +22,10 @@ static mcig_launch_fn launcher_all(int kahan, int maxd)
     }
 }
 
-mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments, int onetype)
+mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments, int lean)
 {
-    if (move == MCIG_MOVE_ALL && maxd == 16 && onetype) { // one step-size type
-        mcig_launch_fn f = mcig_fast_launcher_pk16_onetype(kahan, pk, moments);
+    if (move == MCIG_MOVE_ALL && maxd == 16 && lean) { // one step-size type, unbound domain, known draws
+        mcig_launch_fn f = lean == 2 ? mcig_fast_launcher_pk16_lean2(kahan, pk, moments) : mcig_fast_launcher_pk16_lean1(kahan, pk, moments);
         if (f) { return f; }
     }
     if (move == MCIG_MOVE_ALL && pk != PK_ANY) { // one-pdf kernels where they exist

@@ -24,12 +24,12 @@ mcig_launch_fn mcig_fast_launcher_pk16(int kahan, int pk, int moments)
 }
 
 // calibration with the split tail (mcig_calib.cuh) for one exp(-x.x) or precision-matrix
-// sampling function; NULL for other kinds
-mcig_launch_fn mcig_calib_launcher_pk16(int pk)
+// sampling function and uniform (gauss 0) or Gaussian (1) draws; NULL for other kinds
+mcig_launch_fn mcig_calib_launcher_pk16(int pk, int gauss)
 {
     switch (pk) {
-    case PK_GAUSS: return mcig_calib_launch<16, PK_GAUSS>;
-    case PK_PREC: return mcig_calib_launch<16, PK_PREC>;
+    case PK_GAUSS: return gauss ? mcig_calib_launch<16, PK_GAUSS, 2> : mcig_calib_launch<16, PK_GAUSS, 1>;
+    case PK_PREC: return gauss ? mcig_calib_launch<16, PK_PREC, 2> : mcig_calib_launch<16, PK_PREC, 1>;
     default: return nullptr;
     }
 }

@@ -1,8 +1,8 @@
 // Register-resident float sampling kernels for one exp(-x.x) or precision-matrix sampling
-// function, all-coordinate move with one step-size type, up to 16 dimensions (mcig_fast.cuh,
-// ONET), with the general observable code or the x / x.x variant (MOMENTS), Kahan float or
-// double block sums.  A unit of its own, so the parallel build compiles it beside
-// sample_fast_pk16.cu.
+// function, all-coordinate move with one step-size type and Gaussian draws, unbound domain, up to 16
+// dimensions (mcig_fast.cuh, LEAN = 2), with the general observable code or the x / x.x
+// variant (MOMENTS), Kahan float or double block sums.  Units of their own, so the parallel
+// build compiles them beside sample_fast_pk16.cu.
 #include "mcig_fast.cuh"
 #include "mcig_launchers.h"
 
@@ -10,12 +10,12 @@ template <int PK>
 static mcig_launch_fn pick(int kahan, int moments)
 {
     if (moments) {
-        return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK, true, true> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK, true, true>;
+        return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK, true, 2> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK, true, 2>;
     }
-    return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK, false, true> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK, false, true>;
+    return kahan ? mcig_fast_launch<16, MCIG_MOVE_ALL, true, PK, false, 2> : mcig_fast_launch<16, MCIG_MOVE_ALL, false, PK, false, 2>;
 }
 
-mcig_launch_fn mcig_fast_launcher_pk16_onetype(int kahan, int pk, int moments)
+mcig_launch_fn mcig_fast_launcher_pk16_lean2(int kahan, int pk, int moments)
 {
     switch (pk) {
     case PK_GAUSS: return pick<PK_GAUSS>(kahan, moments);

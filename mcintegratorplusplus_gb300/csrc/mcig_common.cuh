@@ -156,6 +156,10 @@ struct KParams {
     // reversed, largest float margin of a reversed decision as float bits] (NULL: none)
     int f64_decide;
     unsigned long long *dstats;
+    // register-resident kernel, x / x.x variant: the observables ordered as four groups (Full
+    // x.x, Full x, Simple/Block x.x, Simple/Block x) with these counts (set by its launcher)
+    int mgroup[4];
+    int mgroup_slots;   // at most one observable per group, group g's at obs[g]
 };
 
 // Register-resident kernel only: Philox round keys (key + r*W for r = 0..9), the

@@ -416,6 +416,81 @@ struct FastSampler {
         observe_put(od, k, flush, blk);
     }
 
+    // MOMENTS: observable od of a group whose accumulator (Full or Simple/Block) and kind (x or
+    // x.x) are known at compile time, after step r (the accumulation index and block end of
+    // obs_step; Full data in float).  Without the general code's runtime choice of kind and
+    // accumulator per observable, the step issues only the chosen path.
+    template <bool FULL, bool VEC>
+    __device__ __forceinline__ void obs_group_one(const ObsDesc &od, uint32_t r)
+    {
+        constexpr int NV = VEC ? MAXD : 1;
+        uint32_t k = r;
+        if (od.nskip != 1) {
+            k = fast_div(r, od.sk_magic, od.sk_shift);
+            if (k * (uint32_t)od.nskip != r) { return; }
+        }
+        const uint32_t nc = (uint32_t)p.nchains; // value stride; j * nc < 2^32 for any device array
+        const float *v = VEC ? x : &xx;
+        const bool all = !VEC || p.ndim == MAXD; // every value exists: no predicate per value
+        if constexpr (FULL) {
+            float *dst = (float *)od.data + ((size_t)p.acc_offset + k) * (size_t)od.nv * nc + c;
+            if (all) {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) { dst[j * nc] = v[j]; }
+            } else {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    if (j < od.nv) { dst[j * nc] = v[j]; }
+                }
+            }
+        } else {
+            ST *sl = slots + od.voff * MCIG_FAST_BLOCK + threadIdx.x;
+            if (all) {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) { Slot::add(sl[j * MCIG_FAST_BLOCK], v[j]); }
+            } else {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    if (j < od.nv) { Slot::add(sl[j * MCIG_FAST_BLOCK], v[j]); }
+                }
+            }
+            if (od.acc == MCIG_ACC_BLOCK) {
+                const uint32_t q = fast_div(k + 1, od.bs_magic, od.bs_shift);
+                if (q * (uint32_t)od.bs == k + 1) { // block end: mean of the block, sums reset
+                    double *dst = (double *)od.data + (size_t)(q - 1) * od.nv * nc + c;
+#pragma unroll
+                    for (int j = 0; j < NV; ++j) {
+                        if (all || j < od.nv) {
+                            dst[j * nc] = Slot::get(sl[j * MCIG_FAST_BLOCK]) * od.inv_bs;
+                            Slot::zero(sl[j * MCIG_FAST_BLOCK]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    // MOMENTS: every observable after step r, group by group (FastSampler's launcher orders
+    // them).  With at most one observable per group (mgroup[4] == 1 marks that layout; the
+    // launcher then puts group g's observable, if any, at obs[g]) the groups are straight-line
+    // code over descriptors at fixed parameter offsets (constant-bank operands); otherwise
+    // loops over each group.
+    __device__ __forceinline__ void obs_groups(uint32_t r)
+    {
+        if (p.mgroup_slots) {
+            if (p.mgroup[0]) { obs_group_one<true, false>(p.obs[0], r); }
+            if (p.mgroup[1]) { obs_group_one<true, true>(p.obs[1], r); }
+            if (p.mgroup[2]) { obs_group_one<false, false>(p.obs[2], r); }
+            if (p.mgroup[3]) { obs_group_one<false, true>(p.obs[3], r); }
+            return;
+        }
+        int o = 0;
+        for (int i = 0; i < p.mgroup[0]; ++i, ++o) { obs_group_one<true, false>(p.obs[o], r); }
+        for (int i = 0; i < p.mgroup[1]; ++i, ++o) { obs_group_one<true, true>(p.obs[o], r); }
+        for (int i = 0; i < p.mgroup[2]; ++i, ++o) { obs_group_one<false, false>(p.obs[o], r); }
+        for (int i = 0; i < p.mgroup[3]; ++i, ++o) { obs_group_one<false, true>(p.obs[o], r); }
+    }
+
     // n < 2^32 (checked on the host); accumulation indices in 32-bit arithmetic.
     // The first MCIG_FAST_UNROLLED_OBS observables are unrolled, so their
     // descriptors are constant-bank operands; any further ones loop.
@@ -434,6 +509,8 @@ struct FastSampler {
 #pragma unroll
                 for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); }
                 xx = s;
+                obs_groups(r0 + r);
+                continue;
             }
 #pragma unroll
             for (int o = 0; o < MCIG_FAST_UNROLLED_OBS; ++o) {
@@ -540,5 +617,34 @@ void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, i
     auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS, LEAN>;
     // shared memory as large as possible, so the accumulator slots never limit residency
     mcig_smem_attrs((const void *)k, smem);
+    if constexpr (MOMENTS) { // the observables in four groups (KParams::mgroup), order kept within each
+        KParams q = p;
+        int n = 0, most = 0;
+        for (int g = 0; g < 4; ++g) {
+            q.mgroup[g] = 0;
+            for (int o = 0; o < p.nobs; ++o) {
+                const ObsDesc &od = p.obs[o];
+                const int og = (od.acc == MCIG_ACC_FULL ? 0 : 2) + (od.kind == MCIG_OBS_XND ? 1 : 0);
+                if (og == g) {
+                    q.obs[n++] = od;
+                    ++q.mgroup[g];
+                }
+            }
+            most = q.mgroup[g] > most ? q.mgroup[g] : most;
+        }
+        q.mgroup_slots = most <= 1;
+        if (q.mgroup_slots) { // group g's observable at obs[g] (the Simple finalize reads every slot < nobs)
+            KParams r = q;
+            int o = 0;
+            for (int g = 0; g < 4; ++g) {
+                if (q.mgroup[g]) { r.obs[g] = q.obs[o++]; }
+                else { r.obs[g] = ObsDesc{}; r.obs[g].acc = -1; }
+            }
+            r.nobs = 4;
+            q = r;
+        }
+        k<<<grid, block, smem, st>>>(q, *fc);
+        return;
+    }
     k<<<grid, block, smem, st>>>(p, *fc);
 }

@@ -13,8 +13,8 @@ struct BatchPhase {
 
 // one work item of the persistent launch: `count` (<= 32) consecutive chains of one
 // integral, one chain per lane of the warp that takes it; `variant` selects the code:
-// 0 the general sampler, 1 + u the block-separable sampler with its sub-step loop
-// unrolled 2^u times
+// 0 the general sampler, 1 + u (uniform sub-moves) or 4 + u (Gaussian sub-moves) the
+// block-separable sampler with its sub-step loop unrolled 2^u times
 struct BatchTask {
     int integral;
     int chain0;

@@ -2632,7 +2632,7 @@ static int batch_upload_tasks(mcig_batch *b)
 {
     for (int t = 0; t < b->ntasks; ++t) {
         BatchTask &k = b->htasks[t];
-        k.variant = b->bs[k.integral] ? 1 + b->unroll[b->task_bucket[t]] : 0;
+        k.variant = b->bs[k.integral] ? 1 + b->unroll[b->task_bucket[t]] + (b->hs[k.integral]->ms_srrd == MCIG_SRRD_GAUSSIAN ? 3 : 0) : 0;
     }
     CK(cudaMemcpy(b->tasks.p, b->htasks.data(), b->ntasks * sizeof(BatchTask), cudaMemcpyHostToDevice));
     return MCIG_OK;

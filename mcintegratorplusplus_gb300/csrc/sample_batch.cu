@@ -35,7 +35,7 @@ struct BatchLayout {
     }
 };
 
-template <bool KAHAN, int UNR>
+template <bool KAHAN, int UNR, bool GAUSS> // GAUSS: Gaussian (else uniform) sub-move draws
 struct BlockSepSampler {
     using Slot = FastSlot<KAHAN>;
     using ST = typename Slot::T;
@@ -87,11 +87,11 @@ struct BlockSepSampler {
     }
 
     // the draw of coordinate i in sub-step `sub`: move_draws<float> of block i / 4, entry i % 4
-    __device__ __forceinline__ float draw1(uint32_t sub, int i, bool gauss) const
+    __device__ __forceinline__ float draw1(uint32_t sub, int i) const
     {
         const P4 q = block(sub, TAG_MOVE, (uint32_t)(i >> 2));
         const int k = i & 3;
-        if (gauss) {
+        if constexpr (GAUSS) {
             float z0, z1;
             box_muller_f(k < 2 ? q.a : q.c, k < 2 ? q.b : q.d, z0, z1);
             return (k & 1) ? z1 : z0;
@@ -106,7 +106,6 @@ struct BlockSepSampler {
     {
         s0 = (uint32_t)ctr;
         s1 = (uint32_t)(ctr >> 32);
-        const bool gauss = p.ms_srrd == MCIG_SRRD_GAUSSIAN;
         float dsub = 0.f; // log sub-density change of the sub-chain
         float dout = 0.f; // log change of the sampling functions
         int nu = 0;
@@ -116,7 +115,7 @@ struct BlockSepSampler {
             const uint32_t sub = 1 + s;
             const int i = (int)__umulhi(block(sub, TAG_INDEX, 0).a, (uint32_t)p.ndim);
             const float xi = xs[i * ws];
-            const float xn = fmaf(st[0], draw1(sub, i, gauss), xi);
+            const float xn = fmaf(st[0], draw1(sub, i), xi);
             const float diff = xn * xn - xi * xi;
             float dl = 0.f, dp = 0.f;
             bool in[MR];
@@ -244,11 +243,11 @@ struct BlockSepSampler {
     }
 };
 
-template <bool KAHAN, int UNR>
+template <bool KAHAN, int UNR, bool GAUSS>
 __device__ __noinline__ void batch_run_bs(const KParams &p, const BatchPhase &q, const BatchSep &b, int c, unsigned char *smem,
                                           BatchLayout lay)
 {
-    using BS = BlockSepSampler<KAHAN, UNR>;
+    using BS = BlockSepSampler<KAHAN, UNR, GAUSS>;
     using ST = typename BS::ST;
     const size_t ws = blockDim.x;
     float *xs = (float *)smem + threadIdx.x;
@@ -284,10 +283,13 @@ __global__ void __launch_bounds__(256, 3) mcig_batch_kernel(const KParams *__res
         if constexpr (std::is_same<R, float>::value && RNG == RNG_PHILOX) {
             if (task.variant > 0) {
                 const BatchSep &b = sep[task.integral];
-                switch (task.variant) {
-                case 1: batch_run_bs<KAHAN, 1>(p, q, b, c, smem_raw, lay); break;
-                case 2: batch_run_bs<KAHAN, 2>(p, q, b, c, smem_raw, lay); break;
-                default: batch_run_bs<KAHAN, 4>(p, q, b, c, smem_raw, lay); break;
+                switch (task.variant) { // 1 + unroll index, + 3 for Gaussian sub-moves
+                case 1: batch_run_bs<KAHAN, 1, false>(p, q, b, c, smem_raw, lay); break;
+                case 2: batch_run_bs<KAHAN, 2, false>(p, q, b, c, smem_raw, lay); break;
+                case 3: batch_run_bs<KAHAN, 4, false>(p, q, b, c, smem_raw, lay); break;
+                case 4: batch_run_bs<KAHAN, 1, true>(p, q, b, c, smem_raw, lay); break;
+                case 5: batch_run_bs<KAHAN, 2, true>(p, q, b, c, smem_raw, lay); break;
+                default: batch_run_bs<KAHAN, 4, true>(p, q, b, c, smem_raw, lay); break;
                 }
                 continue;
             }

@@ -163,10 +163,12 @@ public:
     void setPrecision(Precision p) { detail::check(mcig_set_precision(_h, static_cast<int>(p))); }
     // device tuning without a counterpart in mci::MCI (results unchanged, include/mcig.h):
     // kernel choice 0 automatic / 1 general / 2 register-resident, the calibration's tail on
-    // four lanes per chain (default on), the three phases in one launch (default off)
+    // four lanes per chain (default on), the three phases in one launch (default off), lanes
+    // per chain of the multi-lane kernels (0 automatic, 1, 2, 4, 8)
     void setKernel(int policy) { detail::check(mcig_set_kernel(_h, policy)); }
     void setCalibrationSplit(bool on) { detail::check(mcig_set_calibration_split(_h, on ? 1 : 0)); }
     void setPhaseFusion(bool on) { detail::check(mcig_set_phase_fusion(_h, on ? 1 : 0)); }
+    void setLanes(int lanes_per_chain) { detail::check(mcig_set_lanes(_h, lanes_per_chain)); }
 
     // --- domain
     void setIRange(double lb, double ub)

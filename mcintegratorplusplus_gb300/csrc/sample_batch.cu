@@ -261,10 +261,12 @@ __device__ __noinline__ void batch_run_bs(const KParams &p, const BatchPhase &q,
     s.store_state();
 }
 
-// at most 85 registers: the block-separable sampler's occupancy (the general sampler keeps its
-// walker arrays in local memory either way)
+// at most 128 registers: the block-separable sampler runs without spills (at 85 registers it
+// spilled 100-900 bytes per thread in its step loop), and 16 warps per SM still hold every task
+// of a batch of ~64,000 chains at once (13 warps per SM); the general sampler keeps its walker
+// arrays in local memory either way
 template <class R, int RNG, bool KAHAN>
-__global__ void __launch_bounds__(256, 3) mcig_batch_kernel(const KParams *__restrict__ cfg, const BatchPhase *__restrict__ ph,
+__global__ void __launch_bounds__(256, 2) mcig_batch_kernel(const KParams *__restrict__ cfg, const BatchPhase *__restrict__ ph,
                                                             const BatchSep *__restrict__ sep, const BatchTask *__restrict__ tasks,
                                                             int ntasks, int *counter, BatchLayout lay)
 {

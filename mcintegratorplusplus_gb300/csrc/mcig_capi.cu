@@ -1153,14 +1153,21 @@ static bool lanes_eligible(const mcig_mci *h)
 }
 
 // every observable of the launch is x or x.x with float Full data or a Simple/Block
-// accumulator: the register-resident kernels have variants holding only those paths
+// accumulator: the register-resident kernels have variants holding only those paths (1), and,
+// where ndim fills the 16-coordinate kernel, every nskip is 1 and each of the four groups (Full
+// x.x, Full x, Simple/Block x.x, Simple/Block x) has exactly one observable, a straight-line
+// variant for that layout (2)
 static int moments_only(const mcig_mci *h, const KParams &kp)
 {
+    int grp[4] = {0, 0, 0, 0}, nskip1 = 1;
     for (size_t o = 0; o < h->obs.size(); ++o) {
         const ObsDesc &od = kp.obs[o];
         if ((od.kind != MCIG_OBS_XND && od.kind != MCIG_OBS_X2SUM) || (od.acc == MCIG_ACC_FULL && !od.full32)) { return 0; }
+        ++grp[(od.acc == MCIG_ACC_FULL ? 0 : 2) + (od.kind == MCIG_OBS_XND ? 1 : 0)];
+        nskip1 &= od.nskip == 1;
     }
-    return 1;
+    const bool fixed4 = h->ndim == 16 && nskip1 && grp[0] == 1 && grp[1] == 1 && grp[2] == 1 && grp[3] == 1;
+    return fixed4 ? 2 : 1;
 }
 
 // Chain counts up to which the two-lane kernel serves its configurations by default, unless
@@ -1219,7 +1226,7 @@ static int launch(mcig_mci *h, const KParams &kp)
         if (h->f64_decide) { return set_err(MCIG_ERR_UNSUPPORTED, "the FP64-certified decision runs in the multi-lane mixture kernel only (mcig_set_lanes)"); }
         const int k = h->pdfs[0].kind;
         mcig_launch_fn pf = mcig_pair_launcher(h->prec == MCIG_PREC_FP32 ? 1 : 0, k == MCIG_PDF_GAUSS_PREC ? 2 : 1,
-                                               moments_only(h, kp), h->srrd == MCIG_SRRD_GAUSSIAN);
+                                               moments_only(h, kp) ? 1 : 0, h->srrd == MCIG_SRRD_GAUSSIAN);
         if (!pf) { return set_err(MCIG_ERR_UNSUPPORTED, "no two-lane kernel for this configuration"); }
         pf(kp, &h->fc, h->movetype, 0, 0, 0, h->stream);
         ++h->launches;

@@ -170,7 +170,10 @@ template <> struct FastSlot<false> {
 // periodic wrap (at the 16-D precision-matrix configuration 115 -> 95 -> 108 registers with
 // the compile-time distribution, and 13 % of the sampling time: the runtime choices are
 // compiled into predicated code that issues part of every alternative); 0: general
-template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, int LEAN = 0>
+// FIXED4 (with MOMENTS): exactly one observable in each of the four groups (Full x.x, Full x,
+// Simple/Block x.x, Simple/Block x), every nskip 1 and ndim == MAXD: the observable step is one
+// straight-line block with no test of its layout
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, int LEAN = 0, bool FIXED4 = false>
 struct FastSampler {
     using Slot = FastSlot<KAHAN>;
     using ST = typename Slot::T;
@@ -425,13 +428,13 @@ struct FastSampler {
     {
         constexpr int NV = VEC ? MAXD : 1;
         uint32_t k = r;
-        if (od.nskip != 1) {
+        if (!FIXED4 && od.nskip != 1) {
             k = fast_div(r, od.sk_magic, od.sk_shift);
             if (k * (uint32_t)od.nskip != r) { return; }
         }
         const uint32_t nc = (uint32_t)p.nchains; // value stride; j * nc < 2^32 for any device array
         const float *v = VEC ? x : &xx;
-        const bool all = !VEC || p.ndim == MAXD; // every value exists: no predicate per value
+        const bool all = FIXED4 || !VEC || p.ndim == MAXD; // every value exists: no predicate per value
         if constexpr (FULL) {
             float *dst = (float *)od.data + ((size_t)p.acc_offset + k) * (size_t)od.nv * nc + c;
             if (all) {
@@ -509,7 +512,14 @@ struct FastSampler {
 #pragma unroll
                 for (int i = 0; i < MAXD; ++i) { s = fmaf(x[i], x[i], s); }
                 xx = s;
-                obs_groups(r0 + r);
+                if constexpr (FIXED4) {
+                    obs_group_one<true, false>(p.obs[0], r0 + r);
+                    obs_group_one<true, true>(p.obs[1], r0 + r);
+                    obs_group_one<false, false>(p.obs[2], r0 + r);
+                    obs_group_one<false, true>(p.obs[3], r0 + r);
+                } else {
+                    obs_groups(r0 + r);
+                }
                 continue;
             }
 #pragma unroll
@@ -587,7 +597,7 @@ struct FastSampler {
 // Up to 16 dimensions the kernel is held to 128 registers per thread: registers are
 // allocated in steps that make 136 or 144 per thread fit only six 64-thread blocks
 // per SM (912 of the 1,024 blocks of 65,536 chains, so a second wave), 128 fits eight.
-template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, int LEAN = 0>
+template <int MAXD, int MOVE, bool KAHAN, int PK, bool MOMENTS = false, int LEAN = 0, bool FIXED4 = false>
 __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast_kernel(const KParams p, const FastConst fc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -596,7 +606,7 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= p.nchains) { return; }
     if (p.active && !p.active[c]) { return; }
-    FastSampler<MAXD, MOVE, KAHAN, PK, MOMENTS, LEAN> s(p, fc, c, slots);
+    FastSampler<MAXD, MOVE, KAHAN, PK, MOMENTS, LEAN, FIXED4> s(p, fc, c, slots);
     if (p.mode == KMODE_CALIB) { s.calibrate(p.nsteps); }
     else if (p.mode == KMODE_FUSED) {
         // MCI::integrate's phases for this chain alone: a chain whose calibration converges
@@ -610,11 +620,11 @@ __global__ void __launch_bounds__(MCIG_FAST_BLOCK, MAXD <= 16 ? 8 : 2) mcig_fast
     s.store_state();
 }
 
-template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY, bool MOMENTS = false, int LEAN = 0>
+template <int MAXD, int MOVE, bool KAHAN, int PK = PK_ANY, bool MOMENTS = false, int LEAN = 0, bool FIXED4 = false>
 void mcig_fast_launch(const KParams &p, const FastConst *fc, int /*movetype*/, int grid, int block, size_t smem,
                       cudaStream_t st)
 {
-    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS, LEAN>;
+    auto k = mcig_fast_kernel<MAXD, MOVE, KAHAN, PK, MOMENTS, LEAN, FIXED4>;
     // shared memory as large as possible, so the accumulator slots never limit residency
     mcig_smem_attrs((const void *)k, smem);
     if constexpr (MOMENTS) { // the observables in four groups (KParams::mgroup), order kept within each

@@ -12,8 +12,10 @@ mcig_launch_fn mcig_generic_launcher(int precision, int rng);
 
 // register-resident float kernel (mcig_fast.cuh): move MCIG_MOVE_ALL / MCIG_MOVE_VEC,
 // maxd 4, 8, 16 or 32, pdf set pk (PK_ANY, or PK_GAUSS / PK_PREC / PK_MIX for a single
-// sampling function of that kind); moments: every observable is x or x.x with float Full
-// data or a Simple/Block accumulator (a kernel holding only those paths where one exists);
+// sampling function of that kind); moments: 1 every observable is x or x.x with float Full
+// data or a Simple/Block accumulator (a kernel holding only those paths where one exists), 2
+// besides that one observable per group (Full x.x, Full x, Simple/Block x.x, Simple/Block x),
+// nskip 1 and ndim == maxd (a straight-line variant where one exists);
 // lean: one step-size type, unbound domain and uniform (1) or Gaussian (2) draws (a kernel
 // without the code of the alternatives where one exists), 0 otherwise; NULL otherwise
 mcig_launch_fn mcig_fast_launcher(int kahan, int move, int maxd, int pk, int moments = 0, int lean = 0);

@@ -173,10 +173,12 @@ def test_chunked_sampling_equals_one_launch(nskip):
             off += nv_of[o]
 
 
-def _moments_run(mcig, prec, pdf, ndim, extra):
+def _moments_run(mcig, prec, pdf, ndim, extra, second_xx=False):
     """Observables x.x and x_i in Block and float Full accumulators (the kernel variant that
-    holds only those paths); extra: one more observable (a constant, Simple) that makes the
-    launch take the general observable code instead."""
+    holds only those paths; at ndim 16 with one observable per group its straight-line layout);
+    second_xx: one more x.x Full observable, every 2nd step (two in a group: the grouped
+    loops); extra: one more observable (a constant, Simple) that makes the launch take the
+    general observable code instead."""
     nc, nmc, nb = 300, 1200, 12
     m = mcig.MCI(ndim, nc, precision=prec)
     m.setSeed(21)
@@ -194,26 +196,31 @@ def _moments_run(mcig, prec, pdf, ndim, extra):
     m.addObservable(mcig.OBS_XND, (), nmc // nb, 1, False, mcig.EST_UNCORRELATED)
     m.addObservable(mcig.OBS_X2SUM, (), 1, 1, False, mcig.EST_UNCORRELATED)
     m.addObservable(mcig.OBS_XND, (), 1, 1, False, mcig.EST_UNCORRELATED)
+    if second_xx:
+        m.addObservable(mcig.OBS_X2SUM, (), 1, 2, False, mcig.EST_UNCORRELATED)
     if extra:
         m.addObservable(mcig.OBS_CONST, (2.5,), 0, 1, False, mcig.EST_NOOP)
     avg, err = m.integrate(nmc)
     ca, ce = m.getChainResults()
-    nv = 2 + 2 * ndim
+    nv = 2 + 2 * ndim + (1 if second_xx else 0)
     out = {"avg": avg[:nv], "err": err[:nv], "ca": ca[:, :nv], "ce": ce[:, :nv], "x": m.getX(),
            "steps": m.getMRT2Steps(), "ctr": m.getStepCounters(), "counts": np.stack(m.getCounts())}
-    for o in range(4):
+    for o in range(5 if second_xx else 4):
         out["data%d" % o] = m.getObsData(o)
     return out
 
 
-@pytest.mark.parametrize("prec_name,pdf,ndim", [("PREC_FP32", "prec", 16), ("PREC_FP32_ACC64", "prec", 16),
-                                                ("PREC_FP32", "gauss", 11)])
-def test_moments_kernel_equals_general_observable_code(prec_name, pdf, ndim):
-    """The register-resident kernel holding only the x and x.x observable paths gives the
-    general observable code's values bit for bit (same float products and sums)."""
+@pytest.mark.parametrize("prec_name,pdf,ndim,second_xx", [("PREC_FP32", "prec", 16, False),
+                                                          ("PREC_FP32_ACC64", "prec", 16, False),
+                                                          ("PREC_FP32", "prec", 16, True),
+                                                          ("PREC_FP32", "gauss", 11, False)])
+def test_moments_kernel_equals_general_observable_code(prec_name, pdf, ndim, second_xx):
+    """The register-resident kernel holding only the x and x.x observable paths (straight-line
+    for one observable per group, grouped loops otherwise) gives the general observable code's
+    values bit for bit (same float products and sums)."""
     import mcintegratorplusplus_gb300 as mcig
     prec = getattr(mcig, prec_name)
-    a = _moments_run(mcig, prec, pdf, ndim, False)
-    b = _moments_run(mcig, prec, pdf, ndim, True)
+    a = _moments_run(mcig, prec, pdf, ndim, False, second_xx)
+    b = _moments_run(mcig, prec, pdf, ndim, True, second_xx)
     for k in a:
         assert np.array_equal(a[k], b[k]), k

@@ -50,8 +50,8 @@ NBLOCKS = 100
 METRIC = "effective samples/s on 1 GB300 at matched std-error: learned/batched vs plain MH"
 # ncu figures of the sampling launch (65,536 chains, 600 steps, 6 blocks of 100, four
 # accumulators): DRAM bytes read + written, and warp instructions per warp-step
-CAPTURE_DRAM_BYTES = 10.26e6 + 2.6776e9
-INST_PER_WARP_STEP = 914.0
+CAPTURE_DRAM_BYTES = 9.70e6 + 2.6774e9
+INST_PER_WARP_STEP = 851.0
 
 
 def target(seed=2024):
@@ -273,7 +273,7 @@ def run_gpu(args):
                      "frac": achieved / float(pk["hbm_gbs"]), "traffic": traffic, "peak_source": pk_kind,
                      "traffic_source": "ncu dram__bytes_read+write of a 600-step capture of this launch "
                                        "(65,536 chains), scaled by chains x steps",
-                     "kernel": "sampling launch (mcig_fast_kernel<16,ALL,Kahan,PREC,moments,lean Gaussian>)",
+                     "kernel": "sampling launch (mcig_fast_kernel<16,ALL,Kahan,PREC,moments,lean Gaussian,fixed4>)",
                      "algorithmic_bytes_per_launch": algo_bytes, "kernel_ms": samp_ms,
                      "fp32_flop_per_step": flop_per_step},
         "issue_roofline": {"bound": "instruction issue", "warp_inst_per_warp_step": INST_PER_WARP_STEP,

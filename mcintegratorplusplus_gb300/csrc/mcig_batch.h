@@ -11,8 +11,9 @@ struct BatchPhase {
     int movetype;
 };
 
-// one work item of the persistent launch: `count` (<= 32) consecutive chains of one
-// integral, one chain per lane of the warp that takes it; `variant` selects the code:
+// one work item of the persistent launch: `count` (<= 32) chains, one per lane of the warp
+// that takes it (their integrals and indices in the task's BatchLane entries; `integral` and
+// `chain0` name the first); `variant`, common to them, selects the code:
 // 0 the general sampler, 1 + u (uniform sub-moves) or 4 + u (Gaussian sub-moves) the
 // block-separable sampler with its sub-step loop unrolled 2^u times
 struct BatchTask {
@@ -20,6 +21,14 @@ struct BatchTask {
     int chain0;
     int count;
     int variant;
+};
+
+// the chain a lane of a task runs: tasks pack up to 32 chains of possibly different integrals
+// of the same code variant (BatchTask::integral / chain0 then name the first), so that
+// integrals with fewer than 32 chains do not leave a warp's other lanes idle
+struct BatchLane {
+    int integral;
+    int chain;
 };
 
 #define MCIG_BS_MAXR 4   // sums of x_i^2 over coordinate ranges kept by the block-separable sampler
@@ -52,8 +61,8 @@ struct BatchSeries {
 // block-separable sampler's shared memory per lane (largest ndim, observable values and
 // MultiStepMove sub-steps of its integrals)
 void mcig_batch_launch(int prec, int rng, const KParams *cfg, const BatchPhase *ph, const BatchSep *sep,
-                       const BatchTask *tasks, int ntasks, int *counter, int grid, int block, int walk, int nslot,
-                       int nundo, cudaStream_t st);
+                       const BatchTask *tasks, const BatchLane *lanes, int ntasks, int *counter, int grid, int block,
+                       int walk, int nslot, int nundo, cudaStream_t st);
 // resident blocks per SM of the launch at this block size, for sizing the persistent grid
 int mcig_batch_blocks_per_sm(int prec, int rng, int block, int walk, int nslot, int nundo);
 void mcig_batch_estimate_launch(const BatchSeries *series, int nseries, double *avg, double *err, cudaStream_t st);

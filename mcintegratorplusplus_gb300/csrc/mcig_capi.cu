@@ -2547,6 +2547,8 @@ struct mcig_batch {
     DBuf<BatchSep> sep;
     DBuf<BatchTask> tasks;
     std::vector<BatchTask> htasks;
+    DBuf<BatchLane> lanes;                // [ntasks][32]: the chain of each lane of each task
+    std::vector<BatchLane> hlanes;
     std::vector<int> task_bucket;         // ndim bucket of each task (for the per-bucket unroll)
     std::vector<char> bs;                 // integral served by the block-separable sampler
     int ntasks = 0;
@@ -2662,7 +2664,7 @@ static int batch_build_graph(mcig_batch *b)
     const int grid = batch_grid(b, b->block); // occupancy query before the capture starts
     CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(b->counter.p, 0, sizeof(int), b->st);
-    mcig_batch_launch(b->prec, b->rng, b->cfg.p, b->ph.p, b->sep.p, b->tasks.p, b->ntasks, b->counter.p, grid, b->block,
+    mcig_batch_launch(b->prec, b->rng, b->cfg.p, b->ph.p, b->sep.p, b->tasks.p, b->lanes.p, b->ntasks, b->counter.p, grid, b->block,
                       b->walk, b->nslot, b->nundo, b->st);
     if (b->nseries) {
         mcig_batch_estimate_launch(b->series.p, b->nseries, b->s_avg.p, b->s_err.p, b->st);
@@ -2682,7 +2684,7 @@ extern "C" int mcig_batch_destroy(mcig_batch *b)
     if (b->st) { cudaStreamSynchronize(b->st); }
     if (b->gexec) { cudaGraphExecDestroy(b->gexec); }
     if (b->graph) { cudaGraphDestroy(b->graph); }
-    b->cfg.release(); b->ph.release(); b->sep.release(); b->tasks.release(); b->counter.release();
+    b->cfg.release(); b->ph.release(); b->sep.release(); b->tasks.release(); b->lanes.release(); b->counter.release();
     b->series.release(); b->s_avg.release(); b->s_err.release();
     if (b->h_avg) { cudaFreeHost(b->h_avg); }
     if (b->h_err) { cudaFreeHost(b->h_err); }
@@ -2731,7 +2733,14 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
     std::vector<BatchPhase> ph(n);
     std::vector<BatchSep> sep(n);
     b->bs.assign(n, 0);
-    std::vector<std::pair<double, std::pair<BatchTask, int>>> tl; // (cost, (task, bucket))
+    // every chain with its cost and packing key (code variant: sampler, ndim bucket, sub-move
+    // distribution); the chains are packed into tasks below
+    struct ChainItem {
+        double cost;
+        int key, bucket;
+        BatchLane lane;
+    };
+    std::vector<ChainItem> items;
     int rc = MCIG_OK;
     for (int i = 0; i < n && !rc; ++i) {
         mcig_mci *h = handles[i];
@@ -2760,28 +2769,44 @@ extern "C" int mcig_batch_create(mcig_mci **handles, int n, const int64_t *nmc, 
         const double per_step = b->bs[i] ? (double)(2 + 3 * h->ms_nsteps) :
                                 (double)(h->ndim + 8) * (h->movetype == MCIG_MOVE_MULTISTEP ? 1 + h->ms_nsteps : 1);
         const double cost = (double)(nmc[i] + (ph[i].do_find ? 10 * ph[i].min_stat : 0) + ph[i].ndecorr) * per_step;
-        for (int64_t c0 = 0; c0 < h->nchains; c0 += 32) {
-            BatchTask t{i, (int)c0, (int)std::min<int64_t>(32, h->nchains - c0), 0};
-            tl.push_back({cost, {t, bucket_of(h->ndim)}});
-        }
+        const int key = (b->bs[i] ? 16 : 0) + 2 * bucket_of(h->ndim) + (h->ms_srrd == MCIG_SRRD_GAUSSIAN ? 1 : 0);
+        for (int64_t c = 0; c < h->nchains; ++c) { items.push_back({cost, key, bucket_of(h->ndim), {i, (int)c}}); }
     }
-    // one queue over the whole batch, longest first: the tail holds the short items
+    // tasks of 32 lanes: within a packing key, chains of similar cost side by side (cost
+    // descending), so a warp's lanes finish together and integrals with few chains share a
+    // warp; then one queue over the whole batch, longest first, so the tail holds the short items
+    std::stable_sort(items.begin(), items.end(), [](const ChainItem &x, const ChainItem &y) {
+        return x.key != y.key ? x.key < y.key : x.cost > y.cost;
+    });
+    std::vector<std::pair<double, std::pair<BatchTask, int>>> tl; // (cost, (task, first item))
+    for (size_t a = 0; a < items.size();) {
+        size_t e = a + 1;
+        while (e < items.size() && e - a < 32 && items[e].key == items[a].key) { ++e; }
+        BatchTask t{items[a].lane.integral, items[a].lane.chain, (int)(e - a), 0};
+        tl.push_back({items[a].cost, {t, (int)a}});
+        a = e;
+    }
     std::stable_sort(tl.begin(), tl.end(), [](const std::pair<double, std::pair<BatchTask, int>> &x,
                                               const std::pair<double, std::pair<BatchTask, int>> &y) { return x.first > y.first; });
     b->ntasks = (int)tl.size();
-    for (auto &e : tl) {
+    b->hlanes.assign((size_t)std::max(b->ntasks, 1) * 32, BatchLane{-1, -1});
+    for (int t = 0; t < b->ntasks; ++t) {
+        const auto &e = tl[t];
         b->htasks.push_back(e.second.first);
-        b->task_bucket.push_back(e.second.second);
+        b->task_bucket.push_back(items[e.second.second].bucket);
+        for (int l = 0; l < e.second.first.count; ++l) { b->hlanes[(size_t)t * 32 + l] = items[e.second.second + l].lane; }
     }
     if (!rc) { rc = b->cfg.alloc(n); }
     if (!rc) { rc = b->ph.alloc(n); }
     if (!rc) { rc = b->sep.alloc(n); }
     if (!rc) { rc = b->tasks.alloc(std::max(b->ntasks, 1)); }
+    if (!rc) { rc = b->lanes.alloc(b->hlanes.size()); }
     if (!rc) { rc = b->counter.alloc(1); }
     if (rc) { mcig_batch_destroy(b); return rc; }
     cudaMemcpy(b->cfg.p, cfg.data(), n * sizeof(KParams), cudaMemcpyHostToDevice);
     cudaMemcpy(b->ph.p, ph.data(), n * sizeof(BatchPhase), cudaMemcpyHostToDevice);
     cudaMemcpy(b->sep.p, sep.data(), n * sizeof(BatchSep), cudaMemcpyHostToDevice);
+    cudaMemcpy(b->lanes.p, b->hlanes.data(), b->hlanes.size() * sizeof(BatchLane), cudaMemcpyHostToDevice);
     if ((rc = batch_upload_tasks(b))) { mcig_batch_destroy(b); return rc; }
     // estimator series: every (handle, observable, chain, value)
     std::vector<BatchSeries> ser;
@@ -2906,7 +2931,7 @@ static int batch_time(mcig_batch *b, float *ms)
     const int grid = batch_grid(b, b->block);
     CK(cudaMemsetAsync(b->counter.p, 0, sizeof(int), b->st));
     CK(cudaEventRecord(b->t0, b->st));
-    mcig_batch_launch(b->prec, b->rng, b->cfg.p, b->ph.p, b->sep.p, b->tasks.p, b->ntasks, b->counter.p, grid, b->block,
+    mcig_batch_launch(b->prec, b->rng, b->cfg.p, b->ph.p, b->sep.p, b->tasks.p, b->lanes.p, b->ntasks, b->counter.p, grid, b->block,
                       b->walk, b->nslot, b->nundo, b->st);
     CK(cudaEventRecord(b->t1, b->st));
     CK(cudaStreamSynchronize(b->st));

@@ -1,9 +1,11 @@
 // Persistent batched sampling kernel: many independent integrals (each its own KParams:
 // dimension, sampling functions, move, observables, seed) in ONE launch.  The warps pull
 // work items from one atomic queue sorted longest-first over the whole batch; an item is
-// up to 32 consecutive chains of one integral, one chain per lane, and each lane runs the
-// whole of MCI::integrate for its chain (findMRT2Step, burn-in, sampling with the
-// accumulators; reference src/MCIntegrator.cpp:43-82).
+// up to 32 chains of integrals that share a code variant (chains of similar cost side by
+// side, so small integrals share a warp instead of leaving its lanes idle), one chain per
+// lane (`BatchLane`), and each lane runs the whole of MCI::integrate for its chain
+// (findMRT2Step, burn-in, sampling with the accumulators; reference
+// src/MCIntegrator.cpp:43-82).
 //
 // Two codes run in the same launch, chosen per item:
 //  * the block-separable sampler (below) for the uneven-batch form: MultiStepMove of
@@ -268,7 +270,8 @@ __device__ __noinline__ void batch_run_bs(const KParams &p, const BatchPhase &q,
 template <class R, int RNG, bool KAHAN>
 __global__ void __launch_bounds__(256, 2) mcig_batch_kernel(const KParams *__restrict__ cfg, const BatchPhase *__restrict__ ph,
                                                             const BatchSep *__restrict__ sep, const BatchTask *__restrict__ tasks,
-                                                            int ntasks, int *counter, BatchLayout lay)
+                                                            const BatchLane *__restrict__ lanes, int ntasks, int *counter,
+                                                            BatchLayout lay)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -279,12 +282,13 @@ __global__ void __launch_bounds__(256, 2) mcig_batch_kernel(const KParams *__res
         if (t >= ntasks) { break; }
         const BatchTask task = tasks[t];
         if (lane >= task.count) { continue; }
-        const KParams &p = cfg[task.integral];
-        const BatchPhase &q = ph[task.integral];
-        const int c = task.chain0 + lane;
+        const BatchLane li = lanes[(size_t)t * 32 + lane]; // this lane's integral and chain
+        const KParams &p = cfg[li.integral];
+        const BatchPhase &q = ph[li.integral];
+        const int c = li.chain;
         if constexpr (std::is_same<R, float>::value && RNG == RNG_PHILOX) {
             if (task.variant > 0) {
-                const BatchSep &b = sep[task.integral];
+                const BatchSep &b = sep[li.integral];
                 switch (task.variant) { // 1 + unroll index, + 3 for Gaussian sub-moves
                 case 1: batch_run_bs<KAHAN, 1, false>(p, q, b, c, smem_raw, lay); break;
                 case 2: batch_run_bs<KAHAN, 2, false>(p, q, b, c, smem_raw, lay); break;
@@ -311,13 +315,14 @@ static size_t smem_k(const BatchLayout &lay, int block)
 }
 
 template <class R, int RNG, bool KAHAN>
-static void launch_k(const KParams *cfg, const BatchPhase *ph, const BatchSep *sep, const BatchTask *tasks, int ntasks,
-                     int *counter, int grid, int block, const BatchLayout &lay, cudaStream_t st)
+static void launch_k(const KParams *cfg, const BatchPhase *ph, const BatchSep *sep, const BatchTask *tasks,
+                     const BatchLane *lanes, int ntasks, int *counter, int grid, int block, const BatchLayout &lay,
+                     cudaStream_t st)
 {
     auto k = mcig_batch_kernel<R, RNG, KAHAN>;
     const size_t smem = smem_k<R, RNG, KAHAN>(lay, block);
     if (smem > 48 * 1024) { cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); }
-    k<<<grid, block, smem, st>>>(cfg, ph, sep, tasks, ntasks, counter, lay);
+    k<<<grid, block, smem, st>>>(cfg, ph, sep, tasks, lanes, ntasks, counter, lay);
 }
 
 template <class R, int RNG, bool KAHAN>
@@ -332,17 +337,17 @@ static int blocks_per_sm_k(const BatchLayout &lay, int block)
 }
 
 void mcig_batch_launch(int prec, int rng, const KParams *cfg, const BatchPhase *ph, const BatchSep *sep,
-                       const BatchTask *tasks, int ntasks, int *counter, int grid, int block, int walk, int nslot,
-                       int nundo, cudaStream_t st)
+                       const BatchTask *tasks, const BatchLane *lanes, int ntasks, int *counter, int grid, int block,
+                       int walk, int nslot, int nundo, cudaStream_t st)
 {
     const BatchLayout lay{walk, nslot, nundo};
     if (prec == MCIG_PREC_FP64) {
-        if (rng == RNG_TAPE) { launch_k<double, RNG_TAPE, false>(cfg, ph, sep, tasks, ntasks, counter, grid, block, lay, st); }
-        else { launch_k<double, RNG_PHILOX, false>(cfg, ph, sep, tasks, ntasks, counter, grid, block, lay, st); }
+        if (rng == RNG_TAPE) { launch_k<double, RNG_TAPE, false>(cfg, ph, sep, tasks, lanes, ntasks, counter, grid, block, lay, st); }
+        else { launch_k<double, RNG_PHILOX, false>(cfg, ph, sep, tasks, lanes, ntasks, counter, grid, block, lay, st); }
     } else if (prec == MCIG_PREC_FP32) {
-        launch_k<float, RNG_PHILOX, true>(cfg, ph, sep, tasks, ntasks, counter, grid, block, lay, st);
+        launch_k<float, RNG_PHILOX, true>(cfg, ph, sep, tasks, lanes, ntasks, counter, grid, block, lay, st);
     } else {
-        launch_k<float, RNG_PHILOX, false>(cfg, ph, sep, tasks, ntasks, counter, grid, block, lay, st);
+        launch_k<float, RNG_PHILOX, false>(cfg, ph, sep, tasks, lanes, ntasks, counter, grid, block, lay, st);
     }
 }
 

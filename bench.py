@@ -223,7 +223,7 @@ def run_gpu(args):
         wall.append(t1 - t0)
         dev_ms.append(tm["calibration_ms"] + tm["burnin_ms"] + tm["sampling_ms"] + tm["estimation_ms"])
         kernel_ms.append(tm["sampling_ms"])
-        launches += tm["launches"]
+        launches += tm["launches"] + 1  # integrate's launches and setX's transpose of the walkers
     torch.cuda.synchronize()
     ck = clocks.stop()
 

@@ -167,9 +167,9 @@ template <> struct FastSlot<false> {
 // LEAN (1: uniform draws, 2: Gaussian draws): one step-size type and the unbound domain, so
 // the step of coordinate i is st[0] (times its 0 / 1 table entry) and the move's distribution
 // is known, without the code of the other types, of the other distribution and of the
-// periodic wrap (at the 16-D precision-matrix configuration 115 -> 95 -> 108 registers with
-// the compile-time distribution, and 13 % of the sampling time: the runtime choices are
-// compiled into predicated code that issues part of every alternative); 0: general
+// periodic wrap: the runtime choices are compiled into predicated code that issues part of
+// every alternative on every step (16-D precision-matrix configuration: sampling launch
+// 31.3 -> 27.0 ms); 0: general
 // FIXED4 (with MOMENTS): exactly one observable in each of the four groups (Full x.x, Full x,
 // Simple/Block x.x, Simple/Block x), every nskip 1 and ndim == MAXD: the observable step is one
 // straight-line block with no test of its layout
